@@ -1,0 +1,92 @@
+"""Parity oracle for the QMCToolsCL hot path.
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, by __graft_entry__.smoke() as
+the checker, and by bench.py for its CPU-baseline leg.  The product package
+(qmctoolscl_gb300) never imports this module.
+
+Two CPU implementations live here:
+
+* ``liboracle.so`` -- qmc_oracle.c, our C restatement of the reference C
+  backend (each function cites the reference file:line it follows).  Built by
+  ``make -C oracle``; it builds on any host with gcc, including the GPU machine.
+* ``_ref/c_lib.so`` -- the reference's own C sources compiled where they lie
+  (``make -C oracle ref``); only available where the reference checkout is.
+  Used to pin the restatement and to make the golden fixtures.
+
+Both are called with numpy arrays in the reference's argument order (without
+the batch-size arguments): ``oracle.call("lat_gen_gray", r, n, d, n_start,
+g, x)``.
+"""
+import ctypes
+import os
+import subprocess
+import threading
+
+import numpy as np
+
+from qmctoolscl_gb300._signatures import SIGNATURES
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ORACLE_SO = os.path.join(HERE, "_build", "liboracle.so")
+REF_SO = os.path.join(HERE, "_ref", "c_lib.so")
+
+_lock = threading.Lock()
+_libs = {}
+
+
+def build(ref=False):
+    """Compile the oracle (and, with ref=True, the reference C backend)."""
+    subprocess.run(["make", "-s", "-C", HERE] + (["ref"] if ref else []), check=True)
+
+
+def _argtype(kind):
+    if kind == "u64":
+        return ctypes.c_uint64
+    if kind == "u64*":
+        return np.ctypeslib.ndpointer(ctypes.c_uint64, flags="C_CONTIGUOUS")
+    return np.ctypeslib.ndpointer(ctypes.c_double, flags="C_CONTIGUOUS")
+
+
+def _load(path, prefix, with_bs):
+    lib = ctypes.CDLL(path)
+    funcs = {}
+    for name, (args, _outs) in SIGNATURES.items():
+        fn = getattr(lib, prefix + name)
+        types = [_argtype(k) for _a, k in args]
+        if with_bs:  # the reference repeats the three leading extents as batch sizes
+            types = types[:3] + [ctypes.c_uint64] * 3 + types[3:]
+        fn.argtypes = types
+        fn.restype = None
+        funcs[name] = fn
+    return funcs
+
+
+def oracle_lib():
+    with _lock:
+        if "oracle" not in _libs:
+            if not os.path.exists(ORACLE_SO):
+                build()
+            _libs["oracle"] = _load(ORACLE_SO, "oracle_", with_bs=False)
+        return _libs["oracle"]
+
+
+def ref_available():
+    return os.path.exists(REF_SO)
+
+
+def ref_lib():
+    with _lock:
+        if "ref" not in _libs:
+            _libs["ref"] = _load(REF_SO, "", with_bs=True)
+        return _libs["ref"]
+
+
+def call(name, *args):
+    """Run the oracle restatement of ``name`` in place on numpy arrays."""
+    oracle_lib()[name](*args)
+
+
+def call_ref(name, *args):
+    """Run the compiled reference C function ``name`` (bs_* set to the extents)."""
+    a = list(args)
+    ref_lib()[name](*(a[:3] + a[:3] + a[3:]))

@@ -1,0 +1,543 @@
+/*
+ * qmc_oracle.c -- CPU restatement of the QMCToolsCL point-generation and
+ * fast-transform C backend.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This file is the parity oracle: the GPU kernels
+ * of qmctoolscl_gb300 are checked against it, and bench.py times it as the
+ * CPU baseline ("port").  Nothing in the product library links, loads or
+ * calls it.
+ *
+ * Each function restates one reference function, named in its comment as
+ * qmctoolscl/c_funcs/<file>.c:<lines>.  Every function takes the reference's
+ * scalar arguments minus the three batch-size arguments (the reference's C
+ * wrapper sets them to the full extents, qmctoolscl/util.py:107, so every
+ * loop below runs over the whole range).  Loop order and the order of every
+ * floating-point operation follow the reference, because both decide the
+ * rounded results and the CPU timing.
+ *
+ * Build with -ffp-contract=off: aarch64 gcc would otherwise fuse a*b+c into
+ * an FMA and change the rounding of gdn_integer_to_float and the transforms.
+ *
+ * Shift counts.  Several reference loops shift a 64-bit word by a count that
+ * can reach 64 or wrap below zero for unusual arguments (undefined in C).
+ * gcc on x86-64 and aarch64 emits a hardware shift that uses the count mod
+ * 64; the oracle writes that behaviour out (SHL/SHR below) so it is defined.
+ */
+#include <math.h>
+#include <stdint.h>
+
+typedef uint64_t u64;
+
+#define SHL(v, s) ((u64)(v) << ((u64)(s) & 63u))
+#define SHR(v, s) ((u64)(v) >> ((u64)(s) & 63u))
+
+#if defined(__GNUC__)
+#define ORACLE_API __attribute__((visibility("default")))
+#else
+#define ORACLE_API
+#endif
+
+/* ------------------------------------------------------------------------ */
+/* rank-1 lattices                                                          */
+/* ------------------------------------------------------------------------ */
+
+/* qmctoolscl/c_funcs/lat_gen_linear.c:3-33 */
+ORACLE_API void oracle_lat_gen_linear(u64 r, u64 n, u64 d, const u64 *g, double *x)
+{
+    const double nd = (double)n;
+    for (u64 i = 0; i < n; i++) {
+        const double frac_i = i / nd;
+        for (u64 j = 0; j < d; j++)
+            for (u64 l = 0; l < r; l++)
+                x[l * n * d + i * d + j] = fmod((double)g[l * d + j] * frac_i, 1.0);
+    }
+}
+
+/* Shared start of the van der Corput recurrence of lat_gen_natural.c:23-34
+ * and lat_gen_gray.c:23-34: p = ceil(log2(n0+1)) bits, v = the Gray code of
+ * n0 written bit-reversed into p bits. */
+static void lat_vdc_start(u64 n0, u64 *p_out, u64 *v_out)
+{
+    u64 p = (u64)ceil(log2((double)n0 + 1));
+    u64 v = 0, t = n0 ^ (n0 >> 1), b = 0;
+    for (; t > 0; t >>= 1, b++)
+        if (t & 1) v += SHL(1, p - b - 1);
+    *p_out = p;
+    *v_out = v;
+}
+
+/* One step of lat_gen_natural.c:48-57 / lat_gen_gray.c:46-55: advance
+ * (p, v) from index itrue-1 to itrue. */
+static void lat_vdc_step(u64 itrue, u64 *p, u64 *v)
+{
+    if ((itrue & (itrue - 1)) == 0) { /* itrue is a power of two */
+        *p += 1;
+        *v <<= 1;
+    }
+    u64 b = 0;
+    while (!((itrue >> b) & 1)) b++;
+    *v ^= SHL(1, *p - b - 1);
+}
+
+/* qmctoolscl/c_funcs/lat_gen_natural.c:3-58 */
+ORACLE_API void oracle_lat_gen_natural(u64 r, u64 n, u64 d, u64 n_start, const u64 *g, double *x)
+{
+    u64 p, v;
+    lat_vdc_start(n_start, &p, &v);
+    for (u64 i = 0; i < n; i++) {
+        const double frac_i = ldexp((double)v, -(int)p);
+        const u64 itrue = i + n_start;
+        const u64 row = ((itrue ^ (itrue >> 1)) - n_start) * d;
+        for (u64 j = 0; j < d; j++)
+            for (u64 l = 0; l < r; l++)
+                x[l * n * d + row + j] = fmod((double)g[l * d + j] * frac_i, 1.0);
+        lat_vdc_step(i + n_start + 1, &p, &v);
+    }
+}
+
+/* qmctoolscl/c_funcs/lat_gen_gray.c:3-56 */
+ORACLE_API void oracle_lat_gen_gray(u64 r, u64 n, u64 d, u64 n_start, const u64 *g, double *x)
+{
+    u64 p, v;
+    lat_vdc_start(n_start, &p, &v);
+    for (u64 i = 0; i < n; i++) {
+        const double frac_i = ldexp((double)v, -(int)p);
+        for (u64 j = 0; j < d; j++)
+            for (u64 l = 0; l < r; l++)
+                x[l * n * d + i * d + j] = fmod((double)g[l * d + j] * frac_i, 1.0);
+        lat_vdc_step(i + n_start + 1, &p, &v);
+    }
+}
+
+/* qmctoolscl/c_funcs/lat_shift_mod_1.c:3-35 */
+ORACLE_API void oracle_lat_shift_mod_1(u64 r, u64 n, u64 d, u64 r_x, const double *x,
+                                       const double *shifts, double *xr)
+{
+    const u64 nelem_x = r_x * n * d;
+    for (u64 l = 0; l < r; l++)
+        for (u64 i = 0; i < n; i++)
+            for (u64 j = 0; j < d; j++) {
+                const u64 idx = l * n * d + i * d + j;
+                xr[idx] = fmod(x[idx % nelem_x] + shifts[l * d + j], 1.0);
+            }
+}
+
+/* ------------------------------------------------------------------------ */
+/* digital nets in base 2                                                   */
+/* ------------------------------------------------------------------------ */
+
+/* Shared body of dnb2_gen_natural.c:23-69 and dnb2_gen_gray.c:23-68.  The
+ * first point is the XOR of the columns picked by the bits of its Gray code;
+ * each later point flips the column picked by the lowest set bit of its
+ * index.  Natural order writes point i at row gray(i)-n_start, Gray order at
+ * row i-n_start. */
+static void dnb2_gen(u64 r, u64 n, u64 d, u64 n_start, u64 mmax, const u64 *C, u64 *xb,
+                     int natural)
+{
+    u64 itrue = n_start;
+    u64 t = itrue ^ (itrue >> 1);
+    u64 prev = natural ? (t - n_start) * d : 0;
+    if (n > 0) {
+        for (u64 j = 0; j < d; j++)
+            for (u64 l = 0; l < r; l++)
+                xb[l * n * d + prev + j] = 0;
+        for (u64 b = 0; t > 0; t >>= 1, b++)
+            if (t & 1)
+                for (u64 j = 0; j < d; j++)
+                    for (u64 l = 0; l < r; l++)
+                        xb[l * n * d + prev + j] ^= C[l * d * mmax + j * mmax + b];
+    }
+    for (u64 i = 1; i < n; i++) {
+        itrue = i + n_start;
+        const u64 cur = natural ? ((itrue ^ (itrue >> 1)) - n_start) * d : i * d;
+        u64 b = 0;
+        while (!((itrue >> b) & 1)) b++;
+        for (u64 j = 0; j < d; j++)
+            for (u64 l = 0; l < r; l++)
+                xb[l * n * d + cur + j] = xb[l * n * d + prev + j] ^ C[l * d * mmax + j * mmax + b];
+        prev = cur;
+    }
+}
+
+/* qmctoolscl/c_funcs/dnb2_gen_natural.c:3-70 */
+ORACLE_API void oracle_dnb2_gen_natural(u64 r, u64 n, u64 d, u64 n_start, u64 mmax, const u64 *C,
+                                        u64 *xb)
+{
+    dnb2_gen(r, n, d, n_start, mmax, C, xb, 1);
+}
+
+/* qmctoolscl/c_funcs/dnb2_gen_gray.c:3-69 */
+ORACLE_API void oracle_dnb2_gen_gray(u64 r, u64 n, u64 d, u64 n_start, u64 mmax, const u64 *C,
+                                     u64 *xb)
+{
+    dnb2_gen(r, n, d, n_start, mmax, C, xb, 0);
+}
+
+/* qmctoolscl/c_funcs/dnb2_digital_shift.c:3-36 */
+ORACLE_API void oracle_dnb2_digital_shift(u64 r, u64 n, u64 d, u64 r_x, const u64 *lshifts,
+                                          const u64 *xb, const u64 *shiftsb, u64 *xrb)
+{
+    const u64 nelem_x = r_x * n * d;
+    for (u64 l = 0; l < r; l++)
+        for (u64 i = 0; i < n; i++)
+            for (u64 j = 0; j < d; j++) {
+                const u64 idx = l * n * d + i * d + j;
+                xrb[idx] = SHL(xb[idx % nelem_x], lshifts[l % r_x]) ^ shiftsb[l * d + j];
+            }
+}
+
+/* qmctoolscl/c_funcs/dnb2_integer_to_float.c:3-32 */
+ORACLE_API void oracle_dnb2_integer_to_float(u64 r, u64 n, u64 d, const u64 *tmaxes, const u64 *xb,
+                                             double *x)
+{
+    for (u64 l = 0; l < r; l++)
+        for (u64 i = 0; i < n; i++)
+            for (u64 j = 0; j < d; j++) {
+                const u64 idx = l * n * d + i * d + j;
+                x[idx] = ldexp((double)xb[idx], -(int)tmaxes[l]);
+            }
+}
+
+/* qmctoolscl/c_funcs/dnb2_linear_matrix_scramble.c:3-51.  The parity of
+ * S-row AND C-column is counted bit by bit, as the reference does. */
+ORACLE_API void oracle_dnb2_linear_matrix_scramble(u64 r, u64 d, u64 mmax, u64 r_C, u64 tmax_new,
+                                                   const u64 *S, const u64 *C, u64 *C_lms)
+{
+    const u64 nelem_C = r_C * d * mmax;
+    for (u64 l = 0; l < r; l++)
+        for (u64 j = 0; j < d; j++)
+            for (u64 k = 0; k < mmax; k++) {
+                const u64 idx = l * d * mmax + j * mmax + k;
+                const u64 col = C[idx % nelem_C];
+                u64 out = 0;
+                for (u64 t = 0; t < tmax_new; t++) {
+                    u64 w = S[l * d * tmax_new + j * tmax_new + t] & col, ones = 0;
+                    for (; w; w &= w - 1) ones++;
+                    if (ones & 1) out += SHL(1, tmax_new - t - 1);
+                }
+                C_lms[idx] = out;
+            }
+}
+
+/* qmctoolscl/c_funcs/dnb2_interlace.c:3-45 */
+ORACLE_API void oracle_dnb2_interlace(u64 r, u64 d_alpha, u64 mmax, u64 d, u64 tmax, u64 tmax_alpha,
+                                      u64 alpha, const u64 *C, u64 *C_alpha)
+{
+    for (u64 l = 0; l < r; l++)
+        for (u64 ja = 0; ja < d_alpha; ja++)
+            for (u64 k = 0; k < mmax; k++) {
+                u64 out = 0;
+                for (u64 ta = 0; ta < tmax_alpha; ta++) {
+                    const u64 t = ta / alpha, j = ja * alpha + ta % alpha;
+                    if (SHR(C[l * d * mmax + j * mmax + k], tmax - t - 1) & 1)
+                        out += SHL(1, tmax_alpha - ta - 1);
+                }
+                C_alpha[l * d_alpha * mmax + ja * mmax + k] = out;
+            }
+}
+
+/* qmctoolscl/c_funcs/dnb2_undo_interlace.c:3-45 */
+ORACLE_API void oracle_dnb2_undo_interlace(u64 r, u64 d, u64 mmax, u64 d_alpha, u64 tmax,
+                                           u64 tmax_alpha, u64 alpha, const u64 *C_alpha, u64 *C)
+{
+    for (u64 l = 0; l < r; l++)
+        for (u64 j = 0; j < d; j++)
+            for (u64 k = 0; k < mmax; k++) {
+                u64 out = 0;
+                for (u64 t = 0; t < tmax; t++) {
+                    const u64 ja = j / alpha, ta = t * alpha + j % alpha;
+                    if (SHR(C_alpha[l * d_alpha * mmax + ja * mmax + k], tmax_alpha - ta - 1) & 1)
+                        out += SHL(1, tmax - t - 1);
+                }
+                C[l * d * mmax + j * mmax + k] = out;
+            }
+}
+
+/* qmctoolscl/c_funcs/dnb2_gmat_lsb_to_msb.c:3-44 */
+ORACLE_API void oracle_dnb2_gmat_lsb_to_msb(u64 r, u64 d, u64 mmax, const u64 *tmaxes,
+                                            const u64 *C_lsb, u64 *C_msb)
+{
+    for (u64 l = 0; l < r; l++) {
+        const u64 tmax = tmaxes[l];
+        for (u64 j = 0; j < d; j++)
+            for (u64 k = 0; k < mmax; k++) {
+                const u64 idx = l * d * mmax + j * mmax + k;
+                u64 v = C_lsb[idx], out = 0;
+                for (u64 t = 0; v != 0; v >>= 1, t++)
+                    if (v & 1) out += SHL(1, tmax - t - 1);
+                C_msb[idx] = out;
+            }
+    }
+}
+
+/* ------------------------------------------------------------------------ */
+/* generalized digital nets (per-dimension base b)                          */
+/* ------------------------------------------------------------------------ */
+
+/* qmctoolscl/c_funcs/gdn_gen_natural.c:3-53.  Digit k of the point index in
+ * base b scales column k; the running digit sums are reduced mod b after
+ * every column, in 64-bit unsigned arithmetic. */
+ORACLE_API void oracle_gdn_gen_natural(u64 r, u64 n, u64 d, u64 r_b, u64 mmax, u64 tmax,
+                                       u64 n_start, const u64 *bases, const u64 *C, u64 *xdig)
+{
+    for (u64 l = 0; l < r; l++)
+        for (u64 i = 0; i < n; i++) {
+            const u64 itrue = i + n_start;
+            for (u64 j = 0; j < d; j++) {
+                u64 *out = xdig + l * n * d * tmax + i * d * tmax + j * tmax;
+                for (u64 t = 0; t < tmax; t++) out[t] = 0;
+                const u64 b = bases[(l % r_b) * d + j];
+                u64 rest = itrue;
+                for (u64 k = 0; rest > 0; k++) {
+                    const u64 dig = rest % b;
+                    rest = (rest - dig) / b;
+                    if (dig > 0) {
+                        const u64 *col = C + l * d * mmax * tmax + j * mmax * tmax + k * tmax;
+                        for (u64 t = 0; t < tmax; t++) out[t] = (out[t] + dig * col[t]) % b;
+                    }
+                }
+            }
+        }
+}
+
+/* qmctoolscl/c_funcs/gdn_gen_natural_same_base.c:3-63 */
+ORACLE_API void oracle_gdn_gen_natural_same_base(u64 r, u64 n, u64 d, u64 mmax, u64 tmax,
+                                                 u64 n_start, u64 b, const u64 *C, u64 *xdig)
+{
+    for (u64 l = 0; l < r; l++)
+        for (u64 i = 0; i < n; i++)
+            for (u64 j = 0; j < d; j++)
+                for (u64 t = 0; t < tmax; t++)
+                    xdig[l * n * d * tmax + i * d * tmax + j * tmax + t] = 0;
+    for (u64 i = 0; i < n; i++) {
+        u64 rest = i + n_start;
+        for (u64 k = 0; rest > 0; k++) {
+            const u64 dig = rest % b;
+            rest = (rest - dig) / b;
+            if (dig == 0) continue;
+            for (u64 l = 0; l < r; l++)
+                for (u64 j = 0; j < d; j++) {
+                    u64 *out = xdig + l * n * d * tmax + i * d * tmax + j * tmax;
+                    const u64 *col = C + l * d * mmax * tmax + j * mmax * tmax + k * tmax;
+                    for (u64 t = 0; t < tmax; t++) out[t] = (out[t] + dig * col[t]) % b;
+                }
+        }
+    }
+}
+
+/* qmctoolscl/c_funcs/gdn_linear_matrix_scramble.c:3-46.  Each product is
+ * reduced mod b but the sum is not. */
+ORACLE_API void oracle_gdn_linear_matrix_scramble(u64 r, u64 d, u64 mmax, u64 r_C, u64 r_b,
+                                                  u64 tmax, u64 tmax_new, const u64 *bases,
+                                                  const u64 *S, const u64 *C, u64 *C_lms)
+{
+    for (u64 l = 0; l < r; l++)
+        for (u64 j = 0; j < d; j++) {
+            const u64 b = bases[(l % r_b) * d + j];
+            for (u64 k = 0; k < mmax; k++) {
+                const u64 *col = C + (l % r_C) * d * mmax * tmax + j * mmax * tmax + k * tmax;
+                u64 *out = C_lms + l * d * mmax * tmax_new + j * mmax * tmax_new + k * tmax_new;
+                for (u64 t = 0; t < tmax_new; t++) {
+                    const u64 *srow = S + l * d * tmax_new * tmax + j * tmax_new * tmax + t * tmax;
+                    u64 acc = 0;
+                    for (u64 c = 0; c < tmax; c++) acc += (srow[c] * col[c]) % b;
+                    out[t] = acc;
+                }
+            }
+        }
+}
+
+/* qmctoolscl/c_funcs/gdn_digital_permutation.c:3-46 */
+ORACLE_API void oracle_gdn_digital_permutation(u64 r, u64 n, u64 d, u64 r_x, u64 r_b, u64 tmax,
+                                               u64 tmax_new, u64 bmax, const u64 *perms,
+                                               const u64 *xdig, u64 *xdig_new)
+{
+    (void)r_b;
+    for (u64 l = 0; l < r; l++)
+        for (u64 i = 0; i < n; i++)
+            for (u64 j = 0; j < d; j++) {
+                const u64 *in = xdig + (l % r_x) * n * d * tmax + i * d * tmax + j * tmax;
+                u64 *out = xdig_new + l * n * d * tmax_new + i * d * tmax_new + j * tmax_new;
+                const u64 *perm = perms + l * d * tmax_new * bmax + j * tmax_new * bmax;
+                for (u64 t = 0; t < tmax; t++) out[t] = perm[t * bmax + in[t]];
+                for (u64 t = tmax; t < tmax_new; t++) out[t] = perm[t * bmax];
+            }
+}
+
+/* qmctoolscl/c_funcs/gdn_digital_shift.c:3-45 */
+ORACLE_API void oracle_gdn_digital_shift(u64 r, u64 n, u64 d, u64 r_x, u64 r_b, u64 tmax,
+                                         u64 tmax_new, const u64 *bases, const u64 *shifts,
+                                         const u64 *xdig, u64 *xdig_new)
+{
+    for (u64 l = 0; l < r; l++)
+        for (u64 i = 0; i < n; i++)
+            for (u64 j = 0; j < d; j++) {
+                const u64 *in = xdig + (l % r_x) * n * d * tmax + i * d * tmax + j * tmax;
+                u64 *out = xdig_new + l * n * d * tmax_new + i * d * tmax_new + j * tmax_new;
+                const u64 *sh = shifts + l * d * tmax_new + j * tmax_new;
+                const u64 b = bases[(l % r_b) * d + j];
+                for (u64 t = 0; t < tmax; t++) out[t] = (in[t] + sh[t]) % b;
+                for (u64 t = tmax; t < tmax_new; t++) out[t] = sh[t];
+            }
+}
+
+/* qmctoolscl/c_funcs/gdn_integer_to_float.c:3-43.  v += recip*digit and
+ * recip /= b, each rounded separately (no FMA). */
+ORACLE_API void oracle_gdn_integer_to_float(u64 r, u64 n, u64 d, u64 r_b, u64 tmax,
+                                            const u64 *bases, const u64 *xdig, double *x)
+{
+    for (u64 l = 0; l < r; l++)
+        for (u64 i = 0; i < n; i++)
+            for (u64 j = 0; j < d; j++) {
+                const u64 *in = xdig + l * n * d * tmax + i * d * tmax + j * tmax;
+                const double b = (double)bases[(l % r_b) * d + j];
+                double v = 0.0, recip = 1 / b;
+                for (u64 t = 0; t < tmax; t++) {
+                    v += recip * (double)in[t];
+                    recip /= b;
+                }
+                x[l * n * d + i * d + j] = v;
+            }
+}
+
+/* qmctoolscl/c_funcs/gdn_interlace.c:3-39 */
+ORACLE_API void oracle_gdn_interlace(u64 r, u64 d_alpha, u64 mmax, u64 d, u64 tmax, u64 tmax_alpha,
+                                     u64 alpha, const u64 *C, u64 *C_alpha)
+{
+    for (u64 l = 0; l < r; l++)
+        for (u64 ja = 0; ja < d_alpha; ja++)
+            for (u64 k = 0; k < mmax; k++)
+                for (u64 ta = 0; ta < tmax_alpha; ta++) {
+                    const u64 t = ta / alpha, j = ja * alpha + ta % alpha;
+                    C_alpha[l * d_alpha * mmax * tmax_alpha + ja * mmax * tmax_alpha +
+                            k * tmax_alpha + ta] = C[l * d * mmax * tmax + j * mmax * tmax + k * tmax + t];
+                }
+}
+
+/* qmctoolscl/c_funcs/gdn_undo_interlace.c:3-39 */
+ORACLE_API void oracle_gdn_undo_interlace(u64 r, u64 d, u64 mmax, u64 d_alpha, u64 tmax,
+                                          u64 tmax_alpha, u64 alpha, const u64 *C_alpha, u64 *C)
+{
+    for (u64 l = 0; l < r; l++)
+        for (u64 j = 0; j < d; j++)
+            for (u64 k = 0; k < mmax; k++)
+                for (u64 t = 0; t < tmax; t++) {
+                    const u64 ja = j / alpha, ta = t * alpha + j % alpha;
+                    C[l * d * mmax * tmax + j * mmax * tmax + k * tmax + t] =
+                        C_alpha[l * d_alpha * mmax * tmax_alpha + ja * mmax * tmax_alpha +
+                                k * tmax_alpha + ta];
+                }
+}
+
+/* ------------------------------------------------------------------------ */
+/* fast transforms along the last axis (length n = 2*n_half)                */
+/* ------------------------------------------------------------------------ */
+
+/* Twiddle table of fft_bro_1d_radix2.c:32-42 (sign -1) and
+ * ifft_bro_1d_radix2.c:32-42 (sign +1): angle sign*2*pi*t/n, evaluated
+ * left to right as the reference writes it. */
+static void fill_twiddles(u64 n, double sign, double *twr, double *twi)
+{
+    const double PI = acos(-1.);
+    for (u64 t = 0; t < n; t++) {
+        const double ang = sign * 2 * PI * t / n;
+        twr[t] = cos(ang);
+        twi[t] = sin(ang);
+    }
+}
+
+/* Partner indices of one butterfly (fft_bro_1d_radix2.c:50-57): the
+ * n_half work items each own the pair (i1, i1 + f) whose i1 has bit `bit`
+ * clear; items with that bit set take the pair in the upper half. */
+static void pair_of(u64 i, u64 n_half, u64 f, u64 bit, u64 *i1, u64 *i2)
+{
+    if ((i >> bit) & 1) {
+        *i2 = i + n_half;
+        *i1 = *i2 ^ f;
+    } else {
+        *i1 = i;
+        *i2 = i ^ f;
+    }
+}
+
+/* qmctoolscl/c_funcs/fft_bro_1d_radix2.c:3-80 (decimation in time,
+ * bit-reversed input, natural output, 1/sqrt(2) per stage). */
+ORACLE_API void oracle_fft_bro_1d_radix2(u64 d1, u64 d2, u64 n_half, double *twr, double *twi,
+                                         double *xr, double *xi)
+{
+    const u64 n = 2 * n_half, m = (u64)log2((double)n);
+    const double sqrt2 = sqrt(2.0);
+    fill_twiddles(n, -1.0, twr, twi);
+    for (u64 k = 0; k < m; k++) {
+        const u64 s = m - k - 1, f = SHL(1, k);
+        for (u64 i = 0; i < n_half; i++) {
+            u64 i1, i2;
+            pair_of(i, n_half, f, k, &i1, &i2);
+            const u64 t = (i1 % f) * SHL(1, s);
+            const double c = twr[t], sn = twi[t];
+            for (u64 j1 = 0; j1 < d1; j1++)
+                for (u64 j2 = 0; j2 < d2; j2++) {
+                    const u64 base = j1 * d2 * n + j2 * n;
+                    const double ar = xr[base + i1], br = xr[base + i2];
+                    const double ai = xi[base + i1], bi = xi[base + i2];
+                    const double yr = br * c - bi * sn;
+                    const double yi = br * sn + bi * c;
+                    xr[base + i1] = (ar + yr) / sqrt2;
+                    xi[base + i1] = (ai + yi) / sqrt2;
+                    xr[base + i2] = (ar - yr) / sqrt2;
+                    xi[base + i2] = (ai - yi) / sqrt2;
+                }
+        }
+    }
+}
+
+/* qmctoolscl/c_funcs/ifft_bro_1d_radix2.c:3-81 (decimation in frequency,
+ * natural input, bit-reversed output, 1/sqrt(2) per stage). */
+ORACLE_API void oracle_ifft_bro_1d_radix2(u64 d1, u64 d2, u64 n_half, double *twr, double *twi,
+                                          double *xr, double *xi)
+{
+    const u64 n = 2 * n_half, m = (u64)log2((double)n);
+    const double sqrt2 = sqrt(2.0);
+    fill_twiddles(n, 1.0, twr, twi);
+    for (u64 k = 0; k < m; k++) {
+        const u64 s = m - k - 1, f = SHL(1, s);
+        for (u64 i = 0; i < n_half; i++) {
+            u64 i1, i2;
+            pair_of(i, n_half, f, s, &i1, &i2);
+            const u64 t = (i1 % f) * SHL(1, k);
+            const double c = twr[t], sn = twi[t];
+            for (u64 j1 = 0; j1 < d1; j1++)
+                for (u64 j2 = 0; j2 < d2; j2++) {
+                    const u64 base = j1 * d2 * n + j2 * n;
+                    const double ar = xr[base + i1], br = xr[base + i2];
+                    const double ai = xi[base + i1], bi = xi[base + i2];
+                    const double yr = ar - br, yi = ai - bi;
+                    xr[base + i1] = (ar + br) / sqrt2;
+                    xi[base + i1] = (ai + bi) / sqrt2;
+                    xr[base + i2] = (yr * c - yi * sn) / sqrt2;
+                    xi[base + i2] = (yr * sn + yi * c) / sqrt2;
+                }
+        }
+    }
+}
+
+/* qmctoolscl/c_funcs/fwht_1d_radix2.c:3-53 */
+ORACLE_API void oracle_fwht_1d_radix2(u64 d1, u64 d2, u64 n_half, double *x)
+{
+    const u64 n = 2 * n_half, m = (u64)log2((double)n);
+    const double sqrt2 = sqrt(2.0);
+    for (u64 k = 0; k < m; k++) {
+        const u64 s = m - k - 1, f = SHL(1, s);
+        for (u64 i = 0; i < n_half; i++) {
+            u64 i1, i2;
+            pair_of(i, n_half, f, s, &i1, &i2);
+            for (u64 j1 = 0; j1 < d1; j1++)
+                for (u64 j2 = 0; j2 < d2; j2++) {
+                    const u64 base = j1 * d2 * n + j2 * n;
+                    const double a = x[base + i1], b = x[base + i2];
+                    x[base + i1] = (a + b) / sqrt2;
+                    x[base + i2] = (a - b) / sqrt2;
+                }
+        }
+    }
+}
