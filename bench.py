@@ -1,0 +1,389 @@
+#!/usr/bin/env python
+"""Benchmark of the QMCToolsCL hot path on GB300.
+
+Default workload (the headline configuration): rank-1 lattice in Gray order
+plus a uniform random shift mod 1, r = 16 randomisations, n = 2^20 points,
+d = 64 dimensions, float64 output (8 GiB per step), generating vector of
+odd integers in [1, 2^20) and shifts U[0,1), both seeded
+(np.random.SFC64(2)).  One step = one pass of the path over that batch:
+
+  value  -- the fused batched kernel (qmc_lat_gen_shift: generation + shift in
+            one launch, writes only the shifted points), inputs resident in HBM,
+            timed with CUDA events on the launching stream;
+  plain  -- the reference's two calls (lat_gen_gray then lat_shift_mod_1) as
+            two launches with the intermediate array in HBM;
+  e2e    -- the public API with host numpy buffers: host->device copy of the
+            inputs, the kernel, device->host copy of the 8 GiB result into
+            pinned host memory, every step.
+
+The output (8 GiB) is far larger than L2 (129 MB), so no flush is needed
+between steps.  cpu_baseline times the oracle (a C restatement of the
+reference C backend) over all host cores on a sample of the same workload.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+--impl reference times the reference's CPU implementation (the oracle port;
+the reference's own compiled backend is not available on the GPU host) on
+the same metric and workload.  Under torchrun (N>1) every rank runs its own
+replica of the workload (weak scaling, no data exchange); rank 0 prints.
+"""
+import argparse
+import concurrent.futures
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+
+METRIC = "points/s + % HBM roofline, batched vs plain on 1 GB300; FFT Gsamples/s @≤1e-6 err"
+R, LOG2N, D = 16, 20, 64
+PROFILE_LOG2N = 16  # --small: the same kernel on 512 MiB of output, for ncu captures
+SEED = 2
+FALLBACK_HBM_GBS = 6800.0
+
+
+def workload_inputs(seed=SEED):
+    import qmctoolscl_gb300 as q
+    rng = np.random.Generator(np.random.SFC64(seed))
+    g = (rng.integers(0, 1 << 19, (R, D)) * 2 + 1).astype(np.uint64)
+    shifts = q.lat_get_shifts(rng, R, D)
+    return g, shifts
+
+
+# ---------------------------------------------------------------- CPU side
+
+def cpu_pipeline(g, shifts, n, threads):
+    """The reference pipeline (Gray-order lattice, then shift mod 1) run by
+    the oracle, one randomisation per task over `threads` host threads."""
+    import oracle
+    U = np.uint64
+    x = np.empty((R, n, D))
+    xr = np.empty((R, n, D))
+
+    def one(l):
+        oracle.call("lat_gen_gray", U(1), U(n), U(D), U(0), np.ascontiguousarray(g[l:l + 1]), x[l:l + 1])
+        oracle.call("lat_shift_mod_1", U(1), U(n), U(D), U(1), x[l:l + 1], np.ascontiguousarray(shifts[l:l + 1]),
+                    xr[l:l + 1])
+
+    t0 = time.perf_counter()
+    with concurrent.futures.ThreadPoolExecutor(max_workers=threads) as ex:
+        list(ex.map(one, range(R)))
+    return time.perf_counter() - t0, xr
+
+
+def host_threads():
+    try:
+        return len(os.sched_getaffinity(0))
+    except AttributeError:
+        return os.cpu_count() or 1
+
+
+CPU_SAMPLE_LOG2N = 18
+
+
+def cpu_baseline(g, shifts):
+    import oracle
+    oracle.oracle_lib()
+    threads = host_threads()
+    n = 1 << CPU_SAMPLE_LOG2N
+    cpu_pipeline(g, shifts, 1 << 12, threads)  # warm the page cache / thread pool
+    t, _ = cpu_pipeline(g, shifts, n, threads)
+    return {"value": R * n / t, "unit": "points/s", "cores": threads, "kind": "port",
+            "sample": "r=16, n=2^%d (first quarter of the rows), d=64; lat_gen_gray then lat_shift_mod_1 by the "
+                      "oracle (C restatement of the reference C backend, gcc -O2 -ffp-contract=off), one "
+                      "randomisation per thread" % CPU_SAMPLE_LOG2N,
+            "seconds": t}
+
+
+# ---------------------------------------------------------------- clocks
+
+class ClockSampler:
+    FIELDS = ["index", "clocks.sm", "clocks.max.sm", "power.draw", "clocks_event_reasons.active",
+              "clocks_event_reasons.hw_slowdown", "clocks_event_reasons.hw_thermal_slowdown",
+              "clocks_event_reasons.sw_thermal_slowdown", "clocks_event_reasons.sw_power_cap"]
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + ",".join(self.FIELDS),
+                 "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.thread.join(timeout=2)
+        rows = []
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) != len(self.FIELDS):
+                continue
+            try:
+                rows.append({"sm": float(parts[1]), "max": float(parts[2]), "pw": float(parts[3]),
+                             "hw": parts[5], "hwt": parts[6], "swt": parts[7], "pcap": parts[8]})
+            except ValueError:
+                continue
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        pmax = max(r_["pw"] for r_ in rows)
+        load = [r_ for r_ in rows if r_["pw"] >= 0.5 * pmax] or rows
+        reasons = set()
+        for r_ in load:
+            for key, name in (("hw", "hw_slowdown"), ("hwt", "hw_thermal_slowdown"),
+                              ("swt", "sw_thermal_slowdown"), ("pcap", "sw_power_cap")):
+                if r_[key].lower().startswith("active"):
+                    reasons.add(name)
+        return {"sm_mhz": float(np.median([r_["sm"] for r_ in load])), "sm_max_mhz": max(r_["max"] for r_ in rows),
+                "reasons": sorted(reasons), "samples_under_load": len(load), "power_w_max": pmax}
+
+
+# ---------------------------------------------------------------- helpers
+
+def measured_peak():
+    path = os.path.join(HERE, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            pk = json.load(f)
+        return float(pk["hbm_gbs"]), "measured (MEASURED_PEAKS.json hbm_gbs)"
+    except (OSError, KeyError, ValueError):
+        return FALLBACK_HBM_GBS, "fallback 6.8 TB/s"
+
+
+def profiled_traffic(name):
+    """dram read+write bytes per launch of `name` from the committed ncu summary."""
+    path = os.path.join(HERE, "profiles", name)
+    try:
+        with open(path) as f:
+            for ln in f:
+                if ln.startswith("traffic_bytes_per_launch:"):
+                    return float(ln.split(":", 1)[1].split()[0])
+    except OSError:
+        pass
+    return None
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    return world, rank, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(v, world):
+    if world == 1:
+        return v
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([v], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+# ---------------------------------------------------------------- arms
+
+def run_reference(args):
+    world, rank, _local = int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("RANK", "0")), 0
+    if rank != 0:
+        return
+    import oracle
+    oracle.oracle_lib()
+    g, shifts = workload_inputs()
+    threads = host_threads()
+    n = 1 << CPU_SAMPLE_LOG2N
+    for _ in range(args.warmup):
+        cpu_pipeline(g, shifts, n, threads)
+    times = []
+    for _ in range(args.steps):
+        t, _ = cpu_pipeline(g, shifts, n, threads)
+        times.append(t)
+    ms = 1e3 * float(np.mean(times))
+    value = R * n / (ms / 1e3)
+    line = {"metric": METRIC, "value": value, "unit": "points/s", "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded np.random.SFC64(2))",
+            "impl": "reference",
+            "config": {"workload": "rank-1 lattice Gray order + shift mod 1, r=16, n=2^20, d=64 "
+                                   "(each step: the first 2^%d rows)" % CPU_SAMPLE_LOG2N,
+                       "r": R, "n": 1 << LOG2N, "d": D, "n_sample": n},
+            "cpu_baseline": {"value": value, "unit": "points/s", "cores": threads, "kind": "port",
+                             "sample": "r=16, n=2^%d, d=64 per step, one randomisation per thread"
+                                       % CPU_SAMPLE_LOG2N},
+            "e2e": {"value": value, "unit": "points/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args):
+    import torch
+    world, rank, local = dist_setup()
+    torch.cuda.set_device(local)
+    from qmctoolscl_gb300 import _ffi, batch
+    lib = _ffi.lib()
+    n = 1 << (PROFILE_LOG2N if args.small else LOG2N)
+    g, shifts = workload_inputs(SEED + 1000 * rank)
+    dev = torch.device("cuda", local)
+    stream = torch.cuda.current_stream(dev)
+    h = stream.cuda_stream
+    g_d = torch.from_numpy(g.view(np.int64)).to(dev)
+    s_d = torch.from_numpy(shifts).to(dev)
+    xr_d = torch.empty((R, n, D), dtype=torch.float64, device=dev)
+
+    def fused():
+        _ffi.check(lib.qmc_lat_gen_shift(R, n, D, 0, 1, g_d.data_ptr(), s_d.data_ptr(), xr_d.data_ptr(), h),
+                   "lat_gen_shift")
+
+    # parity spot check of this very launch configuration against the oracle
+    fused()
+    torch.cuda.synchronize()
+    _, xr_sample = cpu_pipeline(g, shifts, 1 << 10, host_threads())
+    assert np.array_equal(xr_d[:, :1 << 10].cpu().numpy().view(np.uint64), xr_sample.view(np.uint64)), \
+        "fused kernel output differs from the oracle"
+
+    clocks = ClockSampler(local)
+    clocks.start()
+    for _ in range(args.warmup):
+        fused()
+    torch.cuda.synchronize()
+    barrier(world)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        fused()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    barrier(world)
+    ms_fused = e0.elapsed_time(e1) / args.steps
+    ms_fused_max = max_over_ranks(ms_fused, world)
+    if args.small:  # profiling mode: the fused kernel only
+        clocks.stop()
+        if rank == 0:
+            print(json.dumps({"small": True, "n": n, "ms_per_step": ms_fused_max,
+                              "gbs": 8.0 * R * n * D / (ms_fused_max / 1e3) / 1e9}), flush=True)
+        return
+
+    # plain: the reference's two calls as two launches
+    x_d = torch.empty((R, n, D), dtype=torch.float64, device=dev)
+
+    def plain():
+        _ffi.check(lib.qmc_lat_gen_gray(R, n, D, 0, g_d.data_ptr(), x_d.data_ptr(), h), "lat_gen_gray")
+        _ffi.check(lib.qmc_lat_shift_mod_1(R, n, D, R, x_d.data_ptr(), s_d.data_ptr(), xr_d.data_ptr(), h),
+                   "lat_shift_mod_1")
+
+    for _ in range(args.warmup):
+        plain()
+    torch.cuda.synchronize()
+    barrier(world)
+    p0, p1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    p0.record(stream)
+    for _ in range(args.steps):
+        plain()
+    p1.record(stream)
+    torch.cuda.synchronize()
+    barrier(world)
+    ms_plain = max_over_ranks(p0.elapsed_time(p1) / args.steps, world)
+    clk = clocks.stop()
+    del x_d
+
+    # e2e: public API, host numpy buffers (pinned output), copies in the timed region
+    xr_host_t = torch.empty((R, n, D), dtype=torch.float64, pin_memory=True)
+    xr_host = xr_host_t.numpy()
+    e2e_steps = max(1, min(args.steps, 5))
+    batch.lattice_gen_shift(R, n, D, 0, g, shifts, xr_host, order="gray")  # warm-up
+    torch.cuda.synchronize()
+    barrier(world)
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        A = batch.lattice_gen_shift(R, n, D, 0, g, shifts, xr_host, order="gray")
+    torch.cuda.synchronize()
+    t_e2e = max_over_ranks((time.perf_counter() - t0) / e2e_steps, world)
+    assert np.array_equal(xr_host[:, :1 << 10].view(np.uint64), xr_sample.view(np.uint64))
+
+    if rank != 0:
+        return
+    points = R * n
+    value = world * points / (ms_fused_max / 1e3)
+    peak, peak_src = measured_peak()
+    alg_bytes = 8.0 * R * n * D  # each coordinate written once as a float64
+    achieved = alg_bytes / (ms_fused / 1e3) / 1e9
+    traffic = profiled_traffic("lat_gen_shift_kernel_r16_n2p20_d64.md")
+    line = {
+        "metric": METRIC, "value": value, "unit": "points/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_fused_max, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded np.random.SFC64(2); odd g in [1,2^20), "
+                                                     "shifts U[0,1))",
+        "config": {"workload": "rank-1 lattice Gray order + shift mod 1, r=16, n=2^20, d=64 (fused batched kernel)",
+                   "r": R, "n": n, "d": D, "points_per_step": points, "coords_per_step": points * D,
+                   "l2": "8 GiB output per step >> 129 MB L2, no flush needed", "parallelism":
+                   "replicas" if world > 1 else "1 GPU"},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": traffic, "peak_source": peak_src,
+                     "kernel": "lat_gen_kernel<ORDER_GRAY,SHIFT> (qmc_lat_gen_shift)",
+                     "alg_bytes_per_launch": alg_bytes},
+        "plain": {"ms_per_step": ms_plain, "points_per_s": world * points / (ms_plain / 1e3), "launches_per_step": 2,
+                  "alg_bytes_per_step": 24.0 * R * n * D,
+                  "achieved_gbs": 24.0 * R * n * D / (ms_plain / 1e3) / 1e9,
+                  "fused_speedup": ms_plain / ms_fused_max},
+        "e2e": {"value": world * points / t_e2e, "unit": "points/s", "h2d_bytes_per_step": A.h2d_bytes,
+                "d2h_bytes_per_step": A.d2h_bytes, "steps": e2e_steps, "ms_per_step": 1e3 * t_e2e,
+                "path": "qmctoolscl_gb300.batch.lattice_gen_shift with numpy inputs, pinned numpy output"},
+        "gpu_launches": args.steps,
+        "clocks": clk,
+        "cpu_baseline": cpu_baseline(g, shifts),
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--small", action="store_true",
+                    help="profiling mode: the fused kernel only, on n=2^%d (512 MiB output)" % PROFILE_LOG2N)
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

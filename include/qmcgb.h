@@ -1,0 +1,175 @@
+/*
+ * qmcgb.h -- C ABI of libqmcgb.so, the GB300 (sm_103a) implementation of the
+ * QMCToolsCL point-generation and fast-transform hot path.
+ *
+ * One entry point per reference C function.  Each takes the reference's
+ * scalar arguments in the reference's order WITHOUT the three batch-size
+ * arguments bs_r/bs_n/bs_d (the reference's C wrapper sets them to the full
+ * extents, qmctoolscl/util.py:107), then the reference's arrays as DEVICE
+ * pointers, then a CUDA stream.  Array layouts are the reference's:
+ * C-contiguous in the order of the size strings of the reference comments
+ * (e.g. x is r*n*d with d fastest).  Outputs are written in place; the
+ * transforms work in place and also fill both twiddle arrays.
+ *
+ * Every call is stream-ordered and asynchronous, allocates nothing, keeps no
+ * host state between calls and is safe to call from several host threads.
+ * It returns QMC_OK or a negative status; qmc_last_error() gives the
+ * message for the calling thread.
+ *
+ * Where the reference's behaviour is undefined (shift counts >= 64 in C,
+ * reads past an array) the kernels follow what gcc builds of the reference
+ * do on x86-64 and aarch64 (shift counts mod 64) or report QMC_ERR_DOMAIN.
+ */
+#ifndef QMCGB_H
+#define QMCGB_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef void *qmc_stream_t; /* a cudaStream_t; NULL is the legacy default stream */
+
+enum qmc_status {
+    QMC_OK = 0,
+    QMC_ERR_ARG = -1,    /* bad size, null pointer or unsupported argument combination */
+    QMC_ERR_DOMAIN = -2, /* arguments for which the reference's result is undefined */
+    QMC_ERR_CUDA = -3,   /* a CUDA runtime or launch error */
+    QMC_ERR_DEVICE = -4  /* a kernel met an index the reference would read out of its array */
+};
+
+/* message of the last failing call on this host thread ("" if none) */
+const char *qmc_last_error(void);
+/* ABI version: major*10000 + minor*100 + patch */
+int qmc_version(void);
+/* clears the device error word on stream s */
+int qmc_device_error_reset(qmc_stream_t s);
+/* synchronises s, then returns QMC_ERR_DEVICE (and clears the word) if a
+ * kernel recorded an out-of-array index since the last reset */
+int qmc_device_error_check(qmc_stream_t s);
+
+/* ---- rank-1 lattices ---------------------------------------------------- */
+
+/* qmctoolscl/c_funcs/lat_gen_linear.c:3-13: x[l,i,j] = fmod(g[l,j]*(i/n), 1) */
+int qmc_lat_gen_linear(uint64_t r, uint64_t n, uint64_t d, const uint64_t *g, double *x,
+                       qmc_stream_t s);
+/* qmctoolscl/c_funcs/lat_gen_natural.c:3-14: x[l,k,j] = fmod(g[l,j]*vdc(n_start+k), 1);
+ * n_start and n_start+n must be 0 or powers of two (qmctoolscl/util.py:84-86) */
+int qmc_lat_gen_natural(uint64_t r, uint64_t n, uint64_t d, uint64_t n_start, const uint64_t *g,
+                        double *x, qmc_stream_t s);
+/* qmctoolscl/c_funcs/lat_gen_gray.c:3-14: x[l,i,j] = fmod(g[l,j]*vdc(gray(n_start+i)), 1) */
+int qmc_lat_gen_gray(uint64_t r, uint64_t n, uint64_t d, uint64_t n_start, const uint64_t *g,
+                     double *x, qmc_stream_t s);
+/* qmctoolscl/c_funcs/lat_shift_mod_1.c:3-15: xr[l,i,j] = fmod(x[l%r_x,i,j]+shifts[l,j], 1) */
+int qmc_lat_shift_mod_1(uint64_t r, uint64_t n, uint64_t d, uint64_t r_x, const double *x,
+                        const double *shifts, double *xr, qmc_stream_t s);
+
+/* ---- digital nets in base 2 --------------------------------------------- */
+
+/* qmctoolscl/c_funcs/dnb2_gen_natural.c:3-15; [n_start, n_start+n) must map onto
+ * itself under the Gray code and n_start+n <= 2^mmax */
+int qmc_dnb2_gen_natural(uint64_t r, uint64_t n, uint64_t d, uint64_t n_start, uint64_t mmax,
+                         const uint64_t *C, uint64_t *xb, qmc_stream_t s);
+/* qmctoolscl/c_funcs/dnb2_gen_gray.c:3-15; gray(n_start+n-1) < 2^mmax */
+int qmc_dnb2_gen_gray(uint64_t r, uint64_t n, uint64_t d, uint64_t n_start, uint64_t mmax,
+                      const uint64_t *C, uint64_t *xb, qmc_stream_t s);
+/* qmctoolscl/c_funcs/dnb2_digital_shift.c:3-16 */
+int qmc_dnb2_digital_shift(uint64_t r, uint64_t n, uint64_t d, uint64_t r_x,
+                           const uint64_t *lshifts, const uint64_t *xb, const uint64_t *shiftsb,
+                           uint64_t *xrb, qmc_stream_t s);
+/* qmctoolscl/c_funcs/dnb2_integer_to_float.c:3-14 */
+int qmc_dnb2_integer_to_float(uint64_t r, uint64_t n, uint64_t d, const uint64_t *tmaxes,
+                              const uint64_t *xb, double *x, qmc_stream_t s);
+/* qmctoolscl/c_funcs/dnb2_linear_matrix_scramble.c:3-16 */
+int qmc_dnb2_linear_matrix_scramble(uint64_t r, uint64_t d, uint64_t mmax, uint64_t r_C,
+                                    uint64_t tmax_new, const uint64_t *S, const uint64_t *C,
+                                    uint64_t *C_lms, qmc_stream_t s);
+/* qmctoolscl/c_funcs/dnb2_interlace.c:3-17 */
+int qmc_dnb2_interlace(uint64_t r, uint64_t d_alpha, uint64_t mmax, uint64_t d, uint64_t tmax,
+                       uint64_t tmax_alpha, uint64_t alpha, const uint64_t *C, uint64_t *C_alpha,
+                       qmc_stream_t s);
+/* qmctoolscl/c_funcs/dnb2_undo_interlace.c:3-17 */
+int qmc_dnb2_undo_interlace(uint64_t r, uint64_t d, uint64_t mmax, uint64_t d_alpha, uint64_t tmax,
+                            uint64_t tmax_alpha, uint64_t alpha, const uint64_t *C_alpha,
+                            uint64_t *C, qmc_stream_t s);
+/* qmctoolscl/c_funcs/dnb2_gmat_lsb_to_msb.c:3-14 */
+int qmc_dnb2_gmat_lsb_to_msb(uint64_t r, uint64_t d, uint64_t mmax, const uint64_t *tmaxes,
+                             const uint64_t *C_lsb, uint64_t *C_msb, qmc_stream_t s);
+
+/* ---- generalized digital nets (base b per dimension) -------------------- */
+
+/* qmctoolscl/c_funcs/gdn_gen_natural.c:3-18 */
+int qmc_gdn_gen_natural(uint64_t r, uint64_t n, uint64_t d, uint64_t r_b, uint64_t mmax,
+                        uint64_t tmax, uint64_t n_start, const uint64_t *bases, const uint64_t *C,
+                        uint64_t *xdig, qmc_stream_t s);
+/* qmctoolscl/c_funcs/gdn_gen_natural_same_base.c:3-17 */
+int qmc_gdn_gen_natural_same_base(uint64_t r, uint64_t n, uint64_t d, uint64_t mmax, uint64_t tmax,
+                                  uint64_t n_start, uint64_t b, const uint64_t *C, uint64_t *xdig,
+                                  qmc_stream_t s);
+/* qmctoolscl/c_funcs/gdn_linear_matrix_scramble.c:3-19 */
+int qmc_gdn_linear_matrix_scramble(uint64_t r, uint64_t d, uint64_t mmax, uint64_t r_C,
+                                   uint64_t r_b, uint64_t tmax, uint64_t tmax_new,
+                                   const uint64_t *bases, const uint64_t *S, const uint64_t *C,
+                                   uint64_t *C_lms, qmc_stream_t s);
+/* qmctoolscl/c_funcs/gdn_digital_permutation.c:3-19; a digit >= bmax reads
+ * the flat entry the reference reads while that entry lies inside perms
+ * (r*d*tmax_new*bmax elements); beyond it the kernel writes 0 and records
+ * QMC_ERR_DEVICE for qmc_device_error_check */
+int qmc_gdn_digital_permutation(uint64_t r, uint64_t n, uint64_t d, uint64_t r_x, uint64_t r_b,
+                                uint64_t tmax, uint64_t tmax_new, uint64_t bmax,
+                                const uint64_t *perms, const uint64_t *xdig, uint64_t *xdig_new,
+                                qmc_stream_t s);
+/* qmctoolscl/c_funcs/gdn_digital_shift.c:3-19 */
+int qmc_gdn_digital_shift(uint64_t r, uint64_t n, uint64_t d, uint64_t r_x, uint64_t r_b,
+                          uint64_t tmax, uint64_t tmax_new, const uint64_t *bases,
+                          const uint64_t *shifts, const uint64_t *xdig, uint64_t *xdig_new,
+                          qmc_stream_t s);
+/* qmctoolscl/c_funcs/gdn_integer_to_float.c:3-16 */
+int qmc_gdn_integer_to_float(uint64_t r, uint64_t n, uint64_t d, uint64_t r_b, uint64_t tmax,
+                             const uint64_t *bases, const uint64_t *xdig, double *x,
+                             qmc_stream_t s);
+/* qmctoolscl/c_funcs/gdn_interlace.c:3-17 */
+int qmc_gdn_interlace(uint64_t r, uint64_t d_alpha, uint64_t mmax, uint64_t d, uint64_t tmax,
+                      uint64_t tmax_alpha, uint64_t alpha, const uint64_t *C, uint64_t *C_alpha,
+                      qmc_stream_t s);
+/* qmctoolscl/c_funcs/gdn_undo_interlace.c:3-17 */
+int qmc_gdn_undo_interlace(uint64_t r, uint64_t d, uint64_t mmax, uint64_t d_alpha, uint64_t tmax,
+                           uint64_t tmax_alpha, uint64_t alpha, const uint64_t *C_alpha,
+                           uint64_t *C, qmc_stream_t s);
+
+/* ---- fast transforms along the last axis, n = 2*n_half a power of two -- */
+
+/* qmctoolscl/c_funcs/fft_bro_1d_radix2.c:3-17: orthonormal DFT of
+ * bit-reversed input, natural-order output, in place; fills twiddler/twiddlei[0:n] */
+int qmc_fft_bro_1d_radix2(uint64_t d1, uint64_t d2, uint64_t n_half, double *twiddler,
+                          double *twiddlei, double *xr, double *xi, qmc_stream_t s);
+/* qmctoolscl/c_funcs/ifft_bro_1d_radix2.c:3-17: the inverse (natural in,
+ * bit-reversed out) */
+int qmc_ifft_bro_1d_radix2(uint64_t d1, uint64_t d2, uint64_t n_half, double *twiddler,
+                           double *twiddlei, double *xr, double *xi, qmc_stream_t s);
+/* qmctoolscl/c_funcs/fwht_1d_radix2.c:3-14: orthonormal Walsh-Hadamard, in place */
+int qmc_fwht_1d_radix2(uint64_t d1, uint64_t d2, uint64_t n_half, double *x, qmc_stream_t s);
+
+/* ---- fused pipelines (no single reference counterpart) -------------------
+ * Each equals a chain of reference calls, bit for bit, in one kernel. */
+
+/* qmctoolscl/c_funcs/lat_gen_natural.c:3-58 (gray=0) or lat_gen_gray.c:3-56
+ * (gray=1), followed by lat_shift_mod_1.c:3-35 with r_x = r: writes only xr
+ * (r*n*d), never the unshifted points */
+int qmc_lat_gen_shift(uint64_t r, uint64_t n, uint64_t d, uint64_t n_start, int gray, const uint64_t *g,
+                      const double *shifts, double *xr, qmc_stream_t s);
+/* dnb2_gen_natural / dnb2_gen_gray (qmctoolscl/c_funcs/dnb2_gen_natural.c:3-70,
+ * dnb2_gen_gray.c:3-69), then, when shiftsb != NULL, dnb2_digital_shift.c:3-36
+ * ((point << lshifts[l % r_x]) ^ shiftsb[l,j]), then, when x != NULL,
+ * dnb2_integer_to_float.c:3-32 (ldexp(value, -tmaxes[l])).  C holds r_C*d*mmax
+ * columns (randomisation l uses set l % r_C); xrb may be NULL when x is set. */
+int qmc_dnb2_gen_fused(uint64_t r, uint64_t n, uint64_t d, uint64_t n_start, uint64_t mmax, const uint64_t *C,
+                       uint64_t r_C, int gray, const uint64_t *lshifts, uint64_t r_x, const uint64_t *shiftsb,
+                       const uint64_t *tmaxes, uint64_t *xrb, double *x, qmc_stream_t s);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* QMCGB_H */

@@ -1,0 +1,79 @@
+"""ctypes binding of libqmcgb.so (declarations in include/qmcgb.h).
+
+The library is the only compute path: if it is missing or cannot be loaded,
+every call raises.  There is no CPU fallback.
+"""
+import ctypes
+import os
+import threading
+
+from ._signatures import SIGNATURES
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libqmcgb.so")
+
+QMC_OK, QMC_ERR_ARG, QMC_ERR_DOMAIN, QMC_ERR_CUDA, QMC_ERR_DEVICE = 0, -1, -2, -3, -4
+
+_lock = threading.Lock()
+_lib = None
+
+U64 = ctypes.c_uint64
+PTR = ctypes.c_void_p
+INT = ctypes.c_int
+
+# extra entry points beyond the 23 reference functions: name -> argtypes
+EXTRA = {
+    "qmc_lat_gen_shift": [U64, U64, U64, U64, INT, PTR, PTR, PTR, PTR],
+    "qmc_dnb2_gen_fused": [U64, U64, U64, U64, U64, PTR, U64, INT, PTR, U64, PTR, PTR, PTR, PTR, PTR],
+}
+
+
+class LibraryMissing(RuntimeError):
+    pass
+
+
+def lib():
+    """Load libqmcgb.so once; raise if it is not built."""
+    global _lib
+    with _lock:
+        if _lib is not None:
+            return _lib
+        if not os.path.exists(LIB_PATH):
+            raise LibraryMissing(
+                "libqmcgb.so is not built (expected at %s); run "
+                "`python -m qmctoolscl_gb300._build` or __graft_entry__.build()" % LIB_PATH)
+        L = ctypes.CDLL(LIB_PATH)
+        for name, (args, _outs) in SIGNATURES.items():
+            fn = getattr(L, "qmc_" + name)
+            fn.argtypes = [U64 if k == "u64" else PTR for _a, k in args] + [PTR]
+            fn.restype = INT
+        for name, types in EXTRA.items():
+            fn = getattr(L, name)
+            fn.argtypes = types
+            fn.restype = INT
+        L.qmc_last_error.restype = ctypes.c_char_p
+        L.qmc_last_error.argtypes = []
+        L.qmc_version.restype = INT
+        L.qmc_device_error_check.argtypes = [PTR]
+        L.qmc_device_error_check.restype = INT
+        L.qmc_device_error_reset.argtypes = [PTR]
+        L.qmc_device_error_reset.restype = INT
+        _lib = L
+        return _lib
+
+
+def last_error():
+    return lib().qmc_last_error().decode(errors="replace")
+
+
+class QmcError(RuntimeError):
+    """A CUDA-side failure reported by libqmcgb."""
+
+
+def check(rc, what):
+    if rc == QMC_OK:
+        return
+    msg = "%s: %s" % (what, last_error())
+    if rc in (QMC_ERR_ARG, QMC_ERR_DOMAIN):
+        raise ValueError(msg)
+    raise QmcError(msg)

@@ -1,0 +1,83 @@
+// runtime.cu -- status reporting and the device error word of libqmcgb.
+#include <stdarg.h>
+#include <stdio.h>
+#include <string.h>
+
+#include "common.cuh"
+
+namespace qmcgb {
+
+static thread_local char g_msg[512] = "";
+
+void set_error(const char *fmt, ...)
+{
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(g_msg, sizeof(g_msg), fmt, ap);
+    va_end(ap);
+}
+
+int cuda_status(cudaError_t e, const char *what)
+{
+    if (e == cudaSuccess) return QMC_OK;
+    set_error("%s: %s", what, cudaGetErrorString(e));
+    return QMC_ERR_CUDA;
+}
+
+int launch_status(const char *what) { return cuda_status(cudaGetLastError(), what); }
+
+// One word per loaded library and device; kernels OR error codes into it.
+__device__ unsigned int g_device_error;
+
+unsigned int *device_error_ptr()
+{
+    void *p = nullptr;
+    if (cudaGetSymbolAddress(&p, g_device_error) != cudaSuccess) return nullptr;
+    return (unsigned int *)p;
+}
+
+int device_error_reset(cudaStream_t s)
+{
+    unsigned int *p = device_error_ptr();
+    if (!p) return cuda_status(cudaGetLastError(), "locating the device error word");
+    return cuda_status(cudaMemsetAsync(p, 0, sizeof(unsigned int), s), "clearing the device error word");
+}
+
+int sm_count()
+{
+    int dev = 0, n = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return 152;
+    if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return 152;
+    return n > 0 ? n : 152;
+}
+
+}  // namespace qmcgb
+
+extern "C" {
+
+const char *qmc_last_error(void) { return qmcgb::g_msg; }
+
+int qmc_version(void) { return 10000; }
+
+int qmc_device_error_reset(qmc_stream_t s) { return qmcgb::device_error_reset(QMC_STREAM(s)); }
+
+int qmc_device_error_check(qmc_stream_t s)
+{
+    cudaStream_t st = QMC_STREAM(s);
+    unsigned int *p = qmcgb::device_error_ptr();
+    if (!p) return qmcgb::cuda_status(cudaGetLastError(), "locating the device error word");
+    unsigned int h = 0;
+    int rc = qmcgb::cuda_status(cudaMemcpyAsync(&h, p, sizeof(h), cudaMemcpyDeviceToHost, st),
+                                "reading the device error word");
+    if (rc) return rc;
+    rc = qmcgb::cuda_status(cudaStreamSynchronize(st), "synchronising the stream");
+    if (rc) return rc;
+    if (h) {
+        qmcgb::device_error_reset(st);
+        qmcgb::set_error("a kernel met a table index outside its array (code %u)", h);
+        return QMC_ERR_DEVICE;
+    }
+    return QMC_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,235 @@
+// transforms.cu -- FP64 radix-2 FFT (bit-reversed input, natural output),
+// its inverse (natural input, bit-reversed output) and the Walsh-Hadamard
+// transform, all orthonormal and in place along the last axis.
+//
+// Reference: qmctoolscl/c_funcs/fft_bro_1d_radix2.c:3-80 (decimation in
+// time: stage k pairs i1, i1+2^k with twiddle tw[(i1 mod 2^k) * 2^(m-k-1)],
+// tw[t] = exp(-2 pi i t/n)), ifft_bro_1d_radix2.c:3-81 (decimation in
+// frequency: stage k pairs at distance 2^s, s = m-k-1, twiddle
+// tw[(i1 mod 2^s) * 2^k] with the opposite sign), fwht_1d_radix2.c:3-53.
+// Every stage of the reference divides by sqrt(2); here the stages are
+// unscaled and the last pass multiplies by 2^(-m/2) once.  The results agree
+// with the reference to FP64 rounding (not bit for bit).
+//
+// Passes.  Stages whose butterflies span the index bits [k0, k1) act on
+// independent groups {h*2^k1 + q*2^k0 + c : q < 2^(k1-k0)}; a CTA loads one
+// group for CT consecutive c (CT contiguous doubles per q, so loads and
+// stores are coalesced runs), runs those stages in shared memory, and
+// writes the tile back in place.  Up to 4096 complex (8192 real) values fit
+// a tile, so lengths up to 2^12 (2^13 real) take one pass, up to 2^20 two,
+// and so on.  The FFT runs the low-bit pass first, the inverse the high-bit
+// pass first, matching the order of their stages.
+//
+// GB300 runs FP64 at about 1.25 TFLOP/s, so these kernels are FP64-bound;
+// they are the plain, reference-accurate path.  The tensor-core path
+// (tc_fft.cu) is the fast one.
+#include <cmath>
+
+#include "common.cuh"
+
+namespace {
+
+constexpr int FT_THREADS = 256;
+constexpr u32 TILE_COMPLEX = 4096;
+constexpr u32 TILE_REAL = 8192;
+
+enum FtKind { FT_FFT = 0, FT_IFFT = 1, FT_FWHT = 2 };
+
+__global__ void twiddle_kernel(u64 n, double sign, double *twr, double *twi)
+{
+    for (u64 t = (u64)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (u64)gridDim.x * blockDim.x) {
+        double sn, cs;
+        // the angle 2*pi*t/n as a multiple of pi is exact for n a power of two
+        sincospi(__ddiv_rn(__ull2double_rn(2 * t), __ull2double_rn(n)), &sn, &cs);
+        twr[t] = cs;
+        twi[t] = sign * sn;
+    }
+}
+
+struct PassArgs {
+    u64 nvec;        // d1*d2 vectors
+    u32 m;           // log2 n
+    u32 k0, k1;      // index bits spanned by this pass
+    u32 ct;          // consecutive c values per tile
+    double *xr, *xi;
+    const double *twr, *twi;
+    double scale;    // applied on write-back when != 1
+};
+
+template <int KIND>
+__global__ void __launch_bounds__(FT_THREADS) ft_pass_kernel(PassArgs a)
+{
+    extern __shared__ double sm[];
+    const u32 Q = 1u << (a.k1 - a.k0);
+    const u32 ct = a.ct;
+    const u32 tile_elems = Q * ct;
+    double *sr = sm;
+    double *si = sm + tile_elems;  // unused for the WHT
+    const u64 n = 1ull << a.m;
+    const u64 H = n >> a.k1;                 // groups along the high bits
+    const u64 cchunks = (1ull << a.k0) / ct;  // c chunks along the low bits
+    const u64 tiles_per_vec = H * cchunks;
+    const u64 total_tiles = a.nvec * tiles_per_vec;
+    for (u64 tile = blockIdx.x; tile < total_tiles; tile += gridDim.x) {
+        const u64 v = tile / tiles_per_vec, rem = tile % tiles_per_vec;
+        const u64 h = rem / cchunks, c0 = (rem % cchunks) * ct;
+        const u64 base = v * n + (h << a.k1) + c0;
+        for (u32 e = threadIdx.x; e < tile_elems; e += FT_THREADS) {
+            const u32 q = e / ct, cc = e % ct;
+            const u64 gi = base + ((u64)q << a.k0) + cc;
+            sr[e] = a.xr[gi];
+            if (KIND != FT_FWHT) si[e] = a.xi[gi];
+        }
+        __syncthreads();
+        const u32 nb = tile_elems / 2;
+        for (u32 st = 0; st < a.k1 - a.k0; st++) {
+            // FFT and WHT: bits k0..k1-1 ascending; inverse FFT descending
+            const u32 bit = (KIND == FT_IFFT) ? (a.k1 - 1 - st) : (a.k0 + st);
+            const u32 hb = bit - a.k0;  // bit within q
+            const u32 half = 1u << hb;
+            for (u32 b = threadIdx.x; b < nb; b += FT_THREADS) {
+                const u32 p = b / ct, cc = b % ct;
+                const u32 q1 = ((p >> hb) << (hb + 1)) | (p & (half - 1));
+                const u32 e1 = q1 * ct + cc, e2 = e1 + half * ct;
+                if (KIND == FT_FWHT) {
+                    const double x1 = sr[e1], x2 = sr[e2];
+                    sr[e1] = x1 + x2;
+                    sr[e2] = x1 - x2;
+                    continue;
+                }
+                // global index of the upper partner, for the twiddle
+                const u64 i1 = (h << a.k1) + ((u64)q1 << a.k0) + c0 + cc;
+                const u64 t = (i1 & ((1ull << bit) - 1)) << (a.m - bit - 1);
+                const double wr = a.twr[t], wi = a.twi[t];
+                const double ar = sr[e1], ai = si[e1], br = sr[e2], bi = si[e2];
+                if (KIND == FT_FFT) {
+                    const double yr = fma(br, wr, -bi * wi), yi = fma(br, wi, bi * wr);
+                    sr[e1] = ar + yr;
+                    si[e1] = ai + yi;
+                    sr[e2] = ar - yr;
+                    si[e2] = ai - yi;
+                } else {
+                    const double dr = ar - br, di = ai - bi;
+                    sr[e1] = ar + br;
+                    si[e1] = ai + bi;
+                    sr[e2] = fma(dr, wr, -di * wi);
+                    si[e2] = fma(dr, wi, di * wr);
+                }
+            }
+            __syncthreads();
+        }
+        const double sc = a.scale;
+        for (u32 e = threadIdx.x; e < tile_elems; e += FT_THREADS) {
+            const u32 q = e / ct, cc = e % ct;
+            const u64 gi = base + ((u64)q << a.k0) + cc;
+            a.xr[gi] = sc != 1.0 ? sr[e] * sc : sr[e];
+            if (KIND != FT_FWHT) a.xi[gi] = sc != 1.0 ? si[e] * sc : si[e];
+        }
+        __syncthreads();
+    }
+}
+
+struct Pass {
+    u32 k0, k1, ct;
+};
+
+// Bit ranges covered by the passes, low bits first.
+int plan_passes(u32 m, u32 tile, Pass *out)
+{
+    u32 lowbits = 0;
+    while ((1u << (lowbits + 1)) <= tile) lowbits++;
+    int np = 0;
+    u32 k0 = 0;
+    const u32 first = m < lowbits ? m : lowbits;
+    out[np++] = Pass{0, first, 1};
+    k0 = first;
+    while (k0 < m) {
+        const u32 ct = 16;  // 16 consecutive doubles = 128 bytes per run
+        u32 span = 0;
+        while ((ct << (span + 1)) <= tile) span++;
+        const u32 k1 = (k0 + span < m) ? k0 + span : m;
+        out[np++] = Pass{k0, k1, ct < (1u << k0) ? ct : (1u << k0)};
+        k0 = k1;
+    }
+    return np;
+}
+
+int run_transform(int kind, u64 d1, u64 d2, u64 n_half, double *twr, double *twi, double *xr, double *xi,
+                  cudaStream_t s, const char *what)
+{
+    const u64 nvec = d1 * d2;
+    QMC_REQUIRE_DOMAIN(n_half > 0 && (n_half & (n_half - 1)) == 0 && n_half <= (1ull << 40),
+                       "%s: n = 2*n_half must be a power of two (n_half=%llu)", what,
+                       (unsigned long long)n_half);
+    const u64 n = 2 * n_half;
+    u32 m = 0;
+    while ((1ull << m) < n) m++;
+    if (kind != FT_FWHT) {
+        QMC_REQUIRE(twr && twi, "%s: null twiddle pointer", what);
+        twiddle_kernel<<<qmcgb::grid_for(n, 256, (unsigned)qmcgb::sm_count() * 8), 256, 0, s>>>(
+            n, kind == FT_FFT ? -1.0 : 1.0, twr, twi);
+        if (int rc = qmcgb::launch_status(what)) return rc;
+    }
+    if (nvec == 0) return QMC_OK;
+    QMC_REQUIRE(xr && (kind == FT_FWHT || xi), "%s: null data pointer", what);
+    const u32 tile = kind == FT_FWHT ? TILE_REAL : TILE_COMPLEX;
+    Pass passes[16];
+    const int np = plan_passes(m, tile, passes);
+    // orthonormal scaling 2^(-m/2), applied once by the last pass
+    const double scale = (m % 2 == 0) ? ldexp(1.0, -(int)(m / 2)) : ldexp(1.0, -(int)(m / 2)) * 0.70710678118654752440;
+    for (int pi = 0; pi < np; pi++) {
+        const Pass p = (kind == FT_IFFT) ? passes[np - 1 - pi] : passes[pi];
+        PassArgs a;
+        a.nvec = nvec;
+        a.m = m;
+        a.k0 = p.k0;
+        a.k1 = p.k1;
+        a.ct = p.ct;
+        a.xr = xr;
+        a.xi = xi;
+        a.twr = twr;
+        a.twi = twi;
+        a.scale = (pi == np - 1) ? scale : 1.0;
+        const u32 elems = (1u << (p.k1 - p.k0)) * p.ct;
+        const size_t smem = (size_t)elems * sizeof(double) * (kind == FT_FWHT ? 1 : 2);
+        const u64 tiles = nvec * (n >> p.k1) * ((1ull << p.k0) / p.ct);
+        const unsigned grid = qmcgb::grid_for(tiles, 1, (unsigned)qmcgb::sm_count() * 8);
+        cudaError_t e = cudaSuccess;
+        if (kind == FT_FFT) {
+            e = cudaFuncSetAttribute(ft_pass_kernel<FT_FFT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            if (e == cudaSuccess) ft_pass_kernel<FT_FFT><<<grid, FT_THREADS, smem, s>>>(a);
+        } else if (kind == FT_IFFT) {
+            e = cudaFuncSetAttribute(ft_pass_kernel<FT_IFFT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            if (e == cudaSuccess) ft_pass_kernel<FT_IFFT><<<grid, FT_THREADS, smem, s>>>(a);
+        } else {
+            e = cudaFuncSetAttribute(ft_pass_kernel<FT_FWHT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            if (e == cudaSuccess) ft_pass_kernel<FT_FWHT><<<grid, FT_THREADS, smem, s>>>(a);
+        }
+        if (e != cudaSuccess) return qmcgb::cuda_status(e, what);
+        if (int rc = qmcgb::launch_status(what)) return rc;
+    }
+    return QMC_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int qmc_fft_bro_1d_radix2(uint64_t d1, uint64_t d2, uint64_t n_half, double *twiddler, double *twiddlei, double *xr,
+                          double *xi, qmc_stream_t s)
+{
+    return run_transform(FT_FFT, d1, d2, n_half, twiddler, twiddlei, xr, xi, QMC_STREAM(s), "fft_bro_1d_radix2");
+}
+
+int qmc_ifft_bro_1d_radix2(uint64_t d1, uint64_t d2, uint64_t n_half, double *twiddler, double *twiddlei, double *xr,
+                           double *xi, qmc_stream_t s)
+{
+    return run_transform(FT_IFFT, d1, d2, n_half, twiddler, twiddlei, xr, xi, QMC_STREAM(s), "ifft_bro_1d_radix2");
+}
+
+int qmc_fwht_1d_radix2(uint64_t d1, uint64_t d2, uint64_t n_half, double *x, qmc_stream_t s)
+{
+    return run_transform(FT_FWHT, d1, d2, n_half, nullptr, nullptr, x, nullptr, QMC_STREAM(s), "fwht_1d_radix2");
+}
+
+}  // extern "C"

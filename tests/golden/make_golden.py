@@ -43,6 +43,8 @@ from qmctoolscl_gb300._signatures import SIGNATURES  # noqa: E402
 OUT_NPZ = os.path.join(REPO, "tests", "golden", "golden.npz")
 OUT_JSON = os.path.join(REPO, "tests", "golden", "golden.json")
 TWIDDLES = ("twiddler", "twiddlei")
+IN_PLACE = ("xr", "xi", "x")  # transformed in place by the fft/ifft/fwht (the only in/out arrays)
+IN_PLACE_FUNCS = ("fft_bro_1d_radix2", "ifft_bro_1d_radix2", "fwht_1d_radix2")
 
 
 class Recorder:
@@ -62,9 +64,9 @@ class Recorder:
             else:
                 shapes[an] = list(np.shape(a))
                 arrays.append(an)
-                # twiddle buffers are write-only scratch of the transforms: their
-                # input content is never read, so it is not stored
-                if an not in TWIDDLES:
+                # output-only buffers (np.empty in the callers, twiddle tables)
+                # are never read, so their initial content is not stored
+                if an not in outs or (name in IN_PLACE_FUNCS and an in IN_PLACE):
                     self.arrays["%04d/%s" % (cid, an)] = np.array(a, copy=True)
         oracle.call_ref(name, *args)
         names = [s[0] for s in spec]
@@ -136,6 +138,9 @@ def replay_doctests(ref, shim):
               for b in blocks]
     text = "\n".join(blocks[:3] + blocks[4:])  # the C-backend variant
     sys.modules["qmctoolscl"] = shim
+    # a few transform examples draw from numpy's global generator (unseeded in
+    # the docs); seed it so the recorded fixtures are reproducible
+    np.random.seed(7)
     parser = doctest.DocTestParser()
     test = parser.get_doctest(text, {}, "qmctoolscl_docs", "index.md", 0)
     runner = doctest.DocTestRunner(optionflags=doctest.ELLIPSIS)
@@ -305,6 +310,38 @@ def random_cases(rec, rf):
         rec.call("fwht_1d_radix2", [U(d1), U(d2), U(nh), rng.standard_normal((d1, d2, n))])
 
 
+def rand_cases(rf):
+    """Outputs of the reference's random-input helpers for a fixed sequence
+    of calls on one Generator (the helpers' results are defined by numpy's
+    streams; the package restates them and must match these)."""
+    rng = np.random.Generator(np.random.SFC64(11))
+    U = np.uint64
+    b2 = np.array([[2, 3], [5, 7]], U)
+    b1 = np.array([3, 5, 541], U)
+    calls = [
+        ("random_tbit_uint64s", (5, (3, 4))), ("random_tbit_uint64s", (64, (2, 5))),
+        ("random_tbit_uint64s", (0, (2,))), ("random_uint64_permutations", (3, 7)),
+        ("lat_get_shifts", (3, 5)), ("dnb2_get_digital_shifts", (2, 3, 64)),
+        ("dnb2_get_digital_shifts", (2, 3, 20)),
+        ("dnb2_get_linear_scramble_matrix", (2, 3, 4, 6, False)),
+        ("dnb2_get_linear_scramble_matrix", (2, 2, 64, 64, False)),
+        ("gdn_get_linear_scramble_matrix", (4, 2, 5, 10, 2, b2)),
+        ("gdn_get_linear_scramble_matrix", (2, 3, 4, 4, 1, b1)),
+        ("gdn_get_halton_generating_matrix", (2, 3, 4)),
+        ("gdn_get_digital_shifts", (4, 2, 12, 2, b2)), ("gdn_get_digital_shifts", (2, 3, 6, 1, b1)),
+        ("gdn_get_digital_permutations", (4, 2, 3, 2, b2)), ("gdn_get_digital_permutations", (1, 3, 2, 1, b1)),
+    ]
+    out = {}
+    meta = []
+    for idx, (fname, fargs) in enumerate(calls):
+        fn = getattr(rf, fname)
+        res = fn(*fargs) if fname == "gdn_get_halton_generating_matrix" else fn(rng, *fargs)
+        out["%02d" % idx] = np.asarray(res)
+        meta.append({"name": fname, "args": [a.tolist() if isinstance(a, np.ndarray) else a for a in fargs],
+                     "array_args": [i for i, a in enumerate(fargs) if isinstance(a, np.ndarray)]})
+    return out, meta
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default="/root/reference")
@@ -315,6 +352,10 @@ def main():
     replay_doctests(a.ref, make_shim(rec, rf, ref_docstrings(a.ref)))
     n_doc = len(rec.cases)
     random_cases(rec, rf)
+    rand_out, rand_meta = rand_cases(rf)
+    np.savez_compressed(os.path.join(REPO, "tests", "golden", "rand_funcs.npz"), **rand_out)
+    with open(os.path.join(REPO, "tests", "golden", "rand_funcs.json"), "w") as f:
+        json.dump({"seed": "np.random.Generator(np.random.SFC64(11))", "calls": rand_meta}, f, indent=1)
     np.savez_compressed(OUT_NPZ, **rec.arrays)
     with open(OUT_JSON, "w") as f:
         json.dump({"generator": "tests/golden/make_golden.py",

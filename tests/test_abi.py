@@ -1,0 +1,65 @@
+"""The C-ABI library: it builds for sm_103a, loads without a GPU, and exports
+every entry point include/qmcgb.h declares (no compute calls here)."""
+import ctypes
+import os
+import re
+
+import pytest
+
+REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_symbols():
+    names = []
+    for fn in sorted(os.listdir(os.path.join(REPO, "include"))):
+        if fn.endswith(".h"):
+            with open(os.path.join(REPO, "include", fn)) as f:
+                text = re.sub(r"/\*.*?\*/", "", f.read(), flags=re.S)
+            names += re.findall(r"\b(qmc_\w+)\s*\(", text)
+    return sorted(set(names))
+
+
+@pytest.fixture(scope="module")
+def lib():
+    from qmctoolscl_gb300 import _build
+    path = _build.build()
+    return ctypes.CDLL(path)
+
+
+def test_header_declares_all_reference_functions():
+    from qmctoolscl_gb300._signatures import NAMES
+    syms = declared_symbols()
+    for name in NAMES:
+        assert "qmc_" + name in syms
+
+
+def test_library_exports_every_declared_symbol(lib):
+    missing = [s for s in declared_symbols() if not hasattr(lib, s)]
+    assert missing == []
+
+
+def test_library_reports_version_and_empty_error(lib):
+    lib.qmc_version.restype = ctypes.c_int
+    assert lib.qmc_version() >= 10000
+    lib.qmc_last_error.restype = ctypes.c_char_p
+    assert lib.qmc_last_error() == b""
+
+
+def test_ffi_binds_all_entry_points(lib):
+    from qmctoolscl_gb300 import _ffi
+    L = _ffi.lib()
+    for s in declared_symbols():
+        getattr(L, s)
+
+
+def test_argument_errors_need_no_gpu(lib):
+    """Argument checks run on the host before any CUDA call."""
+    from qmctoolscl_gb300 import _ffi
+    L = _ffi.lib()
+    # lat_gen_natural with n_start not a power of two: rejected before launch
+    rc = L.qmc_lat_gen_natural(1, 3, 2, 3, None, None, None)
+    assert rc == _ffi.QMC_ERR_ARG
+    assert b"powers of 2" in L.qmc_last_error()
+    # non-power-of-two transform length
+    rc = L.qmc_fwht_1d_radix2(1, 1, 3, None, None)
+    assert rc == _ffi.QMC_ERR_DOMAIN
