@@ -56,13 +56,17 @@ __device__ __forceinline__ u64 seq_index(bool gray, u64 n_start, u64 i)
     return gray ? (k ^ (k >> 1)) : k;
 }
 
+// FP64 fallback kept out of line so its instructions never sit (predicated
+// off) in the per-coordinate loop, where they would load GB300's slow FP64 pipe.
+__device__ __noinline__ double to_float_hw(u64 v, int e) { return ldexp(__ull2double_rn(v), e); }
+
 __device__ __forceinline__ double to_float_bits(u64 v, int e)
 {
     if (v == 0) return 0.0;
     const int lz = __clzll((long long)v);
     const int E = 1085 - lz + e;
     if (E >= 1 && E <= 2045) return as_double(u64_scaled_bits(v, e));
-    return ldexp(__ull2double_rn(v), e);  // subnormal or overflowing results
+    return to_float_hw(v, e);  // subnormal or overflowing results
 }
 
 template <bool GRAY, bool SHIFT, bool FLOAT, bool WRITE_INT>

@@ -206,6 +206,13 @@ __device__ __forceinline__ void fill_recips(double *rc, u64 b, u64 tmax)
     }
 }
 
+// one step v + recip*digit with FP64 instructions, out of line (see
+// to_float_hw in dnb2.cu for why)
+__device__ __noinline__ u64 digit_step_hw(u64 v, double rc, u64 dg)
+{
+    return as_bits(__dadd_rn(as_double(v), __dmul_rn(rc, __ull2double_rn(dg))));
+}
+
 // v = sum_t recip_t * digit_t with the reference's rounding sequence
 __device__ __forceinline__ double digits_to_double(const double *rc, const u64 *dig, u64 tmax)
 {
@@ -219,7 +226,7 @@ __device__ __forceinline__ double digits_to_double(const double *rc, const u64 *
             const u64 p = dmul_small_bits(rb, (u32)dg);
             v = dadd_pos_bits(v, p);
         } else {
-            v = as_bits(__dadd_rn(as_double(v), __dmul_rn(rc[t], __ull2double_rn(dg))));
+            v = digit_step_hw(v, rc[t], dg);
         }
     }
     return as_double(v);

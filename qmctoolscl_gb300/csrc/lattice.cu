@@ -81,38 +81,144 @@ __device__ __forceinline__ LatCol load_col(const LatArgs &a, u64 l, u64 j, bool 
     return c;
 }
 
-// fmod(g*V, 1) as the reference computes it, for sequence index m.
-__device__ __forceinline__ double lat_value_hw(const LatCol &c, int order, u64 m, u64 i, u64 n)
+// fmod(g*V, 1) as the reference computes it, for sequence index m, with
+// FP64 instructions.  Kept out of line: GB300's FP64 pipe is slow, and if
+// the compiler if-converted these fallbacks into the per-element loop their
+// (predicated-off) FP64 instructions would still be issued for every
+// coordinate and saturate that pipe.
+__device__ __noinline__ double lat_value_hw(double gd, int order, u64 m, u64 i, u64 n)
 {
     if (order == ORDER_LINEAR_POW2 || order == ORDER_LINEAR_GENERIC) {
         const double q = __ddiv_rn(__ull2double_rn(i), __ull2double_rn(n));
-        return frac_mod1(__dmul_rn(c.gd, q));
+        return frac_mod1(__dmul_rn(gd, q));
     }
     const int p = m ? 64 - __clzll((long long)m) : 0;
     const u64 v = m ? (__brevll(m) >> (64 - p)) : 0;
     const double V = scalbn(__ull2double_rn(v), -p);
-    return frac_mod1(__dmul_rn(c.gd, V));
+    return frac_mod1(__dmul_rn(gd, V));
+}
+
+// Every case other than the common one: exact integer generation with a
+// shift that needs general rounding, or FP64 generation/shift.
+__device__ __noinline__ double lat_point_general(const LatCol &c, int order, u64 B, u64 m, u64 i, u64 n,
+                                                 bool shift)
+{
+    double x;
+    if (c.fast) {
+        const u64 W = c.g * B;
+        if (!shift) return fix64_to_double(W);
+        if (c.shift_kind == 1) return fix64_to_double(add_mod1_fix64(W, c.S));
+        x = fix64_to_double(W);
+    } else {
+        x = lat_value_hw(c.gd, order, m, i, n);
+        if (!shift) return x;
+    }
+    return frac_mod1(__dadd_rn(x, c.s));
 }
 
 template <bool SHIFT>
 __device__ __forceinline__ double lat_point(const LatCol &c, int order, u64 B, u64 m, u64 i, u64 n)
 {
-    if (c.fast) {
+    if (c.fast && (!SHIFT || c.shift_kind == 0)) {
         const u64 W = c.g * B;  // fraction of g*V in 0.64 fixed point (<= 53 significant bits)
         if (!SHIFT) return fix64_to_double(W);
-        if (c.shift_kind == 0) {
-            // W and S are multiples of 2^-53: the sum needs rounding only when
-            // it reaches 1, and then only a tie on bit 11 can occur
-            u64 T = W + c.S;
-            if (T < W) T = (T + ((T >> 1) & 0x800ull)) & ~0xFFFull;
-            return fix64_to_double(T);
-        }
-        if (c.shift_kind == 1) return fix64_to_double(add_mod1_fix64(W, c.S));
-        return frac_mod1(__dadd_rn(fix64_to_double(W), c.s));
+        // W and S are multiples of 2^-53: the sum needs rounding only when it
+        // reaches 1, and then only a tie on bit 11 can occur
+        u64 T = W + c.S;
+        if (T < W) T = (T + ((T >> 1) & 0x800ull)) & ~0xFFFull;
+        return fix64_to_double(T);
     }
-    const double x = lat_value_hw(c, order, m, i, n);
-    if (!SHIFT) return x;
-    return frac_mod1(__dadd_rn(x, c.s));
+    return lat_point_general(c, order, B, m, i, n, SHIFT);
+}
+
+// Exact double of (th:tl) * 2^-64 for th != 0 and at most 53 significant
+// bits, on 32-bit halves: normalise with one funnel shift, drop 11 bits with
+// another, add the exponent into the high word.
+__device__ __forceinline__ double fix64_hi_to_double(u32 th, u32 tl)
+{
+    const u32 lz = __clz(th);
+    const u32 hi = __funnelshift_l(tl, th, lz);
+    const u32 lo = tl << lz;
+    const u32 m_lo = __funnelshift_r(lo, hi, 11);
+    const u32 m_hi = (hi >> 11) + ((1021u - lz) << 20);
+    return __hiloint2double((int)m_hi, (int)m_lo);
+}
+
+// fmod(point + shift, 1) for the narrow case (every sequence index below
+// 2^32, so B = bitreverse64(m) has a zero low word and the fraction
+// g*B mod 2^64 is (g mod 2^32) * bitreverse32(m) in the high word); the shift
+// is a multiple of 2^-53 in 0.64 fixed point (sh:sl).
+template <bool SHIFT>
+__device__ __forceinline__ double lat_point_narrow(u32 g_lo, u32 bh, u32 sh, u32 sl, const LatCol &c, int order,
+                                                   u64 m, u64 i, u64 n)
+{
+    const u32 wh = g_lo * bh;
+    if (!SHIFT) return wh ? fix64_hi_to_double(wh, 0u) : 0.0;
+    u32 th = wh + sh, tl = sl;
+    if (th < wh) {  // the sum reached 1: round to the 2^-52 grid (ties to even), drop the 1
+        const u64 t = ((((u64)th << 32) | tl) + ((tl >> 1) & 0x800u)) & ~0xFFFull;
+        th = (u32)(t >> 32);
+        tl = (u32)t;
+    }
+    if (th) return fix64_hi_to_double(th, tl);
+    return fix64_to_double(((u64)th << 32) | tl);  // results below 2^-32
+}
+
+template <int ORDER, bool SHIFT, int VEC>
+__global__ void __launch_bounds__(256) lat_gen_narrow_kernel(LatArgs a)
+{
+    // every index n_start + i < 2^32 and every column on the exact integer
+    // path with (for SHIFT) a shift on the 2^-53 grid: checked per column,
+    // with the general per-element code for columns that are not
+    const u32 ngroups = (u32)((a.d + VEC - 1) / VEC);
+    const u32 row_stride = gridDim.x * blockDim.y;
+    const u32 n = (u32)a.n, n_start = (u32)a.n_start;
+    for (u64 l = blockIdx.y; l < a.r; l += gridDim.y) {
+        for (u32 jg = threadIdx.x; jg < ngroups; jg += blockDim.x) {
+            const u64 j0 = (u64)jg * VEC;
+            LatCol c[VEC];
+            bool easy = true;
+#pragma unroll
+            for (int v = 0; v < VEC; v++) {
+                c[v] = load_col(a, l, j0 + v, SHIFT, ORDER);
+                easy &= c[v].fast && (!SHIFT || c[v].shift_kind == 0);
+            }
+            u32 g_lo[VEC], sh[VEC], sl[VEC];
+#pragma unroll
+            for (int v = 0; v < VEC; v++) {
+                g_lo[v] = (u32)c[v].g;
+                sh[v] = (u32)(c[v].S >> 32);
+                sl[v] = (u32)c[v].S;
+            }
+            double *out = a.out + l * a.n * a.d + j0;
+            for (u32 i = blockIdx.x * blockDim.y + threadIdx.y; i < n; i += row_stride) {
+                u32 bh, m32;
+                if (ORDER == ORDER_LINEAR_POW2) {
+                    m32 = i;
+                    bh = a.log2n ? (i << (32 - a.log2n)) : 0u;  // log2n <= 32 here
+                } else {
+                    const u32 k = n_start + i;
+                    m32 = (ORDER == ORDER_GRAY) ? (k ^ (k >> 1)) : k;
+                    bh = __brev(m32);
+                }
+                double y[VEC];
+                if (easy) {
+#pragma unroll
+                    for (int v = 0; v < VEC; v++)
+                        y[v] = lat_point_narrow<SHIFT>(g_lo[v], bh, sh[v], sl[v], c[v], ORDER, m32, i, a.n);
+                } else {
+#pragma unroll
+                    for (int v = 0; v < VEC; v++)
+                        y[v] = lat_point_general(c[v], ORDER, (u64)bh << 32, m32, i, a.n, SHIFT);
+                }
+                if (VEC == 2) {
+                    __stcs((double2 *)(out + (u64)i * a.d), make_double2(y[0], y[1]));
+                } else {
+                    __stcs(out + (u64)i * a.d, y[0]);
+                }
+            }
+        }
+    }
 }
 
 template <int ORDER, bool SHIFT, int VEC>
@@ -154,11 +260,13 @@ struct ShiftArgs {
     double *xr;
 };
 
+__device__ __noinline__ double shift_one_hw(double x, double s) { return frac_mod1(__dadd_rn(x, s)); }
+
 __device__ __forceinline__ double shift_one(double x, u64 S, bool s_ok, double s)
 {
     u64 X;
     if (s_ok && double_to_fix64(x, &X)) return fix64_to_double(add_mod1_fix64(X, S));
-    return frac_mod1(__dadd_rn(x, s));
+    return shift_one_hw(x, s);
 }
 
 template <int VEC>
@@ -228,10 +336,19 @@ int launch_gen(const LatArgs &a, cudaStream_t s, const char *what)
     const bool vec2 = (a.d % 2 == 0) && aligned16(a.out);
     const u64 ngroups = vec2 ? a.d / 2 : a.d;
     const Shape sh = shape_for(a.r, a.n, ngroups);
-    if (vec2)
+    // 32-bit indexing: every sequence index below 2^32
+    const bool narrow = ORDER != ORDER_LINEAR_GENERIC && a.n_start + a.n <= (1ull << 32) &&
+                        a.n_start + a.n >= a.n_start && (ORDER != ORDER_LINEAR_POW2 || a.log2n <= 32);
+    if (narrow) {
+        if (vec2)
+            lat_gen_narrow_kernel<ORDER, SHIFT, 2><<<sh.grid, sh.block, 0, s>>>(a);
+        else
+            lat_gen_narrow_kernel<ORDER, SHIFT, 1><<<sh.grid, sh.block, 0, s>>>(a);
+    } else if (vec2) {
         lat_gen_kernel<ORDER, SHIFT, 2><<<sh.grid, sh.block, 0, s>>>(a);
-    else
+    } else {
         lat_gen_kernel<ORDER, SHIFT, 1><<<sh.grid, sh.block, 0, s>>>(a);
+    }
     return qmcgb::launch_status(what);
 }
 
