@@ -49,6 +49,14 @@ int qmc_device_error_reset(qmc_stream_t s);
  * kernel recorded an out-of-array index since the last reset */
 int qmc_device_error_check(qmc_stream_t s);
 
+/* device-side address of pinned host memory (cudaHostAlloc / cudaHostRegister)
+ * that kernels may write directly; QMC_ERR_ARG for pageable memory.  No
+ * reference counterpart: used to write results straight into host buffers. */
+int qmc_host_pointer_for_device(const void *host, void **dev);
+/* pageable-memory access, whether it uses the host page tables, SM count of
+ * the current device.  No reference counterpart. */
+int qmc_device_attributes(int *pageable_access, int *uses_host_page_tables, int *sms);
+
 /* ---- rank-1 lattices ---------------------------------------------------- */
 
 /* qmctoolscl/c_funcs/lat_gen_linear.c:3-13: x[l,i,j] = fmod(g[l,j]*(i/n), 1) */
@@ -167,6 +175,74 @@ int qmc_lat_gen_shift(uint64_t r, uint64_t n, uint64_t d, uint64_t n_start, int 
 int qmc_dnb2_gen_fused(uint64_t r, uint64_t n, uint64_t d, uint64_t n_start, uint64_t mmax, const uint64_t *C,
                        uint64_t r_C, int gray, const uint64_t *lshifts, uint64_t r_x, const uint64_t *shiftsb,
                        const uint64_t *tmaxes, uint64_t *xrb, double *x, qmc_stream_t s);
+
+/* ---- batched plans: many requests of uneven size, one persistent launch -----
+ * No single reference counterpart: a plan runs, for every request, the chain
+ * of reference calls written next to each struct, bit for bit, in two
+ * launches in total (matrix preparation, then generation), and can replay
+ * them from a CUDA graph.  A plan keeps device copies of the request
+ * descriptors plus scratch for the prepared matrices and a work counter
+ * (allocated when the plan is created).  The arrays the requests point to
+ * are read at run time, so their contents may change between runs; the
+ * pointers may not. */
+
+/* One base-2 digital-net request with r randomisations:
+ *   dnb2_linear_matrix_scramble (if S)  qmctoolscl/c_funcs/dnb2_linear_matrix_scramble.c:3-51
+ *   dnb2_interlace (if alpha > 1)       qmctoolscl/c_funcs/dnb2_interlace.c:3-45
+ *   dnb2_gen_natural / dnb2_gen_gray    qmctoolscl/c_funcs/dnb2_gen_natural.c:3-70, dnb2_gen_gray.c:3-69
+ *   dnb2_digital_shift (if shifts)      qmctoolscl/c_funcs/dnb2_digital_shift.c:3-36 with r_x = r
+ *   dnb2_integer_to_float (if x)        qmctoolscl/c_funcs/dnb2_integer_to_float.c:3-32 */
+typedef struct qmc_net_request {
+    uint64_t r;          /* randomisations */
+    uint64_t n;          /* points */
+    uint64_t d;          /* output dimension (d_pre / alpha) */
+    uint64_t n_start;    /* index of the first point */
+    uint64_t mmax;       /* generating-matrix columns */
+    uint64_t d_pre;      /* dimension of C and S (d * alpha) */
+    uint64_t alpha;      /* interlacing factor, 1 = none */
+    uint64_t tmax;       /* bits of the columns of C (used when S is NULL) */
+    uint64_t tmax_new;   /* bits after scrambling (used when S is set) */
+    uint64_t tmax_alpha; /* bits after interlacing (alpha > 1) */
+    uint64_t r_C;        /* matrix sets in C; randomisation l uses l % r_C */
+    int32_t gray;        /* 0: natural order, 1: Gray order */
+    int32_t reserved;
+    const uint64_t *C;       /* r_C * d_pre * mmax */
+    const uint64_t *S;       /* r * d_pre * tmax_new scrambling rows, or NULL */
+    const uint64_t *lshifts; /* r left shifts (with shifts) */
+    const uint64_t *shifts;  /* r * d digital shifts, or NULL */
+    const uint64_t *tmaxes;  /* r float scalings (with x) */
+    uint64_t *xb;            /* r * n * d integers out, or NULL */
+    double *x;               /* r * n * d floats out, or NULL */
+} qmc_net_request;
+
+/* One rank-1 lattice request with r randomisations:
+ *   lat_gen_natural / lat_gen_gray      qmctoolscl/c_funcs/lat_gen_natural.c:3-58, lat_gen_gray.c:3-56
+ *   lat_shift_mod_1 (if shifts)         qmctoolscl/c_funcs/lat_shift_mod_1.c:3-35 with r_x = r */
+typedef struct qmc_lat_request {
+    uint64_t r, n, d, n_start;
+    int32_t gray;          /* 0: natural order, 1: Gray order */
+    int32_t reserved;
+    const uint64_t *g;     /* r * d generating vectors */
+    const double *shifts;  /* r * d shifts, or NULL */
+    double *x;             /* r * n * d points out */
+} qmc_lat_request;
+
+typedef struct qmc_plan qmc_plan;
+
+int qmc_net_plan_create(const qmc_net_request *reqs, int nreq, qmc_plan **plan);
+int qmc_lat_plan_create(const qmc_lat_request *reqs, int nreq, qmc_plan **plan);
+/* launch the plan on s (two launches for net plans, one for lattice plans) */
+int qmc_plan_run(qmc_plan *plan, qmc_stream_t s);
+/* the same work from a CUDA graph: captured on s at the first call (s must not be
+ * the legacy default stream), replayed afterwards */
+int qmc_plan_graph_launch(qmc_plan *plan, qmc_stream_t s);
+/* launch shape of the generation kernel: CTAs per SM, tiles taken per work-queue
+ * grab, coordinates per tile (rounded to whole rows); 0 keeps a value.  Drops any
+ * captured graph. */
+int qmc_plan_set_tuning(qmc_plan *plan, int ctas_per_sm, int chunk, uint64_t tile_coords);
+/* tiles, coordinates and output bytes of one run, kernel launches per run */
+int qmc_plan_info(const qmc_plan *plan, uint64_t *tiles, uint64_t *coords, uint64_t *bytes_out, int *launches);
+int qmc_plan_destroy(qmc_plan *plan);
 
 #ifdef __cplusplus
 }

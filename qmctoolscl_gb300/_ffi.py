@@ -58,12 +58,30 @@ def lib():
         L.qmc_device_error_check.restype = INT
         L.qmc_device_error_reset.argtypes = [PTR]
         L.qmc_device_error_reset.restype = INT
+        L.qmc_host_pointer_for_device.argtypes = [PTR, ctypes.POINTER(ctypes.c_void_p)]
+        L.qmc_host_pointer_for_device.restype = INT
+        L.qmc_device_attributes.argtypes = [ctypes.POINTER(INT)] * 3
+        L.qmc_device_attributes.restype = INT
         _lib = L
         return _lib
 
 
 def last_error():
     return lib().qmc_last_error().decode(errors="replace")
+
+
+def device_pointer_of_host(ptr):
+    """Device address of pinned host memory at ptr, or None if it is not pinned."""
+    out = ctypes.c_void_p()
+    if lib().qmc_host_pointer_for_device(ctypes.c_void_p(ptr), ctypes.byref(out)) == QMC_OK:
+        return out.value
+    return None
+
+
+def device_attributes():
+    a, b, c = INT(), INT(), INT()
+    check(lib().qmc_device_attributes(ctypes.byref(a), ctypes.byref(b), ctypes.byref(c)), "device_attributes")
+    return {"pageable_access": a.value, "uses_host_page_tables": b.value, "sms": c.value}
 
 
 class QmcError(RuntimeError):

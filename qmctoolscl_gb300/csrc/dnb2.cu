@@ -26,50 +26,35 @@
 // Layout in HBM: xb/xrb/x are r*n*d, d fastest.  Threads walk the CTA's
 // tile as one flat run of (row, column) pairs, so each step of the CTA
 // writes 256 consecutive words.
-#include "common.cuh"
+#include <type_traits>
+
+#include "net_dev.cuh"
 
 namespace {
 
+using net::MAX_COLS;
+using net::to_float_bits;
 constexpr int GEN_THREADS = 256;
-constexpr int MAX_COLS = 64;   // columns per CTA tile
-constexpr int MAX_BITS = 64;   // generating-matrix columns
+constexpr int MAX_BITS = 64;  // generating-matrix columns
 
 struct GenArgs {
     u64 r, n, d, n_start, mmax;
     const u64 *C;        // r_C*d*mmax generating matrices
     u64 r_C;             // randomisation l uses matrix set l % r_C
     u64 *xb;             // r*n*d integer output (may be null when only floats are wanted)
-    double *x;           // r*n*d float output (FLOAT)
-    const u64 *lshifts;  // r_x-periodic left shifts (SHIFT)
-    const u64 *shifts;   // r*d digital shifts (SHIFT)
+    double *x;           // r*n*d float output (may be null)
+    const u64 *lshifts;  // r_x-periodic left shifts (with shifts)
+    const u64 *shifts;   // r*d digital shifts (may be null)
     u64 r_x;             // period of lshifts
-    const u64 *tmaxes;   // r bit counts (FLOAT)
+    const u64 *tmaxes;   // r bit counts (with x)
     u32 K;               // low bits resolved by the table
     u32 col_tiles;       // column tiles per randomisation
     u64 rows_per_cta;
     u64 l_off;           // first randomisation of this launch
 };
 
-__device__ __forceinline__ u64 seq_index(bool gray, u64 n_start, u64 i)
-{
-    const u64 k = n_start + i;
-    return gray ? (k ^ (k >> 1)) : k;
-}
-
-// FP64 fallback kept out of line so its instructions never sit (predicated
-// off) in the per-coordinate loop, where they would load GB300's slow FP64 pipe.
-__device__ __noinline__ double to_float_hw(u64 v, int e) { return ldexp(__ull2double_rn(v), e); }
-
-__device__ __forceinline__ double to_float_bits(u64 v, int e)
-{
-    if (v == 0) return 0.0;
-    const int lz = __clzll((long long)v);
-    const int E = 1085 - lz + e;
-    if (E >= 1 && E <= 2045) return as_double(u64_scaled_bits(v, e));
-    return to_float_hw(v, e);  // subnormal or overflowing results
-}
-
-template <bool GRAY, bool SHIFT, bool FLOAT, bool WRITE_INT>
+// grid x: row blocks; grid y: (randomisation, column tile)
+template <bool GRAY>
 __global__ void __launch_bounds__(GEN_THREADS) dnb2_gen_kernel(GenArgs a)
 {
     extern __shared__ u64 smem[];
@@ -78,98 +63,58 @@ __global__ void __launch_bounds__(GEN_THREADS) dnb2_gen_kernel(GenArgs a)
     const u32 tile = (u32)((u64)blockIdx.y % a.col_tiles);
     const u64 j0 = (u64)tile * MAX_COLS;
     const u32 ncols = (u32)min((u64)MAX_COLS, a.d - j0);
-    const u32 K = a.K;
-    const u32 nlo = 1u << K;
-    const u32 nhi = a.mmax > K ? (u32)(a.mmax - K) : 0u;
-    u64 *T = smem;                     // [nlo][ncols]: low-bit table
-    u64 *H = smem + (u64)nlo * ncols;  // [nhi][ncols]: high-bit columns
-
-    const u64 *Cl = a.C + (l % a.r_C) * a.d * a.mmax;
-    u32 ls = 0;
-    if (SHIFT) ls = (u32)(a.lshifts[l % a.r_x] & 63);
-
-    for (u32 e = threadIdx.x; e < nhi * ncols; e += blockDim.x) {
-        const u32 b = e / ncols, c = e % ncols;
-        H[e] = Cl[(j0 + c) * a.mmax + K + b] << ls;
-    }
-    // T[0] holds the digital shift (it reaches every entry through the
-    // doubling); T[lo + 2^b] = T[lo] ^ (C[b] << ls)
-    for (u32 c = threadIdx.x; c < ncols; c += blockDim.x) T[c] = SHIFT ? a.shifts[l * a.d + j0 + c] : 0ull;
-    __syncthreads();
-    for (u32 b = 0; b < K; b++) {
-        const u32 half = 1u << b;
-        for (u32 e = threadIdx.x; e < half * ncols; e += blockDim.x) {
-            const u32 lo = e / ncols, c = e % ncols;
-            T[(half + lo) * ncols + c] = T[lo * ncols + c] ^ (Cl[(j0 + c) * a.mmax + b] << ls);
-        }
-        __syncthreads();
-    }
-
-    int e_float = 0;
-    if (FLOAT) e_float = (int)(u32)(0ull - a.tmaxes[l]);
-
+    u64 *T = smem;
+    u64 *H = smem + ((u64)1 << a.K) * ncols;
+    const u32 ls = a.shifts ? (u32)(a.lshifts[l % a.r_x] & 63) : 0u;
+    net::build_table(T, H, a.C + (l % a.r_C) * a.d * a.mmax, a.mmax, j0, ncols, a.K, ls,
+                     a.shifts ? a.shifts + l * a.d : nullptr);
+    const int e_float = a.x ? (int)(u32)(0ull - a.tmaxes[l]) : 0;
     const u64 row_begin = (u64)blockIdx.x * a.rows_per_cta;
     if (row_begin >= a.n) return;
     const u64 row_end = min(a.n, row_begin + a.rows_per_cta);
-    const u64 total = (row_end - row_begin) * ncols;
-    // walk the tile's (row, column) pairs as one flat run: each step of the
-    // CTA covers GEN_THREADS consecutive coordinates
-    const u32 step_rows = GEN_THREADS / ncols, step_cols = GEN_THREADS % ncols;
-    u64 row = row_begin + threadIdx.x / ncols;
-    u32 col = threadIdx.x % ncols;
-    u64 hi_key = ~0ull, hx = 0;
-    u32 col_key = ~0u;
-    u64 *xb_l = WRITE_INT ? a.xb + l * a.n * a.d + j0 : nullptr;
-    double *x_l = FLOAT ? a.x + l * a.n * a.d + j0 : nullptr;
-    for (u64 f = threadIdx.x; f < total; f += GEN_THREADS) {
-        const u64 m = seq_index(GRAY, a.n_start, row);
-        const u64 hi = m >> K;
-        if (hi != hi_key || col != col_key) {
-            // XOR of the high-bit columns picked by the set bits of hi;
-            // changes only every 2^K rows
-            hx = 0;
-            for (u64 hb = hi; hb; hb &= hb - 1) hx ^= H[(__ffsll((long long)hb) - 1) * ncols + col];
-            hi_key = hi;
-            col_key = col;
-        }
-        const u64 v = T[(u32)(m & (nlo - 1)) * ncols + col] ^ hx;
-        const u64 o = row * a.d + col;
-        if (WRITE_INT) __stcs(xb_l + o, v);
-        if (FLOAT) __stcs(x_l + o, to_float_bits(v, e_float));
-        row += step_rows;
-        col += step_cols;
-        if (col >= ncols) {
-            col -= ncols;
-            row += 1;
-        }
-    }
+    net::gen_rows<GRAY>(T, H, a.K, ncols, a.n_start, a.d, row_begin, row_end,
+                        a.xb ? a.xb + l * a.n * a.d + j0 : nullptr, a.x ? a.x + l * a.n * a.d + j0 : nullptr,
+                        e_float);
 }
 
 // ---------------------------------------------------------------------------
 // elementwise kernels
 
+// Rows per thread per iteration: all loads of a group are issued before any
+// arithmetic so each thread keeps several loads outstanding.
+constexpr int ROWS_IN_FLIGHT = 4;
+
 template <int VEC>
 __global__ void __launch_bounds__(256) dnb2_shift_kernel(u64 r, u64 n, u64 d, u64 r_x, const u64 *lshifts,
                                                          const u64 *xb, const u64 *shiftsb, u64 *xrb)
 {
+    typedef typename std::conditional<VEC == 2, ulonglong2, u64>::type vec_t;
     const u64 ngroups = (d + VEC - 1) / VEC;
     const u64 row_stride = (u64)gridDim.x * blockDim.y;
+    const u64 dv = d / VEC;
     for (u64 l = blockIdx.y; l < r; l += gridDim.y) {
         const u32 ls = (u32)(lshifts[l % r_x] & 63);
-        const u64 *in = xb + (l % r_x) * n * d;
-        u64 *out = xrb + l * n * d;
+        const vec_t *in = (const vec_t *)(xb + (l % r_x) * n * d);
+        vec_t *out = (vec_t *)(xrb + l * n * d);
         for (u64 jg = threadIdx.x; jg < ngroups; jg += blockDim.x) {
-            const u64 j0 = jg * VEC;
             u64 s[VEC];
 #pragma unroll
-            for (int v = 0; v < VEC; v++) s[v] = shiftsb[l * d + j0 + v];
-            for (u64 i = (u64)blockIdx.x * blockDim.y + threadIdx.y; i < n; i += row_stride) {
-                const u64 o = i * d + j0;
-                if (VEC == 2) {
-                    const ulonglong2 w = __ldcs((const ulonglong2 *)(in + o));
-                    __stcs((ulonglong2 *)(out + o), make_ulonglong2((w.x << ls) ^ s[0], (w.y << ls) ^ s[1]));
-                } else {
-                    __stcs(out + o, (__ldcs(in + o) << ls) ^ s[0]);
+            for (int v = 0; v < VEC; v++) s[v] = shiftsb[l * d + jg * VEC + v];
+            for (u64 i0 = (u64)blockIdx.x * blockDim.y + threadIdx.y; i0 < n; i0 += ROWS_IN_FLIGHT * row_stride) {
+                vec_t w[ROWS_IN_FLIGHT];
+#pragma unroll
+                for (int u = 0; u < ROWS_IN_FLIGHT; u++) {
+                    const u64 i = i0 + u * row_stride;
+                    if (i < n) w[u] = __ldcs(in + i * dv + jg);
+                }
+#pragma unroll
+                for (int u = 0; u < ROWS_IN_FLIGHT; u++) {
+                    const u64 i = i0 + u * row_stride;
+                    if (i >= n) break;
+                    if constexpr (VEC == 2)
+                        __stcs(out + i * dv + jg, make_ulonglong2((w[u].x << ls) ^ s[0], (w[u].y << ls) ^ s[1]));
+                    else
+                        __stcs(out + i * dv + jg, (w[u] << ls) ^ s[0]);
                 }
             }
         }
@@ -180,21 +125,31 @@ template <int VEC>
 __global__ void __launch_bounds__(256) dnb2_to_float_kernel(u64 r, u64 n, u64 d, const u64 *tmaxes,
                                                             const u64 *xb, double *x)
 {
+    typedef typename std::conditional<VEC == 2, ulonglong2, u64>::type in_t;
+    typedef typename std::conditional<VEC == 2, double2, double>::type out_t;
     const u64 ngroups = (d + VEC - 1) / VEC;
     const u64 row_stride = (u64)gridDim.x * blockDim.y;
+    const u64 dv = d / VEC;
     for (u64 l = blockIdx.y; l < r; l += gridDim.y) {
         const int e = (int)(u32)(0ull - tmaxes[l]);
-        const u64 *in = xb + l * n * d;
-        double *out = x + l * n * d;
+        const in_t *in = (const in_t *)(xb + l * n * d);
+        out_t *out = (out_t *)(x + l * n * d);
         for (u64 jg = threadIdx.x; jg < ngroups; jg += blockDim.x) {
-            const u64 j0 = jg * VEC;
-            for (u64 i = (u64)blockIdx.x * blockDim.y + threadIdx.y; i < n; i += row_stride) {
-                const u64 o = i * d + j0;
-                if (VEC == 2) {
-                    const ulonglong2 w = __ldcs((const ulonglong2 *)(in + o));
-                    __stcs((double2 *)(out + o), make_double2(to_float_bits(w.x, e), to_float_bits(w.y, e)));
-                } else {
-                    __stcs(out + o, to_float_bits(__ldcs(in + o), e));
+            for (u64 i0 = (u64)blockIdx.x * blockDim.y + threadIdx.y; i0 < n; i0 += ROWS_IN_FLIGHT * row_stride) {
+                in_t w[ROWS_IN_FLIGHT];
+#pragma unroll
+                for (int u = 0; u < ROWS_IN_FLIGHT; u++) {
+                    const u64 i = i0 + u * row_stride;
+                    if (i < n) w[u] = __ldcs(in + i * dv + jg);
+                }
+#pragma unroll
+                for (int u = 0; u < ROWS_IN_FLIGHT; u++) {
+                    const u64 i = i0 + u * row_stride;
+                    if (i >= n) break;
+                    if constexpr (VEC == 2)
+                        __stcs(out + i * dv + jg, make_double2(to_float_bits(w[u].x, e), to_float_bits(w[u].y, e)));
+                    else
+                        __stcs(out + i * dv + jg, to_float_bits(w[u], e));
                 }
             }
         }
@@ -296,19 +251,11 @@ unsigned flat_grid(u64 total) { return qmcgb::grid_for(total, 256, (unsigned)qmc
 
 bool aligned16(const void *p) { return ((uintptr_t)p & 15u) == 0; }
 
-// Largest K <= min(mmax, 8) whose table of 2^K x ncols words fits 32 KB.
-u32 pick_K(u64 mmax, u32 ncols)
-{
-    u32 K = (u32)(mmax < 8 ? mmax : 8);
-    while (K > 0 && ((u64)ncols << K) * 8 > 32768) K--;
-    return K;
-}
-
-template <bool GRAY, bool SHIFT, bool FLOAT, bool WRITE_INT>
+template <bool GRAY>
 int launch_gen(GenArgs a, cudaStream_t s, const char *what)
 {
     const u32 ncols = (u32)(a.d < MAX_COLS ? a.d : MAX_COLS);
-    a.K = pick_K(a.mmax, ncols);
+    a.K = net::pick_K(a.mmax, ncols);
     a.col_tiles = (u32)((a.d + MAX_COLS - 1) / MAX_COLS);
     const u64 units = a.r * a.col_tiles;
     // enough CTAs to fill the GPU several times; each CTA covers a row run of
@@ -320,8 +267,8 @@ int launch_gen(GenArgs a, cudaStream_t s, const char *what)
     if (splits > max_splits) splits = max_splits;
     if (splits < 1) splits = 1;
     a.rows_per_cta = (a.n + splits - 1) / splits;
-    const size_t smem = ((size_t(1) << a.K) + (a.mmax > a.K ? a.mmax - a.K : 0)) * ncols * sizeof(u64);
-    auto kern = dnb2_gen_kernel<GRAY, SHIFT, FLOAT, WRITE_INT>;
+    const size_t smem = net::table_words(a.K, a.mmax, ncols) * sizeof(u64);
+    auto kern = dnb2_gen_kernel<GRAY>;
     if (smem > 48 * 1024) {
         cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return qmcgb::cuda_status(e, what);
@@ -380,13 +327,8 @@ int dnb2_gen_fused(u64 r, u64 n, u64 d, u64 n_start, u64 mmax, const u64 *C, u64
     QMC_REQUIRE(!sh || lshifts, "shift stage needs lshifts");
     QMC_REQUIRE(!fl || tmaxes, "float stage needs tmaxes");
     QMC_REQUIRE(fl || wi, "nothing to write");
-#define GEN_CASE(G, S, F, W) \
-    if (gray == G && sh == S && fl == F && wi == W) return launch_gen<G, S, F, W>(a, s, "dnb2_gen");
-    GEN_CASE(0, 0, 0, 1) GEN_CASE(1, 0, 0, 1) GEN_CASE(0, 1, 0, 1) GEN_CASE(1, 1, 0, 1)
-    GEN_CASE(0, 0, 1, 1) GEN_CASE(1, 0, 1, 1) GEN_CASE(0, 1, 1, 1) GEN_CASE(1, 1, 1, 1)
-    GEN_CASE(0, 0, 1, 0) GEN_CASE(1, 0, 1, 0) GEN_CASE(0, 1, 1, 0) GEN_CASE(1, 1, 1, 0)
-#undef GEN_CASE
-    return QMC_ERR_ARG;
+    (void)sh;
+    return gray ? launch_gen<true>(a, s, "dnb2_gen") : launch_gen<false>(a, s, "dnb2_gen");
 }
 
 int dnb2_check_gen(u64 n, u64 n_start, u64 mmax, int natural)

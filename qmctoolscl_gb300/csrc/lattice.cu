@@ -5,17 +5,8 @@
 // Reference: qmctoolscl/c_funcs/lat_gen_linear.c:3-33,
 // lat_gen_natural.c:3-58, lat_gen_gray.c:3-56, lat_shift_mod_1.c:3-35.
 //
-// Closed form.  The reference walks a Gray-code recurrence; the value it
-// writes is fmod((double)g * V, 1) with V = ldexp(v, -p), where for a row
-// whose sequence index is m (m = n_start+k in natural order, the Gray code
-// of n_start+i in Gray order), p = bitlen(m) and v = m bit-reversed in p
-// bits -- i.e. V is the van der Corput radical inverse of m.  With
-// B = bitreverse64(m), V = B * 2^-64 exactly.  When bitlen(g) + p <= 53 the
-// double product g*V is exact, so fmod(g*V, 1) = (g*B mod 2^64) * 2^-64:
-// one 64-bit integer multiply gives the fraction in 0.64 fixed point and
-// fix64_to_double turns it into the double bit pattern.  Other columns take
-// the FP64 instructions the reference's formula names (same rounding, slower
-// on GB300).
+// The per-point arithmetic (closed form of the reference's recurrence,
+// exact integer emulation of its FP64 roundings) is in lattice_dev.cuh.
 //
 // The mod-1 shift adds a double shift and drops the integer part.  When
 // both operands are multiples of 2^-64 in [0,1) (lattice points are, and
@@ -25,232 +16,33 @@
 // Layout in HBM: x and xr are r*n*d doubles, d fastest.  A warp covers one
 // row (or several short rows) with 16-byte stores when d is even and the
 // output is 16-byte aligned, so each warp store is one contiguous span.
-#include "common.cuh"
+#include "lattice_dev.cuh"
 
 namespace {
 
-enum LatOrder { ORDER_LINEAR_POW2 = 0, ORDER_LINEAR_GENERIC = 1, ORDER_NATURAL = 2, ORDER_GRAY = 3 };
+using lat::bitlen;
 
 struct LatArgs {
     u64 r, n, d, n_start;
     const u64 *g;          // r*d
     const double *shifts;  // r*d, only with SHIFT
     double *out;           // r*n*d
-    u32 log2n;             // ORDER_LINEAR_POW2
-    u32 pmax;              // bit length of the largest sequence index
+    u32 p;                 // bit length of the largest sequence index (log2 n for linear order)
+    bool narrow;           // every sequence index below 2^32
 };
 
-// Per-column constants, prepared once per thread and column.
-struct LatCol {
-    u64 g;
-    double gd;   // (double)g, RN as the reference converts it
-    u64 S;       // shift in 0.64 fixed point
-    double s;
-    bool fast;   // exact integer generation
-    u32 shift_kind;  // 0: 0.64 with 11 zero low bits, 1: 0.64, 2: FP64 add
-};
-
-__device__ __forceinline__ u64 row_index(int order, u64 n_start, u64 i)
-{
-    if (order == ORDER_GRAY) {
-        const u64 k = n_start + i;
-        return k ^ (k >> 1);
-    }
-    return n_start + i;
-}
-
-__device__ __forceinline__ LatCol load_col(const LatArgs &a, u64 l, u64 j, bool with_shift, int order)
-{
-    LatCol c;
-    c.g = a.g[l * a.d + j];
-    c.gd = __ull2double_rn(c.g);
-    const u32 bits_g = 64 - __clzll((long long)c.g);
-    const u32 p = (order == ORDER_LINEAR_POW2) ? a.log2n : a.pmax;
-    c.fast = (order != ORDER_LINEAR_GENERIC) && (bits_g + p <= 53) && (p <= 53);
-    c.S = 0;
-    c.s = 0.0;
-    c.shift_kind = 2;
-    if (with_shift) {
-        c.s = a.shifts[l * a.d + j];
-        u64 S;
-        if (double_to_fix64(c.s, &S)) {
-            c.S = S;
-            c.shift_kind = (S & 0x7FFull) ? 1u : 0u;
-        }
-    }
-    return c;
-}
-
-// fmod(g*V, 1) as the reference computes it, for sequence index m, with
-// FP64 instructions.  Kept out of line: GB300's FP64 pipe is slow, and if
-// the compiler if-converted these fallbacks into the per-element loop their
-// (predicated-off) FP64 instructions would still be issued for every
-// coordinate and saturate that pipe.
-__device__ __noinline__ double lat_value_hw(double gd, int order, u64 m, u64 i, u64 n)
-{
-    if (order == ORDER_LINEAR_POW2 || order == ORDER_LINEAR_GENERIC) {
-        const double q = __ddiv_rn(__ull2double_rn(i), __ull2double_rn(n));
-        return frac_mod1(__dmul_rn(gd, q));
-    }
-    const int p = m ? 64 - __clzll((long long)m) : 0;
-    const u64 v = m ? (__brevll(m) >> (64 - p)) : 0;
-    const double V = scalbn(__ull2double_rn(v), -p);
-    return frac_mod1(__dmul_rn(gd, V));
-}
-
-// Every case other than the common one: exact integer generation with a
-// shift that needs general rounding, or FP64 generation/shift.
-__device__ __noinline__ double lat_point_general(const LatCol &c, int order, u64 B, u64 m, u64 i, u64 n,
-                                                 bool shift)
-{
-    double x;
-    if (c.fast) {
-        const u64 W = c.g * B;
-        if (!shift) return fix64_to_double(W);
-        if (c.shift_kind == 1) return fix64_to_double(add_mod1_fix64(W, c.S));
-        x = fix64_to_double(W);
-    } else {
-        x = lat_value_hw(c.gd, order, m, i, n);
-        if (!shift) return x;
-    }
-    return frac_mod1(__dadd_rn(x, c.s));
-}
-
-template <bool SHIFT>
-__device__ __forceinline__ double lat_point(const LatCol &c, int order, u64 B, u64 m, u64 i, u64 n)
-{
-    if (c.fast && (!SHIFT || c.shift_kind == 0)) {
-        const u64 W = c.g * B;  // fraction of g*V in 0.64 fixed point (<= 53 significant bits)
-        if (!SHIFT) return fix64_to_double(W);
-        // W and S are multiples of 2^-53: the sum needs rounding only when it
-        // reaches 1, and then only a tie on bit 11 can occur
-        u64 T = W + c.S;
-        if (T < W) T = (T + ((T >> 1) & 0x800ull)) & ~0xFFFull;
-        return fix64_to_double(T);
-    }
-    return lat_point_general(c, order, B, m, i, n, SHIFT);
-}
-
-// Exact double of (th:tl) * 2^-64 for th != 0 and at most 53 significant
-// bits, on 32-bit halves: normalise with one funnel shift, drop 11 bits with
-// another, add the exponent into the high word.
-__device__ __forceinline__ double fix64_hi_to_double(u32 th, u32 tl)
-{
-    const u32 lz = __clz(th);
-    const u32 hi = __funnelshift_l(tl, th, lz);
-    const u32 lo = tl << lz;
-    const u32 m_lo = __funnelshift_r(lo, hi, 11);
-    const u32 m_hi = (hi >> 11) + ((1021u - lz) << 20);
-    return __hiloint2double((int)m_hi, (int)m_lo);
-}
-
-// fmod(point + shift, 1) for the narrow case (every sequence index below
-// 2^32, so B = bitreverse64(m) has a zero low word and the fraction
-// g*B mod 2^64 is (g mod 2^32) * bitreverse32(m) in the high word); the shift
-// is a multiple of 2^-53 in 0.64 fixed point (sh:sl).
-template <bool SHIFT>
-__device__ __forceinline__ double lat_point_narrow(u32 g_lo, u32 bh, u32 sh, u32 sl, const LatCol &c, int order,
-                                                   u64 m, u64 i, u64 n)
-{
-    const u32 wh = g_lo * bh;
-    if (!SHIFT) return wh ? fix64_hi_to_double(wh, 0u) : 0.0;
-    u32 th = wh + sh, tl = sl;
-    if (th < wh) {  // the sum reached 1: round to the 2^-52 grid (ties to even), drop the 1
-        const u64 t = ((((u64)th << 32) | tl) + ((tl >> 1) & 0x800u)) & ~0xFFFull;
-        th = (u32)(t >> 32);
-        tl = (u32)t;
-    }
-    if (th) return fix64_hi_to_double(th, tl);
-    return fix64_to_double(((u64)th << 32) | tl);  // results below 2^-32
-}
-
-template <int ORDER, bool SHIFT, int VEC>
-__global__ void __launch_bounds__(256) lat_gen_narrow_kernel(LatArgs a)
-{
-    // every index n_start + i < 2^32 and every column on the exact integer
-    // path with (for SHIFT) a shift on the 2^-53 grid: checked per column,
-    // with the general per-element code for columns that are not
-    const u32 ngroups = (u32)((a.d + VEC - 1) / VEC);
-    const u32 row_stride = gridDim.x * blockDim.y;
-    const u32 n = (u32)a.n, n_start = (u32)a.n_start;
-    for (u64 l = blockIdx.y; l < a.r; l += gridDim.y) {
-        for (u32 jg = threadIdx.x; jg < ngroups; jg += blockDim.x) {
-            const u64 j0 = (u64)jg * VEC;
-            LatCol c[VEC];
-            bool easy = true;
-#pragma unroll
-            for (int v = 0; v < VEC; v++) {
-                c[v] = load_col(a, l, j0 + v, SHIFT, ORDER);
-                easy &= c[v].fast && (!SHIFT || c[v].shift_kind == 0);
-            }
-            u32 g_lo[VEC], sh[VEC], sl[VEC];
-#pragma unroll
-            for (int v = 0; v < VEC; v++) {
-                g_lo[v] = (u32)c[v].g;
-                sh[v] = (u32)(c[v].S >> 32);
-                sl[v] = (u32)c[v].S;
-            }
-            double *out = a.out + l * a.n * a.d + j0;
-            for (u32 i = blockIdx.x * blockDim.y + threadIdx.y; i < n; i += row_stride) {
-                u32 bh, m32;
-                if (ORDER == ORDER_LINEAR_POW2) {
-                    m32 = i;
-                    bh = a.log2n ? (i << (32 - a.log2n)) : 0u;  // log2n <= 32 here
-                } else {
-                    const u32 k = n_start + i;
-                    m32 = (ORDER == ORDER_GRAY) ? (k ^ (k >> 1)) : k;
-                    bh = __brev(m32);
-                }
-                double y[VEC];
-                if (easy) {
-#pragma unroll
-                    for (int v = 0; v < VEC; v++)
-                        y[v] = lat_point_narrow<SHIFT>(g_lo[v], bh, sh[v], sl[v], c[v], ORDER, m32, i, a.n);
-                } else {
-#pragma unroll
-                    for (int v = 0; v < VEC; v++)
-                        y[v] = lat_point_general(c[v], ORDER, (u64)bh << 32, m32, i, a.n, SHIFT);
-                }
-                if (VEC == 2) {
-                    __stcs((double2 *)(out + (u64)i * a.d), make_double2(y[0], y[1]));
-                } else {
-                    __stcs(out + (u64)i * a.d, y[0]);
-                }
-            }
-        }
-    }
-}
-
+// threadIdx.x over column groups, threadIdx.y over rows; grid x over row
+// blocks, y over randomisations
 template <int ORDER, bool SHIFT, int VEC>
 __global__ void __launch_bounds__(256) lat_gen_kernel(LatArgs a)
 {
     const u64 ngroups = (a.d + VEC - 1) / VEC;
     const u64 row_stride = (u64)gridDim.x * blockDim.y;
-    for (u64 l = blockIdx.y; l < a.r; l += gridDim.y) {
-        for (u64 jg = threadIdx.x; jg < ngroups; jg += blockDim.x) {
-            const u64 j0 = jg * VEC;
-            LatCol c[VEC];
-#pragma unroll
-            for (int v = 0; v < VEC; v++) c[v] = load_col(a, l, j0 + v, SHIFT, ORDER);
-            double *out = a.out + l * a.n * a.d + j0;
-            for (u64 i = (u64)blockIdx.x * blockDim.y + threadIdx.y; i < a.n; i += row_stride) {
-                const u64 m = row_index(ORDER, a.n_start, i);
-                u64 B;
-                if (ORDER == ORDER_LINEAR_POW2)
-                    B = a.log2n ? (i << (64 - a.log2n)) : 0;
-                else
-                    B = __brevll(m);
-                double y[VEC];
-#pragma unroll
-                for (int v = 0; v < VEC; v++) y[v] = lat_point<SHIFT>(c[v], ORDER, B, m, i, a.n);
-                if (VEC == 2) {
-                    __stcs((double2 *)(out + i * a.d), make_double2(y[0], y[1]));
-                } else {
-                    __stcs(out + i * a.d, y[0]);
-                }
-            }
-        }
-    }
+    for (u64 l = blockIdx.y; l < a.r; l += gridDim.y)
+        for (u64 jg = threadIdx.x; jg < ngroups; jg += blockDim.x)
+            lat::rows<ORDER, SHIFT, VEC>(a.g + l * a.d, SHIFT ? a.shifts + l * a.d : nullptr, a.out + l * a.n * a.d,
+                                         a.d, a.n, a.n_start, a.p, jg, (u64)blockIdx.x * blockDim.y + threadIdx.y,
+                                         a.n, row_stride, a.narrow);
 }
 
 struct ShiftArgs {
@@ -262,38 +54,83 @@ struct ShiftArgs {
 
 __device__ __noinline__ double shift_one_hw(double x, double s) { return frac_mod1(__dadd_rn(x, s)); }
 
-__device__ __forceinline__ double shift_one(double x, u64 S, bool s_ok, double s)
+__device__ __noinline__ double shift_one_fix64(double x, u64 S, bool s_ok, double s)
 {
     u64 X;
     if (s_ok && double_to_fix64(x, &X)) return fix64_to_double(add_mod1_fix64(X, S));
     return shift_one_hw(x, s);
 }
 
+// fmod(RN(x + s), 1) when s is on the 2^-53 grid in [0,1) (K = s*2^53, as
+// numpy's random() draws) and x is too (lattice points with up to 2^53
+// points are): F = x*2^53 is then an integer, the sum F+K needs rounding only
+// when it reaches 2^53 (spacing 2 there, ties to even), and the result is
+// exact.  Other inputs take the general 0.64 fixed-point or FP64 path.
+__device__ __forceinline__ double shift_one(double x, u64 K, bool k_ok, u64 S, bool s_ok, double s)
+{
+    const u64 b = as_bits(x);
+    const u32 E = (u32)(b >> 52);  // sign bit included: negatives fail
+    const u32 sh = 1022u - E;      // x = M * 2^(E-1075) = (M >> sh) * 2^-53
+    const u64 M = (b & 0xFFFFFFFFFFFFFull) | (1ull << 52);
+    if (k_ok && E <= 1022u && sh <= 52u && (M & ((1ull << sh) - 1)) == 0) {
+        u64 T = (M >> sh) + K;
+        if (T >> 53) {  // sum in [1, 2): round to even on bit 0, drop the 1
+            T += (T & 1) & (T >> 1);
+            T = (T & ~1ull) - (1ull << 53);
+            T &= (1ull << 53) - 1;  // a sum that rounded up to 2 leaves 0
+        }
+        return T ? fix64_to_double(T << 11) : 0.0;
+    }
+    if (b == 0 && k_ok) return s;  // x = +0: the sum is s itself
+    return shift_one_fix64(x, S, s_ok, s);
+}
+
+// Rows per thread per iteration: all loads of a group are issued before
+// any arithmetic, so each thread keeps ROWS_IN_FLIGHT loads outstanding (the
+// bytes in flight per SM that a streaming kernel needs to reach HBM speed).
+constexpr int ROWS_IN_FLIGHT = 4;
+
 template <int VEC>
 __global__ void __launch_bounds__(256) lat_shift_kernel(ShiftArgs a)
 {
+    typedef typename std::conditional<VEC == 2, double2, double>::type vec_t;
     const u64 ngroups = (a.d + VEC - 1) / VEC;
     const u64 row_stride = (u64)gridDim.x * blockDim.y;
     for (u64 l = blockIdx.y; l < a.r; l += gridDim.y) {
         for (u64 jg = threadIdx.x; jg < ngroups; jg += blockDim.x) {
             const u64 j0 = jg * VEC;
             double s[VEC];
-            u64 S[VEC];
-            bool ok[VEC];
+            u64 S[VEC], K[VEC];
+            bool ok[VEC], kok[VEC];
 #pragma unroll
             for (int v = 0; v < VEC; v++) {
                 s[v] = a.shifts[l * a.d + j0 + v];
                 ok[v] = double_to_fix64(s[v], &S[v]);
+                kok[v] = ok[v] && (S[v] & 0x7FFull) == 0;
+                K[v] = S[v] >> 11;
             }
-            const double *xin = a.x + (l % a.r_x) * a.n * a.d + j0;
-            double *out = a.xr + l * a.n * a.d + j0;
-            for (u64 i = (u64)blockIdx.x * blockDim.y + threadIdx.y; i < a.n; i += row_stride) {
-                if (VEC == 2) {
-                    const double2 xv = __ldcs((const double2 *)(xin + i * a.d));
-                    __stcs((double2 *)(out + i * a.d),
-                           make_double2(shift_one(xv.x, S[0], ok[0], s[0]), shift_one(xv.y, S[1], ok[1], s[1])));
-                } else {
-                    __stcs(out + i * a.d, shift_one(__ldcs(xin + i * a.d), S[0], ok[0], s[0]));
+            const vec_t *xin = (const vec_t *)(a.x + (l % a.r_x) * a.n * a.d + j0);
+            vec_t *out = (vec_t *)(a.xr + l * a.n * a.d + j0);
+            const u64 dv = a.d / VEC;  // row pitch in vec_t units (d % VEC == 0 when VEC == 2)
+            for (u64 i0 = (u64)blockIdx.x * blockDim.y + threadIdx.y; i0 < a.n; i0 += ROWS_IN_FLIGHT * row_stride) {
+                vec_t xv[ROWS_IN_FLIGHT];
+#pragma unroll
+                for (int u = 0; u < ROWS_IN_FLIGHT; u++) {
+                    const u64 i = i0 + u * row_stride;
+                    if (i < a.n) xv[u] = __ldcs(xin + i * dv);
+                }
+#pragma unroll
+                for (int u = 0; u < ROWS_IN_FLIGHT; u++) {
+                    const u64 i = i0 + u * row_stride;
+                    if (i >= a.n) break;
+                    vec_t y;
+                    if constexpr (VEC == 2) {
+                        y = make_double2(shift_one(xv[u].x, K[0], kok[0], S[0], ok[0], s[0]),
+                                         shift_one(xv[u].y, K[1], kok[1], S[1], ok[1], s[1]));
+                    } else {
+                        y = shift_one(xv[u], K[0], kok[0], S[0], ok[0], s[0]);
+                    }
+                    __stcs(out + i * dv, y);
                 }
             }
         }
@@ -328,27 +165,18 @@ Shape shape_for(u64 r, u64 n, u64 ngroups)
 
 bool aligned16(const void *p) { return ((uintptr_t)p & 15u) == 0; }
 
-u32 bitlen(u64 v) { return v ? 64u - (u32)__builtin_clzll(v) : 0u; }
-
 template <int ORDER, bool SHIFT>
-int launch_gen(const LatArgs &a, cudaStream_t s, const char *what)
+int launch_gen(LatArgs a, cudaStream_t s, const char *what)
 {
     const bool vec2 = (a.d % 2 == 0) && aligned16(a.out);
     const u64 ngroups = vec2 ? a.d / 2 : a.d;
     const Shape sh = shape_for(a.r, a.n, ngroups);
-    // 32-bit indexing: every sequence index below 2^32
-    const bool narrow = ORDER != ORDER_LINEAR_GENERIC && a.n_start + a.n <= (1ull << 32) &&
-                        a.n_start + a.n >= a.n_start && (ORDER != ORDER_LINEAR_POW2 || a.log2n <= 32);
-    if (narrow) {
-        if (vec2)
-            lat_gen_narrow_kernel<ORDER, SHIFT, 2><<<sh.grid, sh.block, 0, s>>>(a);
-        else
-            lat_gen_narrow_kernel<ORDER, SHIFT, 1><<<sh.grid, sh.block, 0, s>>>(a);
-    } else if (vec2) {
+    a.narrow = ORDER != lat::LINEAR_GENERIC && a.n_start + a.n <= (1ull << 32) && a.n_start + a.n >= a.n_start &&
+               a.p <= 32;
+    if (vec2)
         lat_gen_kernel<ORDER, SHIFT, 2><<<sh.grid, sh.block, 0, s>>>(a);
-    } else {
+    else
         lat_gen_kernel<ORDER, SHIFT, 1><<<sh.grid, sh.block, 0, s>>>(a);
-    }
     return qmcgb::launch_status(what);
 }
 
@@ -369,9 +197,9 @@ int lat_gen_shift(u64 r, u64 n, u64 d, u64 n_start, int gray, const u64 *g, cons
                   double *xr, cudaStream_t s)
 {
     if (r == 0 || n == 0 || d == 0) return QMC_OK;
-    LatArgs a{r, n, d, n_start, g, shifts, xr, 0, bitlen(n_start + n - 1)};
-    return gray ? launch_gen<ORDER_GRAY, true>(a, s, "lat_gen_shift")
-                : launch_gen<ORDER_NATURAL, true>(a, s, "lat_gen_shift");
+    LatArgs a{r, n, d, n_start, g, shifts, xr, bitlen(n_start + n - 1), false};
+    return gray ? launch_gen<lat::GRAY, true>(a, s, "lat_gen_shift")
+                : launch_gen<lat::NATURAL, true>(a, s, "lat_gen_shift");
 }
 
 }  // namespace qmcgb
@@ -383,9 +211,9 @@ int qmc_lat_gen_linear(uint64_t r, uint64_t n, uint64_t d, const uint64_t *g, do
     if (int rc = check_common(r, n, d, g, x)) return rc;
     if (r == 0 || n == 0 || d == 0) return QMC_OK;
     const bool pow2 = (n & (n - 1)) == 0;
-    LatArgs a{r, n, d, 0, (const u64 *)g, nullptr, x, pow2 ? bitlen(n) - 1 : 0, 0};
-    return pow2 ? launch_gen<ORDER_LINEAR_POW2, false>(a, QMC_STREAM(s), "lat_gen_linear")
-                : launch_gen<ORDER_LINEAR_GENERIC, false>(a, QMC_STREAM(s), "lat_gen_linear");
+    LatArgs a{r, n, d, 0, (const u64 *)g, nullptr, x, pow2 ? bitlen(n) - 1 : 64, false};
+    return pow2 ? launch_gen<lat::LINEAR_POW2, false>(a, QMC_STREAM(s), "lat_gen_linear")
+                : launch_gen<lat::LINEAR_GENERIC, false>(a, QMC_STREAM(s), "lat_gen_linear");
 }
 
 int qmc_lat_gen_natural(uint64_t r, uint64_t n, uint64_t d, uint64_t n_start, const uint64_t *g,
@@ -395,8 +223,8 @@ int qmc_lat_gen_natural(uint64_t r, uint64_t n, uint64_t d, uint64_t n_start, co
                 "lat_gen_natural requires n_start and n+n_start are either 0 or powers of 2");
     if (int rc = check_common(r, n, d, g, x)) return rc;
     if (r == 0 || n == 0 || d == 0) return QMC_OK;
-    LatArgs a{r, n, d, n_start, (const u64 *)g, nullptr, x, 0, bitlen(n_start + n - 1)};
-    return launch_gen<ORDER_NATURAL, false>(a, QMC_STREAM(s), "lat_gen_natural");
+    LatArgs a{r, n, d, n_start, (const u64 *)g, nullptr, x, bitlen(n_start + n - 1), false};
+    return launch_gen<lat::NATURAL, false>(a, QMC_STREAM(s), "lat_gen_natural");
 }
 
 int qmc_lat_gen_gray(uint64_t r, uint64_t n, uint64_t d, uint64_t n_start, const uint64_t *g,
@@ -404,8 +232,8 @@ int qmc_lat_gen_gray(uint64_t r, uint64_t n, uint64_t d, uint64_t n_start, const
 {
     if (int rc = check_common(r, n, d, g, x)) return rc;
     if (r == 0 || n == 0 || d == 0) return QMC_OK;
-    LatArgs a{r, n, d, n_start, (const u64 *)g, nullptr, x, 0, bitlen(n_start + n - 1)};
-    return launch_gen<ORDER_GRAY, false>(a, QMC_STREAM(s), "lat_gen_gray");
+    LatArgs a{r, n, d, n_start, (const u64 *)g, nullptr, x, bitlen(n_start + n - 1), false};
+    return launch_gen<lat::GRAY, false>(a, QMC_STREAM(s), "lat_gen_gray");
 }
 
 int qmc_lat_shift_mod_1(uint64_t r, uint64_t n, uint64_t d, uint64_t r_x, const double *x,

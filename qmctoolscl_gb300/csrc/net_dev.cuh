@@ -1,0 +1,125 @@
+// net_dev.cuh -- tile-level device code of the base-2 digital-net
+// generator, shared by the per-call kernel (dnb2.cu) and the batched
+// persistent kernel (batch.cu).
+//
+// Reference: qmctoolscl/c_funcs/dnb2_gen_natural.c:23-69,
+// dnb2_gen_gray.c:23-68, dnb2_digital_shift.c:25-35,
+// dnb2_integer_to_float.c:22-32.
+//
+// The point with sequence index m (natural order m = n_start+k, Gray order
+// m = gray(n_start+i)) is the XOR of the generating-matrix columns picked by
+// the set bits of m -- the closed form of the reference's recurrence.  A CTA
+// stages, for one randomisation and a tile of up to 64 columns, the table
+// T[lo][c] of XORs for the K low index bits (built by doubling) and the
+// columns H[b][c] for the high bits.  A coordinate is then T[m mod 2^K] ^
+// (XOR of H over the set bits of m >> K), the second term changing only every
+// 2^K rows.  The digital shift (x << ls) ^ s distributes over XOR and is
+// folded into T and H; the float conversion is done before the store.
+#pragma once
+
+#include "common.cuh"
+
+namespace net {
+namespace {  // internal linkage: included by several translation units
+
+constexpr int MAX_COLS = 64;  // columns per table
+constexpr int MAX_K = 8;      // low index bits resolved by the table
+
+__device__ __forceinline__ u64 seq_index(bool gray, u64 n_start, u64 i)
+{
+    const u64 k = n_start + i;
+    return gray ? (k ^ (k >> 1)) : k;
+}
+
+// FP64 fallback kept out of line so its instructions never sit (predicated
+// off) in the per-coordinate loop, where they would load GB300's slow FP64 pipe.
+__device__ __noinline__ double to_float_hw(u64 v, int e) { return ldexp(__ull2double_rn(v), e); }
+
+// ldexp((double)v, e) (dnb2_integer_to_float.c:29)
+__device__ __forceinline__ double to_float_bits(u64 v, int e)
+{
+    if (v == 0) return 0.0;
+    const int lz = __clzll((long long)v);
+    const int E = 1085 - lz + e;
+    if (E >= 1 && E <= 2045) return as_double(u64_scaled_bits(v, e));
+    return to_float_hw(v, e);  // subnormal or overflowing results
+}
+
+// Largest K <= min(mmax, MAX_K) whose table of 2^K x ncols words fits 32 KB.
+__host__ __device__ __forceinline__ u32 pick_K(u64 mmax, u32 ncols)
+{
+    u32 K = (u32)(mmax < MAX_K ? mmax : MAX_K);
+    while (K > 0 && ((u64)ncols << K) * 8 > 32768) K--;
+    return K;
+}
+
+__host__ __device__ __forceinline__ size_t table_words(u32 K, u64 mmax, u32 ncols)
+{
+    return ((size_t(1) << K) + (mmax > K ? mmax - K : 0)) * ncols;
+}
+
+// Build T and H for columns [j0, j0+ncols) of one matrix set Cl (d*mmax
+// words, column-major per dimension as in the reference), left shift ls and
+// digital shifts s_l (d words, or null).  Called by every thread of the CTA;
+// ends with a barrier.
+__device__ __forceinline__ void build_table(u64 *T, u64 *H, const u64 *Cl, u64 mmax, u64 j0, u32 ncols, u32 K,
+                                            u32 ls, const u64 *s_l)
+{
+    const u32 nhi = mmax > K ? (u32)(mmax - K) : 0u;
+    for (u32 e = threadIdx.x; e < nhi * ncols; e += blockDim.x) {
+        const u32 b = e / ncols, c = e % ncols;
+        H[e] = Cl[(j0 + c) * mmax + K + b] << ls;
+    }
+    // T[0] holds the digital shift (it reaches every entry through the
+    // doubling); T[lo + 2^b] = T[lo] ^ (C[b] << ls)
+    for (u32 c = threadIdx.x; c < ncols; c += blockDim.x) T[c] = s_l ? s_l[j0 + c] : 0ull;
+    __syncthreads();
+    for (u32 b = 0; b < K; b++) {
+        const u32 half = 1u << b;
+        for (u32 e = threadIdx.x; e < half * ncols; e += blockDim.x) {
+            const u32 lo = e / ncols, c = e % ncols;
+            T[(half + lo) * ncols + c] = T[lo * ncols + c] ^ (Cl[(j0 + c) * mmax + b] << ls);
+        }
+        __syncthreads();
+    }
+}
+
+// Write rows [row_begin, row_end) of the tile: the CTA walks its (row,
+// column) pairs as one flat run, so each step writes blockDim.x consecutive
+// coordinates.  xb_l / x_l point at column j0 of the randomisation's slab
+// (either may be null); d is the row pitch.
+template <bool GRAY>
+__device__ __forceinline__ void gen_rows(const u64 *T, const u64 *H, u32 K, u32 ncols, u64 n_start, u64 d,
+                                         u64 row_begin, u64 row_end, u64 *xb_l, double *x_l, int e_float)
+{
+    const u32 nlo = 1u << K;
+    const u64 total = (row_end - row_begin) * ncols;
+    const u32 step_rows = blockDim.x / ncols, step_cols = blockDim.x % ncols;
+    u64 row = row_begin + threadIdx.x / ncols;
+    u32 col = threadIdx.x % ncols;
+    u64 hi_key = ~0ull, hx = 0;
+    u32 col_key = ~0u;
+    for (u64 f = threadIdx.x; f < total; f += blockDim.x) {
+        const u64 m = seq_index(GRAY, n_start, row);
+        const u64 hi = m >> K;
+        if (hi != hi_key || col != col_key) {
+            hx = 0;
+            for (u64 hb = hi; hb; hb &= hb - 1) hx ^= H[(__ffsll((long long)hb) - 1) * ncols + col];
+            hi_key = hi;
+            col_key = col;
+        }
+        const u64 v = T[(u32)(m & (nlo - 1)) * ncols + col] ^ hx;
+        const u64 o = row * d + col;
+        if (xb_l) __stcs(xb_l + o, v);
+        if (x_l) __stcs(x_l + o, to_float_bits(v, e_float));
+        row += step_rows;
+        col += step_cols;
+        if (col >= ncols) {
+            col -= ncols;
+            row += 1;
+        }
+    }
+}
+
+}  // namespace
+}  // namespace net

@@ -80,4 +80,47 @@ int qmc_device_error_check(qmc_stream_t s)
     return QMC_OK;
 }
 
+// Device-side address of host memory a kernel may write directly: memory
+// pinned with cudaHostAlloc/cudaHostRegister is mapped into the device's
+// address space under unified addressing.  Pageable memory is reported as not
+// usable (returns QMC_ERR_ARG) even where the platform could reach it.
+int qmc_host_pointer_for_device(const void *host, void **dev)
+{
+    if (!host || !dev) {
+        qmcgb::set_error("null pointer");
+        return QMC_ERR_ARG;
+    }
+    cudaPointerAttributes attr;
+    cudaError_t e = cudaPointerGetAttributes(&attr, host);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        qmcgb::set_error("cudaPointerGetAttributes: %s", cudaGetErrorString(e));
+        return QMC_ERR_ARG;
+    }
+    if (attr.type != cudaMemoryTypeHost || attr.devicePointer == nullptr) {
+        qmcgb::set_error("host memory is not pinned and mapped");
+        return QMC_ERR_ARG;
+    }
+    *dev = attr.devicePointer;
+    return QMC_OK;
+}
+
+// Attributes of the current device that decide how host buffers are
+// reached: pageable-memory access, whether it goes through the host page
+// tables, and the SM count.
+int qmc_device_attributes(int *pageable_access, int *uses_host_page_tables, int *sms)
+{
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return qmcgb::cuda_status(e, "cudaGetDevice");
+    int a = 0, b = 0, c = 0;
+    cudaDeviceGetAttribute(&a, cudaDevAttrPageableMemoryAccess, dev);
+    cudaDeviceGetAttribute(&b, cudaDevAttrPageableMemoryAccessUsesHostPageTables, dev);
+    cudaDeviceGetAttribute(&c, cudaDevAttrMultiProcessorCount, dev);
+    if (pageable_access) *pageable_access = a;
+    if (uses_host_page_tables) *uses_host_page_tables = b;
+    if (sms) *sms = c;
+    return qmcgb::cuda_status(cudaGetLastError(), "cudaDeviceGetAttribute");
+}
+
 }  // extern "C"
