@@ -574,6 +574,7 @@ def run_net_lms(args):
 
     # uneven batch of 256 single-randomisation requests
     urng = np.random.Generator(np.random.SFC64(33))
+    C128 = triangular_net_matrices(urng, 128, m, 64)  # base matrices for d_pre = 2d up to 128
     reqs, plain_args = [], []
     total_pts = total_coords = 0
     for k in range(256):
@@ -582,7 +583,7 @@ def run_net_lms(args):
         nk = 1 << L
         Sk = q.dnb2_get_linear_scramble_matrix(urng, 1, 2 * dk, 64, 64, False)
         shk = q.dnb2_get_digital_shifts(urng, 1, dk, 64)
-        Ck = dev_tensor(np.ascontiguousarray(C[:, :2 * dk, :]))
+        Ck = dev_tensor(np.ascontiguousarray(C128[:, :2 * dk, :]))
         out = torch.empty(nk * dk, dtype=torch.int64, device="cuda")
         req = dict(r=1, n=nk, d=dk, alpha=2, d_pre=2 * dk, mmax=m, tmax=64, tmax_new=64, tmax_alpha=64, r_C=1,
                    order="natural", C=Ck, S=dev_tensor(Sk), lshifts=dev_tensor(np.zeros(1, U)), shifts=dev_tensor(shk),

@@ -186,6 +186,24 @@ def _dptr(t):
     return None if t is None else t.data_ptr()
 
 
+def _need(q, key, count, dtypes, optional=True):
+    """Check that request field `key` is a contiguous CUDA tensor of one of
+    `dtypes` with at least `count` elements (kernels get raw pointers and
+    would otherwise read or write past it)."""
+    t = q.get(key)
+    if t is None:
+        if optional:
+            return
+        raise ValueError("request field %s is required" % key)
+    torch = _t()
+    if not isinstance(t, torch.Tensor) or not t.is_cuda or not t.is_contiguous():
+        raise TypeError("request field %s must be a contiguous CUDA tensor" % key)
+    if t.dtype not in dtypes:
+        raise TypeError("request field %s has dtype %s" % (key, t.dtype))
+    if t.numel() < count:
+        raise ValueError("request field %s has %d elements, needs %d" % (key, t.numel(), count))
+
+
 class Plan:
     """A batched plan over device tensors (see NetPlan / LatPlan).
 
@@ -259,11 +277,22 @@ class NetPlan(Plan):
     struct_type = NetRequest
 
     def __init__(self, requests):
+        torch = _t()
+        ints, flts = (torch.int64, torch.uint64), (torch.float64,)
         structs, keep, self._rows = [], [], []
         for q in requests:
             q = dict(q)
             alpha = int(q.get("alpha", 1))
             d = int(q["d"])
+            r, n, mmax = int(q["r"]), int(q["n"]), int(q["mmax"])
+            d_pre = int(q.get("d_pre", d * alpha))
+            _need(q, "C", int(q.get("r_C", 1)) * d_pre * mmax, ints, optional=False)
+            _need(q, "S", r * d_pre * int(q.get("tmax_new", q.get("tmax", 64))), ints)
+            _need(q, "shifts", r * d, ints)
+            _need(q, "lshifts", r if q.get("shifts") is not None else 0, ints)
+            _need(q, "tmaxes", r if q.get("x") is not None else 0, ints)
+            _need(q, "xb", r * n * d, ints)
+            _need(q, "x", r * n * d, flts)
             st = NetRequest(r=int(q["r"]), n=int(q["n"]), d=d, n_start=int(q.get("n_start", 0)),
                             mmax=int(q["mmax"]), d_pre=int(q.get("d_pre", d * alpha)), alpha=alpha,
                             tmax=int(q.get("tmax", 64)), tmax_new=int(q.get("tmax_new", q.get("tmax", 64))),
@@ -287,9 +316,14 @@ class LatPlan(Plan):
     struct_type = LatRequest
 
     def __init__(self, requests):
+        torch = _t()
         structs, keep, self._rows = [], [], []
         for q in requests:
             q = dict(q)
+            r, n, d = int(q["r"]), int(q["n"]), int(q["d"])
+            _need(q, "g", r * d, (torch.int64, torch.uint64), optional=False)
+            _need(q, "shifts", r * d, (torch.float64,))
+            _need(q, "x", r * n * d, (torch.float64,), optional=False)
             st = LatRequest(r=int(q["r"]), n=int(q["n"]), d=int(q["d"]), n_start=int(q.get("n_start", 0)),
                             gray=1 if q.get("order", "gray") == "gray" else 0, g=_dptr(q["g"]),
                             shifts=_dptr(q.get("shifts")), x=_dptr(q["x"]))
