@@ -244,6 +244,22 @@ int qmc_plan_set_tuning(qmc_plan *plan, int ctas_per_sm, int chunk, uint64_t til
 int qmc_plan_info(const qmc_plan *plan, uint64_t *tiles, uint64_t *coords, uint64_t *bytes_out, int *launches);
 int qmc_plan_destroy(qmc_plan *plan);
 
+/* ---- one digital-net request without any allocation -------------------------
+ * No counterpart in the reference.  For callers that cannot call cudaMalloc
+ * -- their device memory belongs to another allocator (a framework's caching
+ * pool, a serving process's fixed arena), or they run a latency-bound loop
+ * that must not take cudaMalloc's implicit device synchronisation.  Runs the
+ * chain of one qmc_net_request (as a one-request plan does) on stream s,
+ * allocating nothing: the scrambled/interlaced matrices go to a fixed array
+ * of QMC_NOALLOC_MATRIX_WORDS words (1 MiB) inside the library, present on
+ * every device that loads it until the process exits.  Requests needing
+ * more (r*d*mmax words when S is set or alpha > 1) are rejected with
+ * QMC_ERR_ARG.  The first call on a device looks the array up and should come
+ * before any stream capture.  Calls share the array: calls whose kernels
+ * overlap on the GPU race, so order them on one stream. */
+#define QMC_NOALLOC_MATRIX_WORDS 131072
+int qmc_net_gen_noalloc(const qmc_net_request *req, qmc_stream_t s);
+
 #ifdef __cplusplus
 }
 #endif

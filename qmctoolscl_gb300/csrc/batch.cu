@@ -18,6 +18,7 @@
 //
 // Reference chains reproduced, bit for bit: see qmc_net_request /
 // qmc_lat_request in include/qmcgb.h.
+#include <mutex>
 #include <vector>
 
 #include "lattice_dev.cuh"
@@ -86,11 +87,11 @@ __device__ __forceinline__ u64 lms_word(const u64 *srow, u64 col, u64 tmax_new)
 
 constexpr int MAX_ALPHA = 16;
 
-__global__ void net_prep_kernel(const PrepDesc *ps, int np, u64 total)
+// Word loc of one request's prepared matrices: LMS of the alpha source
+// columns (dnb2_linear_matrix_scramble.c:32-48), then interlacing.
+__device__ __forceinline__ void prep_word(const PrepDesc &P, u64 loc)
 {
-    for (u64 w = (u64)blockIdx.x * blockDim.x + threadIdx.x; w < total; w += (u64)gridDim.x * blockDim.x) {
-        const PrepDesc &P = ps[find_desc(ps, np, w, [](const PrepDesc &p) { return p.word_begin; })];
-        const u64 loc = w - P.word_begin;
+    {
         const u64 k = loc % P.mmax, ja = (loc / P.mmax) % P.d, l = loc / (P.mmax * P.d);
         const u64 *Cl = P.C + (l % P.r_C) * P.d_pre * P.mmax;
         u64 words[MAX_ALPHA];
@@ -110,6 +111,14 @@ __global__ void net_prep_kernel(const PrepDesc *ps, int np, u64 total)
             }
         }
         P.out[loc] = out;
+    }
+}
+
+__global__ void net_prep_kernel(const PrepDesc *ps, int np, u64 total)
+{
+    for (u64 w = (u64)blockIdx.x * blockDim.x + threadIdx.x; w < total; w += (u64)gridDim.x * blockDim.x) {
+        const PrepDesc &P = ps[find_desc(ps, np, w, [](const PrepDesc &p) { return p.word_begin; })];
+        prep_word(P, w - P.word_begin);
     }
 }
 
@@ -563,3 +572,112 @@ int qmc_plan_destroy(qmc_plan *p)
 }
 
 }  // extern "C"
+
+// ------------------------------------------------- entry point without allocation
+//
+// qmc_net_gen_noalloc runs one digital-net request -- the same chain as a
+// one-request plan -- without allocating any device memory.  It exists for
+// callers that cannot call cudaMalloc: a process whose device memory is
+// already handed to another allocator (a framework's caching pool, a fixed
+// arena in a serving process), where a raw cudaMalloc fails or escapes the
+// pool's accounting, and latency-bound loops that must not pay cudaMalloc's
+// implicit device synchronisation.  Inputs and outputs stay the caller's.
+//
+// The only scratch it needs, the scrambled and interlaced generating
+// matrices, lives in the file-scope array below: QMC_NOALLOC_MATRIX_WORDS
+// 64-bit words (1 MiB) on every device that loads this library, held until
+// the process exits.  Host code reaches it through the address that
+// cudaGetSymbolAddress returns for the current device (the array's name in
+// host code is only a stand-in, not a device address); the lookup is done by
+// the first call on each device, so that first call should come before any
+// stream capture.  Every call shares the array and it keeps the last call's
+// contents; the preparation kernel overwrites every word a call reads, so
+// nothing has to start at zero.  Calls whose kernels overlap on the GPU (on
+// different streams, or from different host threads without ordering) race
+// on the array: order them on one stream.
+
+static __device__ __align__(256) unsigned long long g_noalloc_matrices[QMC_NOALLOC_MATRIX_WORDS];
+
+namespace {
+
+constexpr int NOALLOC_MAX_DEVICES = 64;
+std::mutex g_noalloc_mu;
+u64 *g_noalloc_ptr[NOALLOC_MAX_DEVICES];
+
+// device address of g_noalloc_matrices on the current device, looked up once
+int noalloc_scratch(u64 **out)
+{
+    int dev = 0;
+    if (int rc = qmcgb::cuda_status(cudaGetDevice(&dev), "cudaGetDevice")) return rc;
+    if (dev < 0 || dev >= NOALLOC_MAX_DEVICES) {
+        qmcgb::set_error("device %d is beyond the %d devices this entry point serves", dev, NOALLOC_MAX_DEVICES);
+        return QMC_ERR_ARG;
+    }
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    if (!g_noalloc_ptr[dev]) {
+        void *p = nullptr;
+        const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_matrices);
+        if (e != cudaSuccess) return qmcgb::cuda_status(e, "cudaGetSymbolAddress of the matrix scratch");
+        g_noalloc_ptr[dev] = (u64 *)p;
+    }
+    *out = g_noalloc_ptr[dev];
+    return QMC_OK;
+}
+
+__global__ void net_prep_one_kernel(PrepDesc P, u64 total)
+{
+    for (u64 w = (u64)blockIdx.x * blockDim.x + threadIdx.x; w < total; w += (u64)gridDim.x * blockDim.x)
+        prep_word(P, w);
+}
+
+}  // namespace
+
+extern "C" int qmc_net_gen_noalloc(const qmc_net_request *req, qmc_stream_t s)
+{
+    QMC_REQUIRE(req, "null request");
+    const qmc_net_request &Q = *req;
+    if (Q.r == 0 || Q.n == 0 || Q.d == 0) return QMC_OK;
+    const u64 alpha = Q.alpha ? Q.alpha : 1;
+    QMC_REQUIRE(Q.C && (Q.xb || Q.x), "null matrices or no output");
+    QMC_REQUIRE(!Q.shifts || Q.lshifts, "shifts without lshifts");
+    QMC_REQUIRE(!Q.x || Q.tmaxes, "float output without tmaxes");
+    QMC_REQUIRE(alpha <= (u64)MAX_ALPHA && Q.d_pre == Q.d * alpha && Q.mmax <= 64 && Q.r_C > 0,
+                "bad alpha, d_pre, mmax or r_C");
+    if ((!Q.gray && !gray_closed(Q.n_start, Q.n_start + Q.n)) || bitlen(Q.n_start + Q.n - 1) > Q.mmax ||
+        Q.n_start + Q.n < Q.n_start) {
+        qmcgb::set_error("index range not covered by the generating matrices (or not Gray-closed in natural order)");
+        return QMC_ERR_DOMAIN;
+    }
+    const bool prep = Q.S || alpha > 1;
+    const u64 words = Q.r * Q.d * Q.mmax;
+    QMC_REQUIRE(!prep || words <= (u64)QMC_NOALLOC_MATRIX_WORDS,
+                "qmc_net_gen_noalloc: the request needs r*d*mmax = %llu words of matrix scratch, above the %d "
+                "this entry point holds; use a plan (qmc_net_plan_create) for it",
+                (unsigned long long)words, QMC_NOALLOC_MATRIX_WORDS);
+    cudaStream_t st = QMC_STREAM(s);
+    const u64 *C = (const u64 *)Q.C;
+    u64 r_C = Q.r_C;
+    if (prep) {
+        u64 *scratch = nullptr;
+        if (int rc = noalloc_scratch(&scratch)) return rc;
+        PrepDesc P{};
+        P.r = Q.r;
+        P.d = Q.d;
+        P.d_pre = Q.d_pre;
+        P.mmax = Q.mmax;
+        P.alpha = alpha;
+        P.nbits = Q.S ? Q.tmax_new : Q.tmax;
+        P.tmax_alpha = Q.tmax_alpha;
+        P.r_C = Q.r_C;
+        P.C = (const u64 *)Q.C;
+        P.S = (const u64 *)Q.S;
+        P.out = scratch;
+        net_prep_one_kernel<<<qmcgb::grid_for(words, 256, (unsigned)qmcgb::sm_count() * 8), 256, 0, st>>>(P, words);
+        if (int rc = qmcgb::launch_status("net_prep_one_kernel")) return rc;
+        C = scratch;
+        r_C = Q.r;
+    }
+    return qmcgb::dnb2_gen_fused(Q.r, Q.n, Q.d, Q.n_start, Q.mmax, C, r_C, Q.gray ? 1 : 0,
+                                 Q.shifts ? (const u64 *)Q.lshifts : nullptr, Q.r, (const u64 *)Q.shifts,
+                                 Q.x ? (const u64 *)Q.tmaxes : nullptr, (u64 *)Q.xb, Q.x, st);
+}

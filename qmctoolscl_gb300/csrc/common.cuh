@@ -205,6 +205,12 @@ inline unsigned grid_for(u64 work, unsigned per_block, unsigned cap)
 
 int sm_count();
 
+// base-2 net generation with optional fused digital shift / float output
+// (dnb2.cu); stream-ordered, allocates nothing
+int dnb2_gen_fused(u64 r, u64 n, u64 d, u64 n_start, u64 mmax, const u64 *C, u64 r_C, int gray,
+                   const u64 *lshifts, u64 r_x, const u64 *shifts, const u64 *tmaxes, u64 *xrb, double *x,
+                   cudaStream_t s);
+
 }  // namespace qmcgb
 
 #define QMC_REQUIRE(cond, ...)                \
