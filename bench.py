@@ -527,6 +527,9 @@ def run_net_lms(args):
     rng = np.random.Generator(np.random.SFC64(3))
     r, d_pre, alpha, m, C, S, shifts = cfg3_uniform_inputs(rng)
     d, n = d_pre // alpha, 1 << m
+    if args.small:  # profiling mode: 8 randomisations (2 GiB of output), no uneven batch
+        r = 8
+        S, shifts = np.ascontiguousarray(S[:r]), np.ascontiguousarray(shifts[:r])
     st = torch.cuda.Stream()
     h = st.cuda_stream
     Cd, Sd, sd = dev_tensor(C), dev_tensor(S), dev_tensor(shifts)
@@ -571,6 +574,9 @@ def run_net_lms(args):
     assert same and np.array_equal(xrb[:nn * d].cpu().numpy().view(U), orb.reshape(-1))
     del xrb, plan
     torch.cuda.empty_cache()
+    if args.small:
+        return {"small": True, "r": r, "graph_ms": ms_graph, "plain_ms": ms_plain,
+                "gbs": 8.0 * r * n * d / (ms_graph / 1e3) / 1e9}
 
     # uneven batch of 256 single-randomisation requests
     urng = np.random.Generator(np.random.SFC64(33))

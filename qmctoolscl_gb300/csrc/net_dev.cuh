@@ -84,41 +84,64 @@ __device__ __forceinline__ void build_table(u64 *T, u64 *H, const u64 *Cl, u64 m
     }
 }
 
-// Write rows [row_begin, row_end) of the tile: the CTA walks its (row,
-// column) pairs as one flat run, so each step writes blockDim.x consecutive
-// coordinates.  xb_l / x_l point at column j0 of the randomisation's slab
-// (either may be null); d is the row pitch.
+// Write rows [row_begin, row_end) of the tile.  Each thread owns VEC
+// adjacent columns (16-byte loads and stores for VEC = 2) and walks rows
+// ry, ry + R, ...: R rows per step, so a step of the CTA writes R consecutive
+// row segments, and a thread's high-bit term stays cached while m >> K holds.
+// Threads beyond R*groups idle (ncols need not divide the CTA).  xb_l / x_l
+// point at column j0 of the randomisation's slab (either may be null); d is
+// the row pitch.
+template <bool GRAY, int VEC>
+__device__ __forceinline__ void gen_rows_vec(const u64 *T, const u64 *H, u32 K, u32 ncols, u64 n_start, u64 d,
+                                             u64 row_begin, u64 row_end, u64 *xb_l, double *x_l, int e_float)
+{
+    const u32 groups = ncols / VEC;
+    const u32 R = blockDim.x / groups;
+    if (threadIdx.x >= R * groups) return;
+    const u32 c0 = (threadIdx.x % groups) * VEC;
+    const u32 nlo = 1u << K;
+    u64 hi_key = ~0ull, hx[VEC];
+#pragma unroll
+    for (int v = 0; v < VEC; v++) hx[v] = 0;
+    for (u64 row = row_begin + threadIdx.x / groups; row < row_end; row += R) {
+        const u64 m = seq_index(GRAY, n_start, row);
+        const u64 hi = m >> K;
+        if (hi != hi_key) {  // XOR of the high-bit columns picked by hi: changes every 2^K rows
+#pragma unroll
+            for (int v = 0; v < VEC; v++) hx[v] = 0;
+            for (u64 hb = hi; hb; hb &= hb - 1) {
+                const u32 b = __ffsll((long long)hb) - 1;
+#pragma unroll
+                for (int v = 0; v < VEC; v++) hx[v] ^= H[b * ncols + c0 + v];
+            }
+            hi_key = hi;
+        }
+        const u32 ti = (u32)(m & (nlo - 1)) * ncols + c0;
+        const u64 o = row * d + c0;
+        if (VEC == 2) {
+            const ulonglong2 t = *(const ulonglong2 *)(T + ti);
+            const u64 v0 = t.x ^ hx[0], v1 = t.y ^ hx[VEC - 1];
+            if (xb_l) __stcs((ulonglong2 *)(xb_l + o), make_ulonglong2(v0, v1));
+            if (x_l) __stcs((double2 *)(x_l + o), make_double2(to_float_bits(v0, e_float), to_float_bits(v1, e_float)));
+        } else {
+            const u64 v0 = T[ti] ^ hx[0];
+            if (xb_l) __stcs(xb_l + o, v0);
+            if (x_l) __stcs(x_l + o, to_float_bits(v0, e_float));
+        }
+    }
+}
+
+// VEC = 2 needs an even column count and 16-byte aligned rows (d even and
+// 16-byte aligned bases).
 template <bool GRAY>
 __device__ __forceinline__ void gen_rows(const u64 *T, const u64 *H, u32 K, u32 ncols, u64 n_start, u64 d,
                                          u64 row_begin, u64 row_end, u64 *xb_l, double *x_l, int e_float)
 {
-    const u32 nlo = 1u << K;
-    const u64 total = (row_end - row_begin) * ncols;
-    const u32 step_rows = blockDim.x / ncols, step_cols = blockDim.x % ncols;
-    u64 row = row_begin + threadIdx.x / ncols;
-    u32 col = threadIdx.x % ncols;
-    u64 hi_key = ~0ull, hx = 0;
-    u32 col_key = ~0u;
-    for (u64 f = threadIdx.x; f < total; f += blockDim.x) {
-        const u64 m = seq_index(GRAY, n_start, row);
-        const u64 hi = m >> K;
-        if (hi != hi_key || col != col_key) {
-            hx = 0;
-            for (u64 hb = hi; hb; hb &= hb - 1) hx ^= H[(__ffsll((long long)hb) - 1) * ncols + col];
-            hi_key = hi;
-            col_key = col;
-        }
-        const u64 v = T[(u32)(m & (nlo - 1)) * ncols + col] ^ hx;
-        const u64 o = row * d + col;
-        if (xb_l) __stcs(xb_l + o, v);
-        if (x_l) __stcs(x_l + o, to_float_bits(v, e_float));
-        row += step_rows;
-        col += step_cols;
-        if (col >= ncols) {
-            col -= ncols;
-            row += 1;
-        }
-    }
+    const bool vec2 = (ncols % 2 == 0) && (d % 2 == 0) && !(((uintptr_t)xb_l | (uintptr_t)x_l) & 15);
+    if (vec2)
+        gen_rows_vec<GRAY, 2>(T, H, K, ncols, n_start, d, row_begin, row_end, xb_l, x_l, e_float);
+    else
+        gen_rows_vec<GRAY, 1>(T, H, K, ncols, n_start, d, row_begin, row_end, xb_l, x_l, e_float);
 }
 
 }  // namespace
