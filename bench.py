@@ -640,7 +640,105 @@ def run_net_lms(args):
             "gpu_launches": 2 * args.steps}
 
 
-WORKLOADS = {"net_plain": run_net_plain, "net_lms": run_net_lms}
+def run_fft(args):
+    """Bit-reversed-order FFT (and FWHT on the real parts) of 4096 vectors of
+    uneven lengths 2^10..2^20 (log2 length uniform, seeded), entries iid
+    N(0,1): the FP64 radix-2 kernels (one call per length) against the
+    tensor-core kernels (BF16 splits, FP32 accumulation), with the relative L2
+    error of the tensor-core result against the FP64 one per length."""
+    import torch
+    from qmctoolscl_gb300 import _ffi
+    lib = _ffi.lib()
+    rng = np.random.Generator(np.random.SFC64(5))
+    L = rng.integers(10, 21, 4096 if not args.small else 256)
+    counts = {int(l): int((L == l).sum()) for l in sorted(set(L.tolist()))}
+    groups = []
+    for l, cnt in counts.items():
+        n = 1 << l
+        xr = rng.standard_normal((cnt, n))
+        xi = rng.standard_normal((cnt, n))
+        groups.append(dict(L=l, n=n, cnt=cnt, xr0=torch.from_numpy(xr).cuda(), xi0=torch.from_numpy(xi).cuda()))
+    samples = sum(g["n"] * g["cnt"] for g in groups)
+    st = torch.cuda.current_stream()
+    h = st.cuda_stream
+    for g in groups:
+        g["xr"], g["xi"] = g["xr0"].clone(), g["xi0"].clone()
+        g["twr"] = torch.empty(g["n"], dtype=torch.float64, device="cuda")
+        g["twi"] = torch.empty_like(g["twr"])
+
+    def fp64():
+        for g in groups:
+            _ffi.check(lib.qmc_fft_bro_1d_radix2(g["cnt"], 1, g["n"] // 2, g["twr"].data_ptr(), g["twi"].data_ptr(),
+                                                 g["xr"].data_ptr(), g["xi"].data_ptr(), h), "fft")
+
+    def tc():
+        for g in groups:
+            _ffi.check(lib.qmc_tc_fft_bro_1d(g["cnt"], 1, g["n"] // 2, g["xr"].data_ptr(), g["xi"].data_ptr(), h),
+                       "tc_fft")
+
+    def wht64():
+        for g in groups:
+            _ffi.check(lib.qmc_fwht_1d_radix2(g["cnt"], 1, g["n"] // 2, g["xr"].data_ptr(), h), "fwht")
+
+    def wht_tc():
+        for g in groups:
+            _ffi.check(lib.qmc_tc_fwht_1d(g["cnt"], 1, g["n"] // 2, g["xr"].data_ptr(), h), "tc_fwht")
+
+    steps, warm = max(3, min(args.steps, 10)), 3
+    ms = {}
+    for name, fn in (("fft_fp64", fp64), ("fft_tc", tc), ("fwht_fp64", wht64), ("fwht_tc", wht_tc)):
+        ms[name] = gpu_ms(fn, steps, warm, st)  # in place: repeated transforms of whatever is there
+    # accuracy: one transform of the original data by each path
+    err = {}
+    for g in groups:
+        xr64, xi64 = g["xr0"].clone(), g["xi0"].clone()
+        _ffi.check(lib.qmc_fft_bro_1d_radix2(g["cnt"], 1, g["n"] // 2, g["twr"].data_ptr(), g["twi"].data_ptr(),
+                                             xr64.data_ptr(), xi64.data_ptr(), h), "fft")
+        xrt, xit = g["xr0"].clone(), g["xi0"].clone()
+        _ffi.check(lib.qmc_tc_fft_bro_1d(g["cnt"], 1, g["n"] // 2, xrt.data_ptr(), xit.data_ptr(), h), "tc_fft")
+        wr64, wrt = g["xr0"].clone(), g["xr0"].clone()
+        _ffi.check(lib.qmc_fwht_1d_radix2(g["cnt"], 1, g["n"] // 2, wr64.data_ptr(), h), "fwht")
+        _ffi.check(lib.qmc_tc_fwht_1d(g["cnt"], 1, g["n"] // 2, wrt.data_ptr(), h), "tc_fwht")
+        torch.cuda.synchronize()
+        num = torch.sqrt(((xrt - xr64) ** 2 + (xit - xi64) ** 2).sum(dim=1))
+        den = torch.sqrt((xr64 ** 2 + xi64 ** 2).sum(dim=1))
+        wnum = torch.linalg.norm(wrt - wr64, dim=1)
+        wden = torch.linalg.norm(wr64, dim=1)
+        err[g["L"]] = {"fft_max": float((num / den).max()), "fwht_max": float((wnum / wden).max()), "vectors": g["cnt"]}
+    # FP64 result against numpy on one vector of the largest length
+    g = groups[-1]
+    m = g["L"]
+    br = np.zeros(g["n"], dtype=np.int64)
+    idx = np.arange(g["n"])
+    for b in range(m):
+        br |= ((idx >> b) & 1) << (m - 1 - b)
+    z = g["xr0"][0].cpu().numpy() + 1j * g["xi0"][0].cpu().numpy()
+    want = np.fft.fft(z[br], norm="ortho")
+    xr64, xi64 = g["xr0"][:1].clone(), g["xi0"][:1].clone()
+    _ffi.check(lib.qmc_fft_bro_1d_radix2(1, 1, g["n"] // 2, g["twr"].data_ptr(), g["twi"].data_ptr(),
+                                         xr64.data_ptr(), xi64.data_ptr(), h), "fft")
+    got = xr64[0].cpu().numpy() + 1j * xi64[0].cpu().numpy()
+    fp64_vs_numpy = float(np.linalg.norm(got - want) / np.linalg.norm(want))
+    worst = max(e["fft_max"] for e in err.values())
+    passes = lambda l: 1 if l <= 12 else 2  # noqa: E731
+    alg_tc = sum(32.0 * g["n"] * g["cnt"] * passes(g["L"]) for g in groups)
+    return {"metric": METRIC, "value": samples / (ms["fft_tc"] / 1e3) / 1e9, "unit": "Gsamples/s", "n_gpus": 1,
+            "steps": steps, "warmup": warm, "ms_per_step": ms["fft_tc"], "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "bf16x3 products, fp32 accumulate, fp64 I/O",
+            "data": "synthetic (np.random.SFC64(5)), N(0,1) complex",
+            "config": {"workload": "bit-reversed FFT of %d vectors, log2 n uniform in [10,20]" % len(L),
+                       "samples": samples, "lengths": counts},
+            "roofline": dict(roofline(alg_tc, ms["fft_tc"]), note="32 B per complex sample per pass (FP64 read+write)"),
+            "fp64": {"fft_ms": ms["fft_fp64"], "fwht_ms": ms["fwht_fp64"],
+                     "fft_gsamples_per_s": samples / (ms["fft_fp64"] / 1e3) / 1e9,
+                     "fp64_vs_numpy_rel_l2": fp64_vs_numpy},
+            "tc": {"fft_ms": ms["fft_tc"], "fwht_ms": ms["fwht_tc"], "fft_speedup_vs_fp64": ms["fft_fp64"] / ms["fft_tc"],
+                   "fwht_speedup_vs_fp64": ms["fwht_fp64"] / ms["fwht_tc"], "max_rel_l2_error": worst,
+                   "error_by_log2n": err},
+            "gpu_launches": None}
+
+
+WORKLOADS = {"net_plain": run_net_plain, "net_lms": run_net_lms, "fft": run_fft}
 
 
 def main():

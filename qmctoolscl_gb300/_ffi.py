@@ -25,6 +25,10 @@ INT = ctypes.c_int
 EXTRA = {
     "qmc_lat_gen_shift": [U64, U64, U64, U64, INT, PTR, PTR, PTR, PTR],
     "qmc_dnb2_gen_fused": [U64, U64, U64, U64, U64, PTR, U64, INT, PTR, U64, PTR, PTR, PTR, PTR, PTR],
+    "qmc_tc_mma_probe": [PTR, PTR, PTR, ctypes.c_uint32, ctypes.c_uint32, PTR],
+    "qmc_tc_fft_bro_1d": [U64, U64, U64, PTR, PTR, PTR],
+    "qmc_tc_ifft_bro_1d": [U64, U64, U64, PTR, PTR, PTR],
+    "qmc_tc_fwht_1d": [U64, U64, U64, PTR, PTR],
 }
 
 

@@ -1,0 +1,480 @@
+// tc_fft.cu -- tensor-core (tcgen05, BF16 in / FP32 accumulate) paths of
+// the fast transforms.
+//
+// qmc_tc_mma_probe: one CTA computes D = A * B^T (A 128 x K, B N x K, BF16,
+// D FP32) through tcgen05.mma with the operand layout and descriptors of
+// tc_sm100.cuh; the tests compare it with an exact host product to pin the
+// descriptor encodings every tensor-core kernel here relies on.
+#include "tc_sm100.cuh"
+
+namespace {
+
+constexpr u32 WAIT_LIMIT = 1u << 22;  // mbarrier polls before giving up (~ a fraction of a second)
+
+__global__ void __launch_bounds__(128) tc_probe_kernel(const __nv_bfloat16 *A, const __nv_bfloat16 *B, float *D,
+                                                       u32 N, u32 K, u32 tcols, unsigned *err)
+{
+    extern __shared__ __align__(128) unsigned char sm[];
+    __shared__ __align__(8) u64 bar;
+    __shared__ u32 tmem_base;
+    unsigned char *sA = sm, *sB = sm + 128 * K * 2;
+    const u32 warp = threadIdx.x / 32, lane = threadIdx.x % 32;
+    if (warp == 0) tc::tmem_alloc(&tmem_base, tcols);
+    for (u32 e = threadIdx.x; e < 128 * K; e += blockDim.x)
+        *(__nv_bfloat16 *)(sA + tc::kmajor_offset(e / K, e % K, K)) = A[e];
+    for (u32 e = threadIdx.x; e < N * K; e += blockDim.x)
+        *(__nv_bfloat16 *)(sB + tc::kmajor_offset(e / K, e % K, K)) = B[e];
+    tc::fence_smem_to_async();
+    if (threadIdx.x == 0) tc::mbar_init(&bar, 1);
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    const u32 tmem = tmem_base;
+    if (threadIdx.x == 0) {
+        const u32 idesc = tc::idesc_bf16_f32(128, N);
+        const u32 sbo = (K / 8) * 128;
+        for (u32 s = 0; s < K / 16; s++)
+            tc::mma_bf16(tmem, tc::smem_desc(sA + s * 256, 128, sbo), tc::smem_desc(sB + s * 256, 128, sbo), idesc,
+                         s > 0);
+        tc::mma_commit(&bar);
+    }
+    const bool ok = __all_sync(0xFFFFFFFFu, tc::mbar_wait(&bar, 0, WAIT_LIMIT));
+    if (!ok && lane == 0) atomicOr(err, 4u);
+    tc::fence_after_sync();
+    if (ok) {
+        const u32 row = warp * 32 + lane;
+        for (u32 c0 = 0; c0 < N; c0 += 16) {
+            u32 r[16];
+            tc::tmem_ld16(tmem + ((warp * 32) << 16) + c0, r);
+            tc::tmem_wait_ld();
+#pragma unroll
+            for (int j = 0; j < 16; j++) D[row * N + c0 + j] = __uint_as_float(r[j]);
+        }
+    } else {
+        // give the MMAs one more bounded chance to finish before freeing their tensor memory
+        tc::mbar_wait(&bar, 0, WAIT_LIMIT);
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+    if (warp == 0) tc::tmem_dealloc(tmem, tcols);
+}
+
+}  // namespace
+
+extern "C" int qmc_tc_mma_probe(const void *A, const void *B, float *D, uint32_t N, uint32_t K, qmc_stream_t s)
+{
+    QMC_REQUIRE(A && B && D, "null pointer");
+    QMC_REQUIRE(N >= 16 && N <= 256 && N % 16 == 0 && K >= 16 && K <= 256 && K % 16 == 0,
+                "probe shape: N in [16,256] and K in [16,256], multiples of 16");
+    unsigned *err = qmcgb::device_error_ptr();
+    QMC_REQUIRE(err, "device error word unavailable");
+    u32 tcols = 32;
+    while (tcols < N) tcols <<= 1;
+    const size_t smem = (size_t)(128 + N) * K * 2;
+    if (smem > 48 * 1024) {
+        cudaError_t e = cudaFuncSetAttribute(tc_probe_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return qmcgb::cuda_status(e, "tc probe smem");
+    }
+    tc_probe_kernel<<<1, 128, smem, QMC_STREAM(s)>>>((const __nv_bfloat16 *)A, (const __nv_bfloat16 *)B, D, N, K,
+                                                     tcols, err);
+    return qmcgb::launch_status("tc_probe_kernel");
+}
+
+// ===========================================================================
+// Tensor-core FFT / inverse FFT / Walsh-Hadamard transform.
+//
+// Same contract as the FP64 transforms (transforms.cu): orthonormal, in place
+// along the last axis of d1*d2 vectors of length n = 2^L, FFT input in
+// bit-reversed order and output natural, the inverse the other way round,
+// FP64 arrays in HBM.  Arithmetic is FP32 with BF16 tensor-core products;
+// the error against the FP64 transform is about 1e-7 relative (tests bound
+// it by 1e-6).
+//
+// Passes.  As in transforms.cu, each pass covers a range of index bits
+// [k0, k1) on tiles of 4096 values: pass 1 bits [0, min(L,12)) on contiguous
+// blocks (several short vectors per tile), pass 2 bits [12, L) on tiles of
+// Q = 2^(L-12) rows by 4096/Q consecutive columns.  The FFT runs pass 1
+// first, the inverse pass 2 first.
+//
+// Radix-16 step.  The reference's radix-2 stages k..k+3 on bit-reversed
+// input, fused, act on groups of 16 values at positions base + p*2^k
+// (p < 16, base with bits k..k+3 clear): with c = base mod 2^k and
+// w = exp(-2*pi*i*c/2^(k+4)),
+//     Y[m] = sum_p (X[p] * w^br(p)) * exp(-2*pi*i*br(p)*m/16),   br = 4-bit reversal,
+// written back to base + m*2^k.  The inverse step applies the conjugate
+// 16-point matrix first and the conjugate twiddle w^-br(q) after; the WHT
+// step is the 16-point Hadamard matrix with no twiddle.
+//
+// GEMM.  The 256 groups of a tile form two M = 128 tiles.  A group's 16
+// complex inputs are 32 reals; each is split into three BF16 terms
+// x = x1 + x2 + x3 (24 significant bits), and so is each entry of the real
+// 32 x 32 form of the 16-point matrix.  The six products with i + j <= 4
+// (x1m1, x1m2, x2m1, x1m3, x2m2, x3m1) are laid side by side along K, so one
+// M=128, N=32, K=192 product (12 tcgen05.mma, FP32 accumulation in tensor
+// memory) gives the step for 128 groups.  The tensor core's accumulation does
+// not round to nearest, and chaining all twelve MMAs into one accumulator
+// measured about 1e-6 error per step; so the two MMAs of the dominant x1*m1
+// product each get their own accumulator and the ten small products a third,
+// and the three are added in FP32 (round to nearest) when read back.  Bits
+// left over when a pass does not cover a multiple of 4 use FP32 radix-2
+// butterflies.
+// ===========================================================================
+
+namespace {
+
+constexpr u32 FT_TILE = 4096;          // complex values per tile
+constexpr u32 FT_GROUPS = FT_TILE / 16;
+constexpr u32 FT_KS = 192;             // K of the split product: 6 x 32 reals
+constexpr u32 FT_THREADS = 256;
+constexpr u32 TMEM_COLS = 128;         // three 32-column FP32 accumulators
+enum TcKind { TC_FFT = 0, TC_IFFT = 1, TC_WHT = 2 };
+
+struct TcPassArgs {
+    u64 total;       // nvec * n values
+    u32 L;           // log2 n
+    u32 k0, k1;      // index bits of this pass
+    u32 ct;          // consecutive columns per tile row (1 for pass 1)
+    u32 Q;           // tile rows
+    double *xr, *xi;
+    float scale;     // applied on write-back when != 1
+};
+
+__device__ __forceinline__ u32 brev4(u32 p) { return __brev(p) >> 28; }
+
+__device__ __forceinline__ void split3(float x, __nv_bfloat16 &a, __nv_bfloat16 &b, __nv_bfloat16 &c)
+{
+    a = __float2bfloat16_rn(x);
+    const float r1 = x - __bfloat162float(a);
+    b = __float2bfloat16_rn(r1);
+    c = __float2bfloat16_rn(r1 - __bfloat162float(b));
+}
+
+// which split of the data (first) and of the matrix (second) product j uses
+__device__ __forceinline__ u32 prod_a(u32 j) { return j == 0 ? 0u : j == 1 ? 0u : j == 2 ? 1u : j == 3 ? 0u : j == 4 ? 1u : 2u; }
+__device__ __forceinline__ u32 prod_b(u32 j) { return j == 0 ? 0u : j == 1 ? 1u : j == 2 ? 0u : j == 3 ? 2u : j == 4 ? 1u : 0u; }
+
+// real 32 x 32 form of the 16-point step matrix: row kk = input real index
+// (0..15 real parts of input member p, 16..31 imaginary parts), column n =
+// output real index (0..15 real, 16..31 imaginary parts of output member m)
+template <int KIND>
+__device__ __forceinline__ float step_matrix(u32 kk, u32 n)
+{
+    const u32 p = kk & 15, m = n & 15;
+    if (KIND == TC_WHT) {  // real data: only the 16 x 16 block is used
+        return (__popc(p & m) & 1) ? -1.0f : 1.0f;
+    }
+    // forward: F[p][m] = exp(-2 pi i br(p) m / 16); inverse: G[m'][q] with input
+    // member p and output member m: exp(+2 pi i br(m) p / 16)
+    const u32 e = (KIND == TC_FFT) ? (brev4(p) * m) & 15 : (brev4(m) * p) & 15;
+    float s, c;
+    sincospif((float)e / 8.0f, &s, &c);
+    if (KIND == TC_FFT) s = -s;
+    const bool in_im = kk >= 16, out_im = n >= 16;
+    if (!in_im && !out_im) return c;   // Re(x) Re(F)
+    if (in_im && !out_im) return -s;   // -Im(x) Im(F)
+    if (!in_im && out_im) return s;    // Re(x) Im(F)
+    return c;                          // Im(x) Re(F)
+}
+
+// twiddle exp(sign * 2 pi i * t / 2^bits) in FP32 (t < 2^bits <= 2^24)
+__device__ __forceinline__ void twiddle(u64 t, u32 bits, float sign, float &wr, float &wi)
+{
+    float s, c;
+    sincospif(ldexpf((float)t, 1 - (int)bits), &s, &c);
+    wr = c;
+    wi = sign * s;
+}
+
+template <int KIND>
+__global__ void __launch_bounds__(FT_THREADS) tc_pass_kernel(TcPassArgs a, unsigned *err)
+{
+    extern __shared__ __align__(128) unsigned char sm[];
+    float *sr = (float *)sm;                            // [FT_TILE] real parts
+    float *si = sr + FT_TILE;                           // [FT_TILE] imaginary parts
+    unsigned char *sA = (unsigned char *)(si + FT_TILE);  // [128 x FT_KS] bf16 operand A
+    unsigned char *sB = sA + 128 * FT_KS * 2;           // [32 x FT_KS]  bf16 operand B
+    __shared__ __align__(8) u64 bar;
+    __shared__ u32 tmem_base;
+    const u32 warp = threadIdx.x / 32, lane = threadIdx.x % 32;
+    const u32 NOUT = (KIND == TC_WHT) ? 16u : 32u;      // GEMM N
+    const u32 KIN = (KIND == TC_WHT) ? 16u : 32u;       // reals per group and split
+
+    if (warp == 0) tc::tmem_alloc(&tmem_base, TMEM_COLS);
+    // operand B: the split step matrix, B[n][32j + kk] = M_b(j)[kk][n]
+    for (u32 e = threadIdx.x; e < NOUT * 6 * KIN; e += FT_THREADS) {
+        const u32 n = e / (6 * KIN), rest = e % (6 * KIN), j = rest / KIN, kk = rest % KIN;
+        __nv_bfloat16 m1, m2, m3;
+        split3(step_matrix<KIND>(kk, n), m1, m2, m3);
+        const u32 pb = prod_b(j);
+        *(__nv_bfloat16 *)(sB + tc::kmajor_offset(n, j * KIN + kk, 6 * KIN)) = pb == 0 ? m1 : pb == 1 ? m2 : m3;
+    }
+    if (threadIdx.x == 0) tc::mbar_init(&bar, 1);
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    const u32 tmem = tmem_base;
+    const u32 KTOT = 6 * KIN;
+    const u32 idesc = tc::idesc_bf16_f32(128, NOUT);
+    const u32 sbo = (KTOT / 8) * 128;
+    u32 phase = 0;
+    bool ok = true;
+
+    const u64 n = 1ull << a.L;
+    const u32 Q = a.Q, ct = a.ct;
+    const u64 cchunks = (a.k0 == 0) ? 1 : ((1ull << a.k0) / ct);
+    const u64 hchunks = (a.k0 == 0) ? 1 : (n >> a.k1);
+    const u64 tiles_per_vec = cchunks * hchunks;
+    const u64 ntiles = (a.k0 == 0) ? (a.total + FT_TILE - 1) / FT_TILE : (a.total / n) * tiles_per_vec;
+    const float tw_sign = (KIND == TC_FFT) ? -1.0f : 1.0f;
+
+    for (u64 tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
+        u64 base;
+        if (a.k0 == 0) {
+            base = tile * FT_TILE;
+        } else {
+            const u64 v = tile / tiles_per_vec, rem = tile % tiles_per_vec;
+            base = v * n + (rem / cchunks) * (1ull << a.k1) + (rem % cchunks) * ct;
+        }
+        // load (zeros beyond the data)
+        for (u32 e = threadIdx.x; e < Q * ct; e += FT_THREADS) {
+            const u64 f = base + ((u64)(e / ct) << a.k0) + (e % ct);
+            const bool in = f < a.total;
+            sr[e] = in ? (float)a.xr[f] : 0.0f;
+            if (KIND != TC_WHT) si[e] = in ? (float)a.xi[f] : 0.0f;
+        }
+        __syncthreads();
+        // steps over the pass's bits: FFT/WHT low to high, inverse high to low
+        const u32 nb = a.k1 - a.k0;
+        const u32 n16 = nb / 4, nrem = nb % 4;
+        for (u32 st = 0; st < n16 + nrem; st++) {
+            // step st covers bits [lo, lo + w) of the pass (w = 4 or 1)
+            u32 lo, w;
+            if (KIND == TC_IFFT) {  // remainder radix-2 bits first (highest), then radix-16 downward
+                if (st < nrem) { lo = nb - 1 - st; w = 1; }
+                else { lo = (n16 - 1 - (st - nrem)) * 4; w = 4; }
+            } else {
+                if (st < n16) { lo = st * 4; w = 4; }
+                else { lo = n16 * 4 + (st - n16); w = 1; }
+            }
+            const u32 k = a.k0 + lo;  // global bit of the step
+            if (w == 1) {
+                // FP32 radix-2 butterflies on bit k (as the reference's stage)
+                for (u32 b = threadIdx.x; b < Q * ct / 2; b += FT_THREADS) {
+                    const u32 cc = b % ct, pq = b / ct;
+                    const u32 q1 = ((pq >> lo) << (lo + 1)) | (pq & ((1u << lo) - 1));
+                    const u32 e1 = q1 * ct + cc, e2 = e1 + (1u << lo) * ct;
+                    if (KIND == TC_WHT) {
+                        const float x1 = sr[e1], x2 = sr[e2];
+                        sr[e1] = x1 + x2;
+                        sr[e2] = x1 - x2;
+                        continue;
+                    }
+                    const u64 f1 = base + ((u64)q1 << a.k0) + cc;
+                    float wr, wi;
+                    twiddle(f1 & ((1ull << k) - 1), k + 1, tw_sign, wr, wi);
+                    const float ar = sr[e1], ai = si[e1], br = sr[e2], bi = si[e2];
+                    if (KIND == TC_FFT) {
+                        const float yr = br * wr - bi * wi, yi = br * wi + bi * wr;
+                        sr[e1] = ar + yr; si[e1] = ai + yi; sr[e2] = ar - yr; si[e2] = ai - yi;
+                    } else {
+                        const float dr = ar - br, di = ai - bi;
+                        sr[e1] = ar + br; si[e1] = ai + bi;
+                        sr[e2] = dr * wr - di * wi; si[e2] = dr * wi + di * wr;
+                    }
+                }
+                __syncthreads();
+                continue;
+            }
+            // radix-16 step through the tensor cores, two M-tiles of 128 groups
+            for (u32 mt = 0; mt < FT_GROUPS / 128 && ok; mt++) {
+                // build A: thread t handles group 128*mt + t%128, members 8*(t/128) .. +7
+                {
+                    const u32 gi = 128 * mt + (threadIdx.x & 127), half = threadIdx.x >> 7;
+                    const u32 cc = gi % ct, qq = gi / ct;
+                    const u32 qlo = qq & ((1u << lo) - 1), qhi = qq >> lo;
+                    const u32 row = threadIdx.x & 127;
+                    for (u32 pp = 0; pp < 8; pp++) {
+                        const u32 p = half * 8 + pp;
+                        const u32 q = qlo | (p << lo) | (qhi << (lo + 4));
+                        const u32 e = q * ct + cc;
+                        float xr_ = sr[e], xi_ = (KIND == TC_WHT) ? 0.0f : si[e];
+                        if (KIND == TC_FFT) {  // pre-twiddle w^br(p)
+                            const u64 f = base + ((u64)q << a.k0) + cc;
+                            const u64 c = f & ((1ull << k) - 1);
+                            float wr, wi;
+                            twiddle((c * brev4(p)) & ((1ull << (k + 4)) - 1), k + 4, -1.0f, wr, wi);
+                            const float tr = xr_ * wr - xi_ * wi;
+                            xi_ = xr_ * wi + xi_ * wr;
+                            xr_ = tr;
+                        }
+                        __nv_bfloat16 r1, r2, r3, i1, i2, i3;
+                        split3(xr_, r1, r2, r3);
+                        if (KIND != TC_WHT) split3(xi_, i1, i2, i3);
+                        for (u32 j = 0; j < 6; j++) {
+                            const u32 pa = prod_a(j);
+                            *(__nv_bfloat16 *)(sA + tc::kmajor_offset(row, j * KIN + p, KTOT)) =
+                                pa == 0 ? r1 : pa == 1 ? r2 : r3;
+                            if (KIND != TC_WHT)
+                                *(__nv_bfloat16 *)(sA + tc::kmajor_offset(row, j * KIN + 16 + p, KTOT)) =
+                                    pa == 0 ? i1 : pa == 1 ? i2 : i3;
+                        }
+                    }
+                }
+                tc::fence_smem_to_async();
+                tc::fence_before_sync();
+                __syncthreads();
+                tc::fence_after_sync();
+                if (threadIdx.x == 0) {
+                    // accumulators: D0, D1 the two K-slices of x1*m1 (one MMA each),
+                    // D2 the products about 2^-8 smaller; summed in FP32 on read-back
+                    const u32 nmain = (KIND == TC_WHT) ? 1u : 2u;
+                    for (u32 s = 0; s < KTOT / 16; s++) {
+                        const u32 dst = tmem + (s < nmain ? 32u * s : 64u);
+                        tc::mma_bf16(dst, tc::smem_desc(sA + s * 256, 128, sbo), tc::smem_desc(sB + s * 256, 128, sbo),
+                                     idesc, s > nmain ? 1u : 0u);
+                    }
+                    tc::mma_commit(&bar);
+                }
+                ok = __syncthreads_and(tc::mbar_wait(&bar, phase, WAIT_LIMIT) ? 1 : 0);
+                phase ^= 1;
+                tc::fence_after_sync();
+                if (!ok) break;
+                // read back: warps 0-3 the real outputs, warps 4-7 the imaginary ones
+                {
+                    const u32 gi = 128 * mt + 32 * (warp & 3) + lane;
+                    const u32 cc = gi % ct, qq = gi / ct;
+                    const u32 qlo = qq & ((1u << lo) - 1), qhi = qq >> lo;
+                    const u32 col0 = (KIND == TC_WHT) ? 0u : 16u * (warp >> 2);
+                    if (KIND != TC_WHT || warp < 4) {
+                        const u32 lanes = (32 * (warp & 3)) << 16;
+                        u32 v0[16], v1[16], v2[16];
+                        tc::tmem_ld16(tmem + lanes + col0, v0);
+                        if (KIND != TC_WHT) tc::tmem_ld16(tmem + lanes + 32 + col0, v1);
+                        tc::tmem_ld16(tmem + lanes + 64 + col0, v2);
+                        tc::tmem_wait_ld();
+                        float *dst = (KIND == TC_WHT || warp < 4) ? sr : si;
+                        for (u32 m = 0; m < 16; m++) {
+                            const u32 q = qlo | (m << lo) | (qhi << (lo + 4));
+                            float y = __uint_as_float(v0[m]);
+                            if (KIND != TC_WHT) y += __uint_as_float(v1[m]);
+                            y += __uint_as_float(v2[m]);
+                            dst[q * ct + cc] = y;
+                        }
+                    }
+                }
+                tc::fence_before_sync();
+                __syncthreads();
+                if (KIND == TC_IFFT) {
+                    // post-twiddle w^-br(q) of the inverse step
+                    const u32 gi = 128 * mt + (threadIdx.x & 127), half = threadIdx.x >> 7;
+                    const u32 cc = gi % ct, qq = gi / ct;
+                    const u32 qlo = qq & ((1u << lo) - 1), qhi = qq >> lo;
+                    for (u32 pp = 0; pp < 8; pp++) {
+                        const u32 p = half * 8 + pp;
+                        const u32 q = qlo | (p << lo) | (qhi << (lo + 4));
+                        const u32 e = q * ct + cc;
+                        const u64 f = base + ((u64)q << a.k0) + cc;
+                        const u64 c = f & ((1ull << k) - 1);
+                        float wr, wi;
+                        twiddle((c * brev4(p)) & ((1ull << (k + 4)) - 1), k + 4, 1.0f, wr, wi);
+                        const float xr_ = sr[e], xi_ = si[e];
+                        sr[e] = xr_ * wr - xi_ * wi;
+                        si[e] = xr_ * wi + xi_ * wr;
+                    }
+                    __syncthreads();
+                }
+            }
+            if (!ok) break;
+        }
+        if (!ok) break;
+        // store
+        for (u32 e = threadIdx.x; e < Q * ct; e += FT_THREADS) {
+            const u64 f = base + ((u64)(e / ct) << a.k0) + (e % ct);
+            if (f < a.total) {
+                a.xr[f] = (double)(sr[e] * a.scale);
+                if (KIND != TC_WHT) a.xi[f] = (double)(si[e] * a.scale);
+            }
+        }
+        __syncthreads();
+    }
+    if (!ok && threadIdx.x == 0) atomicOr(err, 4u);
+    tc::fence_before_sync();
+    __syncthreads();
+    if (warp == 0) tc::tmem_dealloc(tmem, TMEM_COLS);
+}
+
+int run_tc(int kind, u64 d1, u64 d2, u64 n_half, double *xr, double *xi, cudaStream_t s, const char *what)
+{
+    QMC_REQUIRE_DOMAIN(n_half > 0 && (n_half & (n_half - 1)) == 0 && n_half <= (1ull << 23),
+                       "%s: n = 2*n_half must be a power of two up to 2^24", what);
+    const u64 nvec = d1 * d2, n = 2 * n_half;
+    if (nvec == 0) return QMC_OK;
+    QMC_REQUIRE(xr && (kind == TC_WHT || xi), "%s: null data pointer", what);
+    unsigned *err = qmcgb::device_error_ptr();
+    QMC_REQUIRE(err, "device error word unavailable");
+    u32 L = 0;
+    while ((1ull << L) < n) L++;
+    // passes: bits [0, min(L,12)), then chunks of at most 8 bits
+    struct P { u32 k0, k1; } passes[8];
+    int np = 0;
+    passes[np++] = {0, L < 12 ? L : 12};
+    for (u32 k0 = 12; k0 < L; k0 += 8) passes[np++] = {k0, (k0 + 8 < L) ? k0 + 8 : L};
+    const size_t smem = FT_TILE * 8 + 128 * FT_KS * 2 + 32 * FT_KS * 2;
+    const float scale = (float)(1.0 / sqrt((double)n));
+    for (int pi = 0; pi < np; pi++) {
+        const P p = (kind == TC_IFFT) ? passes[np - 1 - pi] : passes[pi];
+        TcPassArgs A;
+        A.total = nvec * n;
+        A.L = L;
+        A.k0 = p.k0;
+        A.k1 = p.k1;
+        if (p.k0 == 0) {
+            A.Q = FT_TILE;
+            A.ct = 1;
+        } else {
+            A.Q = 1u << (p.k1 - p.k0);
+            A.ct = FT_TILE / A.Q;
+            if ((1ull << p.k0) < A.ct) A.ct = (u32)(1ull << p.k0);
+        }
+        A.xr = xr;
+        A.xi = xi;
+        A.scale = (pi == np - 1) ? scale : 1.0f;
+        const u64 tiles = (p.k0 == 0) ? (A.total + FT_TILE - 1) / FT_TILE : A.total / (A.Q * (u64)A.ct);
+        const unsigned grid = qmcgb::grid_for(tiles, 1, (unsigned)qmcgb::sm_count() * 2);
+        cudaError_t e;
+        if (kind == TC_FFT) {
+            e = cudaFuncSetAttribute(tc_pass_kernel<TC_FFT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            if (e == cudaSuccess) tc_pass_kernel<TC_FFT><<<grid, FT_THREADS, smem, s>>>(A, err);
+        } else if (kind == TC_IFFT) {
+            e = cudaFuncSetAttribute(tc_pass_kernel<TC_IFFT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            if (e == cudaSuccess) tc_pass_kernel<TC_IFFT><<<grid, FT_THREADS, smem, s>>>(A, err);
+        } else {
+            e = cudaFuncSetAttribute(tc_pass_kernel<TC_WHT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            if (e == cudaSuccess) tc_pass_kernel<TC_WHT><<<grid, FT_THREADS, smem, s>>>(A, err);
+        }
+        if (e != cudaSuccess) return qmcgb::cuda_status(e, what);
+        if (int rc = qmcgb::launch_status(what)) return rc;
+    }
+    return QMC_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int qmc_tc_fft_bro_1d(uint64_t d1, uint64_t d2, uint64_t n_half, double *xr, double *xi, qmc_stream_t s)
+{
+    return run_tc(TC_FFT, d1, d2, n_half, xr, xi, QMC_STREAM(s), "tc_fft_bro_1d");
+}
+
+int qmc_tc_ifft_bro_1d(uint64_t d1, uint64_t d2, uint64_t n_half, double *xr, double *xi, qmc_stream_t s)
+{
+    return run_tc(TC_IFFT, d1, d2, n_half, xr, xi, QMC_STREAM(s), "tc_ifft_bro_1d");
+}
+
+int qmc_tc_fwht_1d(uint64_t d1, uint64_t d2, uint64_t n_half, double *x, qmc_stream_t s)
+{
+    return run_tc(TC_WHT, d1, d2, n_half, x, nullptr, QMC_STREAM(s), "tc_fwht_1d");
+}
+
+}  // extern "C"

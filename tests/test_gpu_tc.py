@@ -1,0 +1,66 @@
+"""The tcgen05 (fifth-generation tensor core) building blocks: a one-CTA
+BF16 x BF16 -> FP32 MMA through tensor memory, with the shared-memory and
+instruction descriptors the tensor-core transforms use, against an exact
+host product (small integers are exact in BF16 and in the FP32 sums)."""
+import ctypes
+
+import numpy as np
+import pytest
+
+from qmctoolscl_gb300 import _ffi
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("N,K", [(16, 16), (32, 16), (32, 64), (64, 32), (128, 128), (256, 16), (32, 192)])
+def test_tcgen05_mma_probe_exact(N, K):
+    import torch
+    g = torch.Generator().manual_seed(N * 1000 + K)
+    A = torch.randint(-8, 9, (128, K), generator=g).to(torch.bfloat16).cuda()
+    B = torch.randint(-8, 9, (N, K), generator=g).to(torch.bfloat16).cuda()
+    D = torch.full((128, N), float("nan"), dtype=torch.float32, device="cuda")
+    L = _ffi.lib()
+    s = torch.cuda.current_stream().cuda_stream
+    _ffi.check(L.qmc_tc_mma_probe(A.data_ptr(), B.data_ptr(), D.data_ptr(), N, K, s), "tc_mma_probe")
+    _ffi.check(L.qmc_device_error_check(ctypes.c_void_p(s)), "tc_mma_probe wait")
+    want = A.double() @ B.double().T
+    assert torch.equal(D.double(), want)
+
+
+def _bitrev(m):
+    i = np.arange(1 << m)
+    out = np.zeros_like(i)
+    for b in range(m):
+        out |= ((i >> b) & 1) << (m - 1 - b)
+    return out
+
+
+@pytest.mark.parametrize("m,d1,d2", [(1, 1, 1), (4, 2, 3), (5, 1, 1), (8, 3, 5), (10, 2, 2), (11, 1, 3), (12, 2, 1),
+                                     (13, 1, 2), (16, 1, 1), (17, 2, 1), (20, 1, 1)])
+def test_tc_fft_and_inverse_against_numpy(m, d1, d2):
+    from qmctoolscl_gb300 import tc_fft
+    rng = np.random.Generator(np.random.SFC64(m))
+    n = 1 << m
+    z = rng.standard_normal((d1, d2, n)) + 1j * rng.standard_normal((d1, d2, n))
+    xr, xi = np.ascontiguousarray(z.real), np.ascontiguousarray(z.imag)
+    tc_fft.fft_bro_1d_tc(d1, d2, n // 2, xr, xi)
+    want = np.fft.fft(z[:, :, _bitrev(m)], norm="ortho")
+    err = np.linalg.norm((xr + 1j * xi) - want) / np.linalg.norm(want)
+    assert err < 1e-6, err
+    tc_fft.ifft_bro_1d_tc(d1, d2, n // 2, xr, xi)
+    err2 = np.linalg.norm((xr + 1j * xi) - z) / np.linalg.norm(z)
+    assert err2 < 1e-6, err2
+
+
+@pytest.mark.parametrize("m", [1, 4, 7, 12, 14, 19])
+def test_tc_fwht_against_fp64(m):
+    from qmctoolscl_gb300 import tc_fft
+    import qmctoolscl_gb300 as q
+    rng = np.random.Generator(np.random.SFC64(100 + m))
+    n = 1 << m
+    x = rng.standard_normal((2, 1, n))
+    want = x.copy()
+    q.fwht_1d_radix2(np.uint64(2), np.uint64(1), np.uint64(n // 2), want)
+    tc_fft.fwht_1d_tc(2, 1, n // 2, x)
+    err = np.linalg.norm(x - want) / np.linalg.norm(want)
+    assert err < 1e-6, err
