@@ -738,7 +738,184 @@ def run_fft(args):
             "gpu_launches": None}
 
 
-WORKLOADS = {"net_plain": run_net_plain, "net_lms": run_net_lms, "fft": run_fft}
+def first_primes(k):
+    out, c = [], 2
+    while len(out) < k:
+        if all(c % p for p in out if p * p <= c):
+            out.append(c)
+        c += 1
+    return out
+
+
+def halton_inputs(r, log2n, d, seed=4):
+    """Per-dimension inputs of the randomised Halton workload: bases = the
+    first d primes, tmax_j = ceil(64/log2 b), mmax_j = ceil(log2n/log2 b)
+    (at least the base-b digits of n-1), identity generating matrices, and
+    the reference's generators for S, perms and shifts called per dimension
+    (d=1, r_b=1, tmax_new=tmax_j) in dimension order."""
+    import math
+    import qmctoolscl_gb300 as q
+    rng = np.random.Generator(np.random.SFC64(seed))
+    dims = []
+    for b in first_primes(d):
+        tmax = math.ceil(64 / math.log2(b))
+        mmax, v = 0, (1 << log2n) - 1
+        while v:
+            v //= b
+            mmax += 1
+        mmax = max(mmax, math.ceil(log2n / math.log2(b)))
+        bb = np.array([[b]], np.uint64)
+        C = np.ascontiguousarray(q.gdn_get_halton_generating_matrix(1, 1, max(mmax, tmax))[:, :, :mmax, :tmax])
+        dims.append(dict(b=b, tmax=tmax, mmax=mmax, C=C,
+                         S=q.gdn_get_linear_scramble_matrix(rng, r, 1, tmax, tmax, 1, bb),
+                         perms=q.gdn_get_digital_permutations(rng, r, 1, tmax, 1, bb),
+                         shifts=q.gdn_get_digital_shifts(rng, r, 1, tmax, 1, bb)))
+    return dims
+
+
+def halton_oracle(dims, l, i0, cnt):
+    """The reference chain on the oracle, one dimension per call, for
+    randomisation l and points [i0, i0+cnt): an (cnt, d) float64 array."""
+    import oracle
+    U = np.uint64
+    out = np.empty((cnt, len(dims)))
+    for j, dm in enumerate(dims):
+        b, tmax, mmax = dm["b"], dm["tmax"], dm["mmax"]
+        bb = np.array([[b]], U)
+        S = np.ascontiguousarray(dm["S"][l:l + 1])
+        C_lms = np.empty((1, 1, mmax, tmax), U)
+        oracle.call("gdn_linear_matrix_scramble", U(1), U(1), U(mmax), U(1), U(1), U(tmax), U(tmax), bb, S, dm["C"],
+                    C_lms)
+        xdig = np.empty((1, cnt, 1, tmax), U)
+        oracle.call("gdn_gen_natural", U(1), U(cnt), U(1), U(1), U(mmax), U(tmax), U(i0), bb, C_lms, xdig)
+        xp = np.empty_like(xdig)
+        oracle.call("gdn_digital_permutation", U(1), U(cnt), U(1), U(1), U(1), U(tmax), U(tmax), U(b),
+                    np.ascontiguousarray(dm["perms"][l:l + 1]), xdig, xp)
+        xs = np.empty_like(xdig)
+        oracle.call("gdn_digital_shift", U(1), U(cnt), U(1), U(1), U(1), U(tmax), U(tmax), bb,
+                    np.ascontiguousarray(dm["shifts"][l:l + 1]), xp, xs)
+        x = np.empty((1, cnt, 1))
+        oracle.call("gdn_integer_to_float", U(1), U(cnt), U(1), U(1), U(tmax), bb, xs, x)
+        out[:, j] = x[0, :, 0]
+    return out
+
+
+def run_halton(args):
+    """Randomised Halton / generalized digital net: bases = first 100 primes,
+    d=100, n=2^18, r=32, tmax_j = ceil(64/log2 b); LMS -> generation ->
+    digit permutation -> digital shift -> float, bit-exact.  value: the fused
+    plan (prepare + generate per step); plain: the reference's five calls per
+    dimension through the C ABI with the digit tensors in HBM."""
+    import torch
+    from qmctoolscl_gb300 import _ffi, batch, halton
+    lib = _ffi.lib()
+    r, log2n, d = (8 if args.small else 32), 18, 100
+    n = 1 << log2n
+    dims = halton_inputs(r, log2n, d)
+    st = torch.cuda.current_stream()
+    h = st.cuda_stream
+    ddims = [dict(b=dm["b"], tmax=dm["tmax"], mmax=dm["mmax"], C=dev_tensor(dm["C"]), S=dev_tensor(dm["S"]),
+                  perms=dev_tensor(dm["perms"]), shifts=dev_tensor(dm["shifts"])) for dm in dims]
+    x = torch.empty((r, n, d), dtype=torch.float64, device="cuda")
+    plan = halton.HaltonPlan(r, n, 0, ddims, x)
+
+    def fused():
+        plan.prepare(st)
+        plan.run(st)
+
+    _ffi.check(lib.qmc_device_error_reset(h), "reset")
+    plan.prepare(st)
+    ms_gen = gpu_ms(lambda: plan.run(st), args.steps, args.warmup, st)
+    if args.small:
+        return {"small": True, "r": r, "gen_ms": ms_gen, "gbs": 8.0 * r * n * d / (ms_gen / 1e3) / 1e9}
+    clocks = ClockSampler(0)
+    clocks.start()
+    ms_fused = gpu_ms(fused, args.steps, args.warmup, st)
+    clk = clocks.stop()
+    _ffi.check(lib.qmc_device_error_check(h), "halton plan")
+    # parity: two slices against the oracle chain
+    for l, i0 in ((0, 0), (r - 1, n - 1500)):
+        want = halton_oracle(dims, l, i0, 1500)
+        got = x[l, i0:i0 + 1500].cpu().numpy()
+        assert np.array_equal(got.view(np.uint64), want.view(np.uint64)), "fused Halton differs from the oracle"
+
+    # plain: per dimension, LMS -> gen -> perm -> shift -> float, then the column into x
+    tmax_hi = max(dm["tmax"] for dm in dims)
+    mm_hi = max(dm["mmax"] for dm in dims)
+    xdig = torch.empty(r * n * tmax_hi, dtype=torch.int64, device="cuda")
+    xp, xs = torch.empty_like(xdig), torch.empty_like(xdig)
+    C_lms = torch.empty(r * mm_hi * tmax_hi, dtype=torch.int64, device="cuda")
+    col = torch.empty((r, n), dtype=torch.float64, device="cuda")
+    x2 = torch.empty_like(x)
+    bases = [dev_tensor(np.array([[dm["b"]]], np.uint64)) for dm in dims]
+
+    def plain():
+        for j, (dm, dd) in enumerate(zip(dims, ddims)):
+            b, tmax, mmax, bp = dm["b"], dm["tmax"], dm["mmax"], bases[j].data_ptr()
+            _ffi.check(lib.qmc_gdn_linear_matrix_scramble(r, 1, mmax, 1, 1, tmax, tmax, bp, dd["S"].data_ptr(),
+                                                          dd["C"].data_ptr(), C_lms.data_ptr(), h), "lms")
+            _ffi.check(lib.qmc_gdn_gen_natural(r, n, 1, 1, mmax, tmax, 0, bp, C_lms.data_ptr(), xdig.data_ptr(), h),
+                       "gen")
+            _ffi.check(lib.qmc_gdn_digital_permutation(r, n, 1, r, 1, tmax, tmax, b, dd["perms"].data_ptr(),
+                                                       xdig.data_ptr(), xp.data_ptr(), h), "perm")
+            _ffi.check(lib.qmc_gdn_digital_shift(r, n, 1, r, 1, tmax, tmax, bp, dd["shifts"].data_ptr(),
+                                                 xp.data_ptr(), xs.data_ptr(), h), "shift")
+            _ffi.check(lib.qmc_gdn_integer_to_float(r, n, 1, 1, tmax, bp, xs.data_ptr(), col.data_ptr(), h), "float")
+            x2[:, :, j].copy_(col)
+
+    ms_plain = gpu_ms(plain, 2, 1, st)
+    torch.cuda.synchronize()
+    assert torch.equal(x.view(torch.int64), x2.view(torch.int64)), "fused Halton differs from the plain chain"
+    digit_bytes = sum(r * n * dm["tmax"] * 8 for dm in dims)
+    del xdig, xp, xs, x2, col
+    torch.cuda.empty_cache()
+
+    # e2e: numpy inputs copied in, the points written into pinned host memory, every step
+    xh = batch.pinned_empty((r, n, d))
+    halton.generalized_net_fused(r, n, 0, dims, xh)
+    e2e_steps = max(1, min(args.steps, 3))
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        A = halton.generalized_net_fused(r, n, 0, dims, xh, check=False)
+    t_e2e = (time.perf_counter() - t0) / e2e_steps
+    assert np.array_equal(xh.view(np.uint64), x.cpu().numpy().view(np.uint64))
+
+    # CPU: the oracle chain on a sample of randomisation 0, all host threads
+    threads = host_threads()
+    pieces = [(0, k * 4096, 4096) for k in range(2 * threads)]
+    halton_oracle(dims, 0, 0, 64)
+    t0 = time.perf_counter()
+    with concurrent.futures.ThreadPoolExecutor(threads) as ex:
+        list(ex.map(lambda a: halton_oracle(dims, *a), pieces))
+    t_cpu = time.perf_counter() - t0
+    cpu_pts = sum(p[2] for p in pieces)
+    pts = r * n
+    alg = 8.0 * r * n * d
+    return {"metric": METRIC, "value": pts / (ms_fused / 1e3), "unit": "points/s", "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_fused, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "u32 digits, f64 (integer-emulated) output",
+            "data": "synthetic (np.random.SFC64(4)): reference generators per dimension",
+            "config": {"workload": "randomised Halton, bases = first 100 primes, d=100, n=2^18, r=32, "
+                                   "tmax_j=ceil(64/log2 b), LMS + permutation + digital shift + float "
+                                   "(fused plan: prepare + generate)", "r": r, "n": n, "d": d,
+                       "l2": "6.7 GB output per step >> 129 MB L2, no flush needed"},
+            "roofline": dict(roofline(alg, ms_gen), kernel="halton_gen_kernel",
+                             note="generation kernel alone; integer-throughput bound, see profiles/"),
+            "generate_only_ms": ms_gen,
+            "plain": {"ms_per_step": ms_plain, "points_per_s": pts / (ms_plain / 1e3), "launches_per_step": 5 * d,
+                      "digit_tensor_bytes": digit_bytes, "fused_speedup": ms_plain / ms_fused},
+            "e2e": {"value": pts / t_e2e, "unit": "points/s", "ms_per_step": 1e3 * t_e2e,
+                    "h2d_bytes_per_step": A.h2d_bytes, "d2h_bytes_per_step": A.d2h_bytes,
+                    "direct_host_write": A.direct,
+                    "path": "qmctoolscl_gb300.halton.generalized_net_fused, numpy inputs, pinned numpy output"},
+            "gpu_launches": 3 * args.steps, "clocks": clk,
+            "cpu_baseline": {"value": cpu_pts / t_cpu, "unit": "points/s", "cores": threads, "kind": "port",
+                             "sample": "randomisation 0, %d points in %d pieces of 4096, all 100 dimensions; the "
+                                       "oracle chain per dimension, one piece per thread" % (cpu_pts, len(pieces)),
+                             "seconds": t_cpu}}
+
+
+WORKLOADS = {"net_plain": run_net_plain, "net_lms": run_net_lms, "fft": run_fft, "halton": run_halton}
 
 
 def main():

@@ -36,7 +36,9 @@ enum qmc_status {
     QMC_ERR_ARG = -1,    /* bad size, null pointer or unsupported argument combination */
     QMC_ERR_DOMAIN = -2, /* arguments for which the reference's result is undefined */
     QMC_ERR_CUDA = -3,   /* a CUDA runtime or launch error */
-    QMC_ERR_DEVICE = -4  /* a kernel met an index the reference would read out of its array */
+    QMC_ERR_DEVICE = -4  /* a kernel recorded an error in the device error word (bits: 1 an index the
+                            reference would read out of its array, 2 a base below 2, 4 a tensor-core
+                            completion wait that ran out, 8 a fused generalized-net entry >= 2^32) */
 };
 
 /* message of the last failing call on this host thread ("" if none) */
@@ -46,7 +48,7 @@ int qmc_version(void);
 /* clears the device error word on stream s */
 int qmc_device_error_reset(qmc_stream_t s);
 /* synchronises s, then returns QMC_ERR_DEVICE (and clears the word) if a
- * kernel recorded an out-of-array index since the last reset */
+ * kernel recorded an error since the last reset */
 int qmc_device_error_check(qmc_stream_t s);
 
 /* device-side address of pinned host memory (cudaHostAlloc / cudaHostRegister)
@@ -264,6 +266,36 @@ int qmc_plan_set_tuning(qmc_plan *plan, int ctas_per_sm, int chunk, uint64_t til
 /* tiles, coordinates and output bytes of one run, kernel launches per run */
 int qmc_plan_info(const qmc_plan *plan, uint64_t *tiles, uint64_t *coords, uint64_t *bytes_out, int *launches);
 int qmc_plan_destroy(qmc_plan *plan);
+
+/* ---- fused generalized digital net (per-dimension bases, e.g. Halton) -------
+ * For every dimension j the reference chain
+ *   gdn_linear_matrix_scramble  qmctoolscl/c_funcs/gdn_linear_matrix_scramble.c:3-46
+ *   gdn_gen_natural             qmctoolscl/c_funcs/gdn_gen_natural.c:3-53
+ *   gdn_digital_permutation     qmctoolscl/c_funcs/gdn_digital_permutation.c:3-46
+ *   gdn_digital_shift           qmctoolscl/c_funcs/gdn_digital_shift.c:3-45
+ *   gdn_integer_to_float        qmctoolscl/c_funcs/gdn_integer_to_float.c:3-43
+ * called with d = 1, r_b = 1, r_C = 1 and tmax_new = tmax, its result going to
+ * x[l, i, j] of one r*n*d array; digits never reach HBM.  A step whose array
+ * is NULL (S, perms or shifts, the same for every dimension) is left out of
+ * the chain.  Bases in [2, 2048), n_start + n <= 2^32, mmax at least the
+ * base-b digits of the last index, permutation and shift entries below 2^32
+ * (and, without S, generating-matrix entries below 2^32): entries outside
+ * that range set bit 8 of the device error word.  Create allocates the
+ * packed tables; prepare fills them from the arrays the dims point to (read
+ * at that time, on the stream); run generates x. */
+typedef struct qmc_gdn_dim {
+    uint64_t b, tmax, mmax;
+    const uint64_t *S;      /* r * tmax * tmax scrambling matrices */
+    const uint64_t *C;      /* mmax * tmax generating matrix */
+    const uint64_t *perms;  /* r * tmax * b digit permutations */
+    const uint64_t *shifts; /* r * tmax digital shifts */
+} qmc_gdn_dim;
+typedef struct qmc_halton_plan qmc_halton_plan;
+int qmc_halton_plan_create(uint64_t r, uint64_t n, uint64_t n_start, uint64_t d, const qmc_gdn_dim *dims, double *x,
+                           qmc_halton_plan **plan);
+int qmc_halton_plan_prepare(qmc_halton_plan *plan, qmc_stream_t s);
+int qmc_halton_plan_run(qmc_halton_plan *plan, qmc_stream_t s);
+int qmc_halton_plan_destroy(qmc_halton_plan *plan);
 
 /* ---- one digital-net request without any allocation -------------------------
  * No counterpart in the reference.  For callers that cannot call cudaMalloc

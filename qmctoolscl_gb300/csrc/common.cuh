@@ -19,6 +19,7 @@
 
 typedef unsigned long long u64;
 typedef unsigned int u32;
+typedef unsigned short u16;
 
 // ---------------------------------------------------------------- bits ----
 

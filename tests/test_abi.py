@@ -63,3 +63,35 @@ def test_argument_errors_need_no_gpu(lib):
     # non-power-of-two transform length
     rc = L.qmc_fwht_1d_radix2(1, 1, 3, None, None)
     assert rc == _ffi.QMC_ERR_DOMAIN
+
+
+def test_generalized_net_plan_argument_errors_need_no_gpu(lib):
+    """qmc_halton_plan_create validates every dimension on the host, before
+    any allocation; the array pointers are never dereferenced there."""
+    from qmctoolscl_gb300 import _ffi, halton
+    L = halton._lib()
+    fake = ctypes.c_void_p(0x1000)
+    x = ctypes.c_void_p(0x2000)
+
+    def create(dims, r=1, n=8, n_start=0):
+        arr = (halton.GdnDim * len(dims))(*dims)
+        h = ctypes.c_void_p()
+        rc = L.qmc_halton_plan_create(r, n, n_start, len(dims), arr, x, ctypes.byref(h))
+        assert h.value is None
+        return rc, L.qmc_last_error()
+
+    def dim(b=3, tmax=4, mmax=3, **kw):
+        args = dict(b=b, tmax=tmax, mmax=mmax, S=fake, C=fake, perms=fake, shifts=fake)
+        args.update(kw)
+        return halton.GdnDim(**args)
+
+    assert create([dim(b=1)])[0] == _ffi.QMC_ERR_DOMAIN             # the reference never ends its digit loop
+    assert create([dim(b=2048)])[0] == _ffi.QMC_ERR_ARG
+    assert create([dim(tmax=0)])[0] == _ffi.QMC_ERR_ARG
+    assert create([dim(mmax=65)])[0] == _ffi.QMC_ERR_ARG
+    rc, msg = create([dim(b=2, mmax=2)], n=8)                       # index 7 has 3 binary digits
+    assert rc == _ffi.QMC_ERR_ARG and b"digits" in msg
+    rc, msg = create([dim(), dim(S=None)])                          # LMS for some dimensions only
+    assert rc == _ffi.QMC_ERR_ARG and b"all dimensions" in msg
+    assert create([dim()], n=1, n_start=(1 << 32))[0] == _ffi.QMC_ERR_ARG
+    assert create([dim(C=None)])[0] == _ffi.QMC_ERR_ARG

@@ -1,0 +1,173 @@
+"""Fused generalized digital net (randomised Halton) against the oracle.
+
+The oracle runs the reference chain one dimension at a time (d = 1, r_b = 1,
+tmax_new = tmax_j): gdn_linear_matrix_scramble -> gdn_gen_natural ->
+gdn_digital_permutation -> gdn_digital_shift -> gdn_integer_to_float, and the
+fused plan must reproduce every float bit for bit.  Inputs come from the
+reference's own generators (rand_funcs), drawn per dimension in order.
+"""
+import math
+
+import numpy as np
+import pytest
+
+import oracle
+import qmctoolscl_gb300 as q
+from qmctoolscl_gb300 import halton
+
+pytestmark = pytest.mark.gpu
+U = np.uint64
+
+PRIMES = [p for p in range(2, 542) if all(p % k for k in range(2, int(p ** 0.5) + 1))]
+
+
+def digits_needed(n_last, b):
+    k = 0
+    while n_last:
+        n_last //= b
+        k += 1
+    return max(k, 1)
+
+
+def make_dims(rng, r, bases, n_last, bits=64, lms=True, perm=True, shift=True, tmax_cap=None):
+    """Per-dimension inputs in the reference's shapes at d = 1."""
+    dims = []
+    for b in bases:
+        tmax = math.ceil(bits / math.log2(b))
+        if tmax_cap:
+            tmax = min(tmax, tmax_cap)
+        mmax = digits_needed(n_last, b)
+        bb = np.array([[b]], U)
+        C = q.gdn_get_halton_generating_matrix(1, 1, max(mmax, tmax))[:, :, :mmax, :tmax]
+        dim = dict(b=b, tmax=tmax, mmax=mmax, C=np.ascontiguousarray(C))
+        if lms:
+            dim["S"] = q.gdn_get_linear_scramble_matrix(rng, r, 1, tmax, tmax, 1, bb)
+        if perm:
+            dim["perms"] = q.gdn_get_digital_permutations(rng, r, 1, tmax, 1, bb)
+        if shift:
+            dim["shifts"] = q.gdn_get_digital_shifts(rng, r, 1, tmax, 1, bb)
+        dims.append(dim)
+    return dims
+
+
+def oracle_chain(r, n, n_start, dims):
+    """The reference's functions, one dimension per call, on the oracle."""
+    out = np.empty((r, n, len(dims)), np.float64)
+    for j, dm in enumerate(dims):
+        b, tmax, mmax = dm["b"], dm["tmax"], dm["mmax"]
+        bb = np.array([[b]], U)
+        C = dm["C"]
+        if dm.get("S") is not None:
+            C_lms = np.zeros((r, 1, mmax, tmax), U)
+            oracle.call("gdn_linear_matrix_scramble", U(r), U(1), U(mmax), U(1), U(1), U(tmax), U(tmax), bb,
+                        dm["S"], C, C_lms)
+        else:
+            C_lms = np.ascontiguousarray(np.broadcast_to(C, (r, 1, mmax, tmax)))
+        xdig = np.zeros((r, n, 1, tmax), U)
+        oracle.call("gdn_gen_natural", U(r), U(n), U(1), U(1), U(mmax), U(tmax), U(n_start), bb, C_lms, xdig)
+        if dm.get("perms") is not None:
+            xp = np.zeros_like(xdig)
+            oracle.call("gdn_digital_permutation", U(r), U(n), U(1), U(r), U(1), U(tmax), U(tmax), U(b),
+                        dm["perms"], xdig, xp)
+            xdig = xp
+        if dm.get("shifts") is not None:
+            xs = np.zeros_like(xdig)
+            oracle.call("gdn_digital_shift", U(r), U(n), U(1), U(r), U(1), U(tmax), U(tmax), bb, dm["shifts"],
+                        xdig, xs)
+            xdig = xs
+        x = np.zeros((r, n, 1), np.float64)
+        oracle.call("gdn_integer_to_float", U(r), U(n), U(1), U(1), U(tmax), bb, xdig, x)
+        out[:, :, j] = x[:, :, 0]
+    return out
+
+
+def run_fused(r, n, n_start, dims):
+    x = np.full((r, n, len(dims)), np.nan)
+    halton.generalized_net_fused(r, n, n_start, dims, x)
+    return x
+
+
+def same_bits(a, b):
+    return np.array_equal(np.asarray(a).view(U), np.asarray(b).view(U))
+
+
+@pytest.mark.parametrize("n,n_start", [(700, 13), (64, 0), (1, 5), (33, 2 ** 20 - 7)])
+def test_halton_full_chain_matches_oracle(n, n_start):
+    rng = np.random.Generator(np.random.SFC64(11 + n))
+    r = 3
+    bases = [PRIMES[k] for k in (0, 1, 2, 3, 4, 10, 25, 50, 75, 97, 98, 99)]
+    dims = make_dims(rng, r, bases, n_start + n - 1)
+    assert same_bits(run_fused(r, n, n_start, dims), oracle_chain(r, n, n_start, dims))
+
+
+def test_halton_first_100_primes_matches_oracle():
+    """The benchmark's shape (every base of the first 100 primes, digit counts
+    ceil(64/log2 b)), on 2 randomisations of 600 points."""
+    rng = np.random.Generator(np.random.SFC64(2024))
+    r, n, n_start = 2, 600, 1000
+    dims = make_dims(rng, r, PRIMES[:100], n_start + n - 1)
+    assert same_bits(run_fused(r, n, n_start, dims), oracle_chain(r, n, n_start, dims))
+
+
+@pytest.mark.parametrize("lms,perm,shift", [(False, False, False), (True, False, False), (False, True, False),
+                                            (False, False, True), (True, False, True), (True, True, False)])
+def test_halton_partial_chains(lms, perm, shift):
+    rng = np.random.Generator(np.random.SFC64(7 + 4 * lms + 2 * perm + shift))
+    r, n, n_start = 2, 300, 3
+    bases = [2, 3, 5, 7, 11, 97, 541, 1999]
+    dims = make_dims(rng, r, bases, n_start + n - 1, lms=lms, perm=perm, shift=shift)
+    assert same_bits(run_fused(r, n, n_start, dims), oracle_chain(r, n, n_start, dims))
+
+
+def test_halton_unscrambled_is_radical_inverse():
+    """Without randomisation the first dimension (base 2) is the van der
+    Corput sequence: exact dyadic values."""
+    r, n = 1, 256
+    dims = make_dims(None, r, [2, 3], n - 1, lms=False, perm=False, shift=False)
+    x = run_fused(r, n, 0, dims)
+    vdc = np.array([int(format(i, "064b")[::-1], 2) / 2.0 ** 64 for i in range(n)])
+    assert np.array_equal(x[0, :, 0], vdc)
+
+
+def test_halton_big_permutation_values_and_deep_digits():
+    """Permutation entries at or above b without a shift (the digit-to-float
+    step then sees large digits, so no term may be skipped) and 80 digits."""
+    rng = np.random.Generator(np.random.SFC64(99))
+    r, n, n_start = 2, 200, 0
+    dims = make_dims(rng, r, [3, 5, 31], n - 1, bits=140, shift=False, tmax_cap=80)
+    for dm in dims:
+        dm["perms"] = dm["perms"] + U(1) + rng.integers(0, 5000, dm["perms"].shape, dtype=U)
+    assert same_bits(run_fused(r, n, n_start, dims), oracle_chain(r, n, n_start, dims))
+
+
+def test_halton_matches_plain_drop_in_chain():
+    """The fused plan against the plain drop-in functions (GPU, one call per
+    step and dimension) on the same inputs."""
+    rng = np.random.Generator(np.random.SFC64(5))
+    r, n, n_start = 2, 500, 17
+    dims = make_dims(rng, r, [2, 13, 233], n_start + n - 1)
+    plain = np.empty((r, n, len(dims)))
+    for j, dm in enumerate(dims):
+        b, tmax, mmax = dm["b"], dm["tmax"], dm["mmax"]
+        bb = np.array([[b]], U)
+        C_lms = np.zeros((r, 1, mmax, tmax), U)
+        q.gdn_linear_matrix_scramble(U(r), U(1), U(mmax), U(1), U(1), U(tmax), U(tmax), bb, dm["S"], dm["C"], C_lms)
+        xdig = np.zeros((r, n, 1, tmax), U)
+        q.gdn_gen_natural(U(r), U(n), U(1), U(1), U(mmax), U(tmax), U(n_start), bb, C_lms, xdig)
+        xp = np.zeros_like(xdig)
+        q.gdn_digital_permutation(U(r), U(n), U(1), U(r), U(1), U(tmax), U(tmax), U(b), dm["perms"], xdig, xp)
+        xs = np.zeros_like(xdig)
+        q.gdn_digital_shift(U(r), U(n), U(1), U(r), U(1), U(tmax), U(tmax), bb, dm["shifts"], xp, xs)
+        x = np.zeros((r, n, 1))
+        q.gdn_integer_to_float(U(r), U(n), U(1), U(1), U(tmax), bb, xs, x)
+        plain[:, :, j] = x[:, :, 0]
+    assert same_bits(run_fused(r, n, n_start, dims), plain)
+
+
+def test_halton_entry_above_32_bits_is_reported():
+    rng = np.random.Generator(np.random.SFC64(1))
+    dims = make_dims(rng, 1, [3], 9)
+    dims[0]["shifts"] = dims[0]["shifts"].copy()
+    dims[0]["shifts"][0, 0, 0] = U(1 << 40)
+    with pytest.raises(q._ffi.QmcError, match="2\\^32"):
+        run_fused(1, 10, 0, dims)
