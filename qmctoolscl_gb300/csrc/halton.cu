@@ -13,7 +13,7 @@
 // x[l, i, j] of one r x n x d array -- bit for bit, without ever storing a
 // digit in HBM.
 //
-// Plan creation packs, in one preparation kernel: the scrambled generating
+// Preparation (one kernel per plan run) packs the scrambled generating
 // matrices reduced mod b (the reference's gen step reduces after every
 // column; with entries of at most tmax*(b-1) no 64-bit sum wraps, so one
 // reduction of reduced terms gives the same digits), the permutations and
@@ -23,15 +23,20 @@
 // Generation: a CTA owns a tile of 32 consecutive points of one
 // randomisation and all d dimensions.  Each warp takes whole dimensions
 // (assigned longest-first to balance tmax_j * (mmax_j + c) work), one point
-// per lane, so the 32 lanes share base, digit count and tables.  Per digit t:
-// the base-b digits of the index times column t (32-bit direct remainders),
-// the permutation gather, the shift mod b, and v = RN(v + RN(recip_t * digit))
-// in integer arithmetic (dmul_small_bits, dadd_pos_bits).  The tile of
+// per lane, so the 32 lanes share base, digit count and tables.  The index
+// splits as hi * b^K + lo with b^K >= 32: the tile has at most two distinct
+// hi, whose contributions to each output digit the lanes compute together,
+// and K <= 5 low digits per lane.  Per output digit t: the digit mod b, the
+// permutation gather, the shift mod b, and v = RN(v + RN(recip_t * digit)) in
+// integer arithmetic on the unpacked sum (digit_sum.cuh); the FP64 unit is
+// slow on this GPU and the kernel is bound by integer issue.  Once every
+// remaining term is below half an ulp of v the lane stops.  The tile of
 // doubles is staged in shared memory and stored as 32 contiguous rows.
 #include <algorithm>
 #include <vector>
 
 #include "common.cuh"
+#include "digit_sum.cuh"
 
 namespace {
 
@@ -41,11 +46,14 @@ constexpr u32 HT_MAX_DIMS = 1024;
 constexpr u32 HT_MAX_B = 2048;  // bases below 2^11: digit * recip fits the integer product
 
 struct HDim {
-    u32 b, tmax, mmax, pad;
+    u32 b, tmax, mmax, K;  // K low digits per lane: the smallest K with b^K >= 32
     u64 c_off;     // offset of this dimension's (mmax x tmax) block inside a randomisation's C block
     u64 p_off;     // offset of its (tmax x b) permutation block inside a randomisation's block
     u64 s_off;     // offset of its tmax shifts inside a randomisation's block
     u64 fd_M;      // direct-remainder constant for b
+    u64 fdK_M;     // the same for b^K
+    u32 bK;
+    u32 Klo;       // min(K, mmax): low digits that can be nonzero (C has mmax rows)
 };
 
 struct HPlanDev {
@@ -154,11 +162,41 @@ __global__ void halton_recip_kernel(HPlanDev P, u64 *recip, u32 *tail)
 
 // ---------------------------------------------------------------- generation
 
-__device__ __noinline__ u64 halton_step_hw(u64 v, u64 rc, u32 s)
+// RN(v + RN(rc * s)) for the terms the fast form does not take: the general
+// integer routine where it is exact, else the FP64 unit (kept out of line, so
+// the FP64 instructions are not if-converted into the fast path)
+__device__ __noinline__ u64 halton_step_slow(u64 v, u64 rc, u32 s)
 {
+    if (dsum::general_ok(v, rc, s)) return dsum::add_bits(v, dsum::mul_bits(rc, s));
     return as_bits(__dadd_rn(as_double(v), __dmul_rn(as_double(rc), (double)s)));
 }
 
+// floor(x / b) and x mod b for x < 2^32, b >= 2, from M = floor((2^64-1)/b) + 1
+__device__ __forceinline__ u32 hdiv(u64 M, u32 x) { return (u32)__umul64hi(M, (u64)x); }
+__device__ __forceinline__ u32 hmod(u64 M, u32 b, u32 x) { return (u32)__umul64hi(M * (u64)x, (u64)b); }
+
+// sum over the base-b digits k >= K of the index (the digits of h = index / b^K)
+// of digit * C[k][t], reduced mod b
+__device__ __forceinline__ u32 high_part(const HDim &D, const u32 *Cj, u32 h, u32 t)
+{
+    u32 acc = 0;
+    for (u32 k = D.K; h && k < D.mmax; k++) {
+        const u32 q = hdiv(D.fd_M, h);
+        acc += (h - q * D.b) * Cj[k * D.tmax + t];  // < mmax * b^2 < 2^32
+        h = q;
+    }
+    return hmod(D.fd_M, D.b, acc);
+}
+
+// A CTA owns 32 consecutive points of one randomisation (lane = point) and
+// all d dimensions; warp w runs dimensions order[wstart[w] .. wstart[w+1]).
+// Index split: itrue = hi * b^K + lo with b^K >= 32, so the tile's indices
+// have at most two distinct hi (h0, h0 + 1).  Per chunk of 32 output digits
+// lane c computes the high-digit sums of digit t0 + c for both, packed into
+// one word, and every lane takes its own from lane t - t0 by a shuffle; the
+// K <= 5 low digits are per lane.  Lanes stay converged (shuffles); a lane
+// whose remaining terms are all below half an ulp of its sum idles, and the
+// warp leaves the dimension when all have.
 __global__ void __launch_bounds__(HT_THREADS) halton_gen_kernel(HPlanDev P)
 {
     extern __shared__ __align__(16) unsigned char sm[];
@@ -166,57 +204,80 @@ __global__ void __launch_bounds__(HT_THREADS) halton_gen_kernel(HPlanDev P)
     const u32 warp = threadIdx.x / 32, lane = threadIdx.x % 32;
     const u64 tiles_per_l = (P.n + 31) / 32;
     const u64 ntiles = P.r * tiles_per_l;
+    const bool early = !(*P.flags & 1u);
     for (u64 tt = blockIdx.x; tt < ntiles; tt += gridDim.x) {
         const u64 l = tt / tiles_per_l, i0 = (tt % tiles_per_l) * 32;
-        const u64 i = i0 + lane;
-        const bool active = i < P.n;  // lanes past the last point compute nothing
-        const u64 itrue = P.n_start + i;
+        const bool active = i0 + lane < P.n;  // lanes past the last point compute nothing
+        const u32 base = (u32)(P.n_start + i0);
+        const u32 itrue = active ? base + lane : base;  // < 2^32 (checked at plan creation)
         const u32 *Cl = P.C + l * P.c_per_l;
         const u32 *Pl = P.perm + l * P.p_per_l;
         const u32 *Sl = P.shift + l * P.s_per_l;
-        const bool early = !(*P.flags & 1u);
         for (u32 oi = P.wstart[warp]; oi < P.wstart[warp + 1]; oi++) {
             const u32 j = P.order[oi];
             const HDim D = P.dims[j];
-            FastDiv32 fd;
-            fd.b = D.b;
-            fd.M = D.fd_M;
             const u32 *Cj = Cl + D.c_off;
             const u32 *Pj = Pl + D.p_off;
             const u32 *Sj = Sl + D.s_off;
             const u64 *Rj = P.recip + D.s_off;
             const u32 *Tj = P.tail + D.s_off;
-            u64 v = 0;  // bits of the running sum (non-negative double)
-            for (u32 t = 0; active && t < D.tmax; t++) {
-                // Every later term is at most RN(recip_t*(b-1)) (recip_t only shrinks); once that lies
-                // below half an ulp of v (its exponent at most exp(v) - 54), RN(v + term) = v for the
-                // rest of the digits, so they need not be computed.
-                if (early && v && Tj[t] + 54 <= (u32)(v >> 52)) break;
-                // gdn_gen_natural.c:37-50: digits of itrue times column t, mod b
-                u32 x = (u32)itrue, acc = 0;
-                for (u32 k = 0; x; k++) {
-                    const u32 q = fd_div(fd, x);
-                    const u32 dig = x - q * D.b;
+            const u32 h0 = hdiv(D.fdK_M, base);
+            const u32 hi = hdiv(D.fdK_M, itrue);
+            const u32 sel = (hi - h0) * 16;  // 0 or 16: which half of the packed word
+            u32 dl[5];                        // low digits (zero beyond K)
+            {
+                u32 x = itrue - hi * D.bK;
+#pragma unroll
+                for (int k = 0; k < 5; k++) {
+                    const u32 q = hdiv(D.fd_M, x);
+                    dl[k] = x - q * D.b;
                     x = q;
-                    acc += dig * Cj[k * D.tmax + t];  // < mmax * b^2 < 2^32
-                }
-                const u32 xd = fd_mod(fd, acc);
-                const u32 pv = P.has_perm ? Pj[t * D.b + xd] : xd;  // gdn_digital_permutation.c:36-39
-                u32 sv = pv;
-                if (P.has_shift) {                                 // gdn_digital_shift.c:37-39
-                    const u64 sum = (u64)pv + Sj[t];
-                    sv = sum < (1ull << 32) ? fd_mod(fd, (u32)sum) : (u32)(sum % D.b);
-                }
-                if (sv) {                                          // gdn_integer_to_float.c:35-38
-                    const u64 rb = Rj[t];
-                    const u32 er = (u32)(rb >> 52);
-                    if (sv < 2048 && er >= 1 && er < 2036 && (v >> 52) < 2000)
-                        v = dadd_pos_bits(v, dmul_small_bits(rb, sv));
-                    else
-                        v = halton_step_hw(v, rb, sv);
                 }
             }
-            tile[lane * P.d + j] = as_double(v);
+            bool done = !active;
+            dsum::Sum v = dsum::unpack(0);  // the running sum of gdn_integer_to_float, unpacked
+            for (u32 t0 = 0; t0 < D.tmax; t0 += 32) {
+                if (__all_sync(0xffffffffu, done)) break;
+                u32 packed = 0;
+                if (t0 + lane < D.tmax)
+                    packed = high_part(D, Cj, h0, t0 + lane) | (high_part(D, Cj, h0 + 1, t0 + lane) << 16);
+                const u32 tend = min(D.tmax, t0 + 32);
+                for (u32 t = t0; t < tend; t++) {
+                    if (__all_sync(0xffffffffu, done)) break;
+                    const u32 hp = (__shfl_sync(0xffffffffu, packed, t - t0) >> sel) & 0xFFFFu;
+                    if (done) continue;
+                    // Every later term is at most RN(recip_t*(b-1)) (recip_t only shrinks); once that
+                    // lies below half an ulp of v (exponent at most exp(v) - 54), RN(v + term) = v for
+                    // the remaining digits.
+                    if (early && v.M && Tj[t] + 54 <= v.E) {
+                        done = true;
+                        continue;
+                    }
+                    // gdn_gen_natural.c:37-50: digit t of the point, mod b
+                    u32 acc = hp;
+#pragma unroll
+                    for (u32 k = 0; k < 5; k++)
+                        if (k < D.Klo) acc += dl[k] * Cj[k * D.tmax + t];
+                    const u32 xd = hmod(D.fd_M, D.b, acc);
+                    const u32 pv = P.has_perm ? Pj[t * D.b + xd] : xd;  // gdn_digital_permutation.c:36-39
+                    u32 sv = pv;
+                    if (P.has_shift) {                                 // gdn_digital_shift.c:37-39
+                        const u64 sum = (u64)pv + Sj[t];
+                        if (sum < 2ull * D.b)
+                            sv = (u32)sum >= D.b ? (u32)sum - D.b : (u32)sum;
+                        else
+                            sv = sum < (1ull << 32) ? hmod(D.fd_M, D.b, (u32)sum) : (u32)(sum % D.b);
+                    }
+                    if (sv) {                                          // gdn_integer_to_float.c:35-38
+                        const u64 rb = Rj[t];
+                        const u32 er = (u32)(rb >> 52);
+                        if (!((v.M >> 52) && sv < 2048 && er - 1u < 2035u &&
+                              dsum::add_term_fast(v, (rb & dsum::FRAC) | dsum::HIDDEN, er, sv)))
+                            v = dsum::unpack(halton_step_slow(dsum::pack(v), rb, sv));
+                    }
+                }
+            }
+            tile[lane * P.d + j] = as_double(dsum::pack(v));
         }
         __syncthreads();
         // 32 contiguous rows of the output
@@ -286,6 +347,14 @@ int qmc_halton_plan_create(uint64_t r, uint64_t n, uint64_t n_start, uint64_t d,
         h.p_off = p_off;
         h.s_off = s_off;
         h.fd_M = fastdiv32_make((u32)q.b).M;
+        h.K = 1;
+        h.bK = (u32)q.b;
+        while (h.bK < 32) {
+            h.bK *= (u32)q.b;
+            h.K++;
+        }
+        h.fdK_M = fastdiv32_make(h.bK).M;
+        h.Klo = std::min<u32>(h.K, (u32)q.mmax);
         c_off += q.mmax * q.tmax;
         p_off += has_perm ? q.tmax * q.b : 0;
         s_off += q.tmax;
