@@ -825,9 +825,17 @@ def run_halton(args):
 
     _ffi.check(lib.qmc_device_error_reset(h), "reset")
     plan.prepare(st)
-    ms_gen = gpu_ms(lambda: plan.run(st), args.steps, args.warmup, st)
-    if args.small:
+    if args.small:  # profiling mode: the default split of the adds, generation only
+        ms_gen = gpu_ms(lambda: plan.run(st), args.steps, args.warmup, st)
         return {"small": True, "r": r, "gen_ms": ms_gen, "gbs": 8.0 * r * n * d / (ms_gen / 1e3) / 1e9}
+    # the share of digit adds on the FP64 unit (the rest in integer arithmetic): pick the fastest
+    sweep = {}
+    for share in (0.0, 0.25, 0.5, 0.75, 1.0):
+        plan.set_fp64_share(share)
+        sweep[share] = gpu_ms(lambda: plan.run(st), 3, 1, st)
+    best_share = min(sweep, key=sweep.get)
+    plan.set_fp64_share(best_share)
+    ms_gen = gpu_ms(lambda: plan.run(st), args.steps, args.warmup, st)
     clocks = ClockSampler(0)
     clocks.start()
     ms_fused = gpu_ms(fused, args.steps, args.warmup, st)
@@ -902,6 +910,7 @@ def run_halton(args):
             "roofline": dict(roofline(alg, ms_gen), kernel="halton_gen_kernel",
                              note="generation kernel alone; integer-throughput bound, see profiles/"),
             "generate_only_ms": ms_gen,
+            "fp64_share": {"chosen": best_share, "generate_ms_by_share": {str(k): v for k, v in sweep.items()}},
             "plain": {"ms_per_step": ms_plain, "points_per_s": pts / (ms_plain / 1e3), "launches_per_step": 5 * d,
                       "digit_tensor_bytes": digit_bytes, "fused_speedup": ms_plain / ms_fused},
             "e2e": {"value": pts / t_e2e, "unit": "points/s", "ms_per_step": 1e3 * t_e2e,

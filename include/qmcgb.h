@@ -38,7 +38,7 @@ enum qmc_status {
     QMC_ERR_CUDA = -3,   /* a CUDA runtime or launch error */
     QMC_ERR_DEVICE = -4  /* a kernel recorded an error in the device error word (bits: 1 an index the
                             reference would read out of its array, 2 a base below 2, 4 a tensor-core
-                            completion wait that ran out, 8 a fused generalized-net entry >= 2^32) */
+                            completion wait that ran out, 8 a fused generalized-net matrix entry >= 2^32) */
 };
 
 /* message of the last failing call on this host thread ("" if none) */
@@ -278,11 +278,13 @@ int qmc_plan_destroy(qmc_plan *plan);
  * x[l, i, j] of one r*n*d array; digits never reach HBM.  A step whose array
  * is NULL (S, perms or shifts, the same for every dimension) is left out of
  * the chain.  Bases in [2, 2048), n_start + n <= 2^32, mmax at least the
- * base-b digits of the last index, permutation and shift entries below 2^32
- * (and, without S, generating-matrix entries below 2^32): entries outside
- * that range set bit 8 of the device error word.  Create allocates the
- * packed tables; prepare fills them from the arrays the dims point to (read
- * at that time, on the stream); run generates x. */
+ * base-b digits of the last index; without S, generating-matrix entries
+ * below 2^32 (larger ones set bit 8 of the device error word).  Create
+ * allocates the packed tables; prepare fills them from the arrays the dims
+ * point to (read at that time, on the stream); run generates x.
+ * set_fp64_share picks the share of the digit adds that run on the FP64
+ * unit (the rest run in integer arithmetic, same bits either way), a tuning
+ * knob for the balance between the two pipes (default 0.5). */
 typedef struct qmc_gdn_dim {
     uint64_t b, tmax, mmax;
     const uint64_t *S;      /* r * tmax * tmax scrambling matrices */
@@ -295,6 +297,7 @@ int qmc_halton_plan_create(uint64_t r, uint64_t n, uint64_t n_start, uint64_t d,
                            qmc_halton_plan **plan);
 int qmc_halton_plan_prepare(qmc_halton_plan *plan, qmc_stream_t s);
 int qmc_halton_plan_run(qmc_halton_plan *plan, qmc_stream_t s);
+int qmc_halton_plan_set_fp64_share(qmc_halton_plan *plan, double share);
 int qmc_halton_plan_destroy(qmc_halton_plan *plan);
 
 /* ---- one digital-net request without any allocation -------------------------

@@ -13,25 +13,34 @@
 // x[l, i, j] of one r x n x d array -- bit for bit, without ever storing a
 // digit in HBM.
 //
-// Preparation (one kernel per plan run) packs the scrambled generating
-// matrices reduced mod b (the reference's gen step reduces after every
-// column; with entries of at most tmax*(b-1) no 64-bit sum wraps, so one
-// reduction of reduced terms gives the same digits), the permutations and
-// the shifts as 32-bit words, and 1/b^(t+1) as the reference computes it
-// (repeated correctly rounded divisions).
+// Preparation (per plan run, small next to the output):
+//  * the scrambled generating matrices reduced mod b, as 32-bit words (the
+//    reference's gen step reduces after every column; with entries of at
+//    most tmax*(b-1) no 64-bit sum wraps, so one reduction of reduced terms
+//    gives the same digits);
+//  * recip_t = 1/b^(t+1) as the reference computes it (repeated correctly
+//    rounded divisions);
+//  * the term table Y[l][j][t][g] = RN(recip_t * digit) for every raw digit
+//    g < b, where digit = (perm[l][t][g] + shift[l][t]) mod b (either step
+//    left out when its array is absent).  Once the raw digit g of output
+//    digit t is known, permutation, shift and the rounded product of
+//    gdn_integer_to_float.c:37 are one table read;
+//  * the tail table: for each (l, j, t) the largest exponent among the terms
+//    of digits t..tmax-1, for an exact early stop.
 //
 // Generation: a CTA owns a tile of 32 consecutive points of one
 // randomisation and all d dimensions.  Each warp takes whole dimensions
-// (assigned longest-first to balance tmax_j * (mmax_j + c) work), one point
-// per lane, so the 32 lanes share base, digit count and tables.  The index
-// splits as hi * b^K + lo with b^K >= 32: the tile has at most two distinct
-// hi, whose contributions to each output digit the lanes compute together,
-// and K <= 5 low digits per lane.  Per output digit t: the digit mod b, the
-// permutation gather, the shift mod b, and v = RN(v + RN(recip_t * digit)) in
-// integer arithmetic on the unpacked sum (digit_sum.cuh); the FP64 unit is
-// slow on this GPU and the kernel is bound by integer issue.  Once every
-// remaining term is below half an ulp of v the lane stops.  The tile of
-// doubles is staged in shared memory and stored as 32 contiguous rows.
+// (assigned longest-first to balance the work), one point per lane, so the
+// 32 lanes share base, digit count and tables.  The index splits as
+// hi * b^K + lo with b^K >= 32: the tile has at most two distinct hi, whose
+// contributions to each output digit the lanes compute together, and K <= 5
+// low digits per lane.  Per output digit t: the raw digit mod b (32-bit
+// multiply-high division), the term from the table, and v = RN(v + term) --
+// on the FP64 unit or in integer arithmetic on the unpacked sum
+// (digit_sum.cuh), chosen per dimension so that the FP64 pipe and the integer
+// pipes share the work.  Once every remaining term is below half an ulp of v
+// the lane stops.  The tile of doubles is staged in shared memory and stored
+// as 32 contiguous rows.
 #include <algorithm>
 #include <vector>
 
@@ -43,42 +52,61 @@ namespace {
 constexpr int HT_THREADS = 256;
 constexpr int HT_WARPS = HT_THREADS / 32;
 constexpr u32 HT_MAX_DIMS = 1024;
-constexpr u32 HT_MAX_B = 2048;  // bases below 2^11: digit * recip fits the integer product
+constexpr u32 HT_MAX_B = 2048;
+
+enum : u32 { ADD_FP64 = 0, ADD_INT = 1 };
 
 struct HDim {
-    u32 b, tmax, mmax, K;  // K low digits per lane: the smallest K with b^K >= 32
-    u64 c_off;     // offset of this dimension's (mmax x tmax) block inside a randomisation's C block
-    u64 p_off;     // offset of its (tmax x b) permutation block inside a randomisation's block
-    u64 s_off;     // offset of its tmax shifts inside a randomisation's block
-    u64 fd_M;      // direct-remainder constant for b
-    u64 fdK_M;     // the same for b^K
-    u32 bK;
+    u32 b, tmax, mmax;
+    u32 K;         // low digits per lane: the smallest K with b^K >= 32
     u32 Klo;       // min(K, mmax): low digits that can be nonzero (C has mmax rows)
+    u32 bK;        // b^K
+    u32 m32;       // floor(2^32 / b) + 1: x / b = umulhi(x, m32) for x < 2^32 / b
+    u32 wide;      // 1 when digit sums can reach 2^32 / b: 64-bit remainders instead
+    u32 add;       // ADD_FP64 or ADD_INT
+    u32 pad;
+    u64 fd_M;      // direct-remainder constant for b (any 32-bit x)
+    u64 fdK_M;     // the same for b^K
+    u64 c_off;     // offset of this dimension's (mmax x tmax) block inside a randomisation's C block
+    u64 y_off;     // offset of its (tmax x b) term rows inside a randomisation's Y block
+    u64 s_off;     // offset of its tmax digits inside the recip / tail blocks
 };
 
 struct HPlanDev {
     u64 r, n, n_start, d;
-    u64 c_per_l, p_per_l, s_per_l;  // words per randomisation
+    u64 c_per_l, y_per_l, s_per_l;  // words per randomisation
     u32 has_lms, has_perm, has_shift, pad;
     const HDim *dims;
-    const u32 *C;                    // r * c_per_l: scrambled matrices mod b
-    const u32 *perm;                 // r * p_per_l
-    const u32 *shift;                // r * s_per_l
-    const u64 *recip;                // s_per_l: bits of 1/b^(t+1), per (j, t)
-    const u32 *tail;                 // s_per_l: biased exponent of RN(recip_t * (b-1)), per (j, t)
-    const unsigned *flags;           // bit 0: some digit can reach b (permutation values >= b, no shift)
-    const u16 *order;                // d dimension ids, warp-balanced: dims of warp w at order[wstart[w]..wstart[w+1])
-    const u32 *wstart;               // HT_WARPS + 1
+    const u32 *C;        // r * c_per_l: scrambled matrices mod b
+    const u64 *Y;        // r * y_per_l: term bits RN(recip_t * digit)
+    const u64 *recip;    // s_per_l: bits of recip_t, per (j, t)
+    const u32 *tail;     // r * s_per_l: largest biased exponent among the terms of digits t.. of (l, j)
+    const u16 *order;    // d dimension ids: warp w runs order[wstart[w] .. wstart[w+1])
+    const u32 *wstart;   // HT_WARPS + 1
     double *x;
     unsigned *err;
 };
-
-// ---------------------------------------------------------------- prep
 
 struct PrepDim {
     u64 b, tmax, mmax;
     const u64 *S, *C, *perms, *shifts;  // caller's per-dimension arrays
 };
+
+// floor(x / b) and x mod b for any x < 2^32, b >= 2, from M = floor((2^64-1)/b) + 1
+__device__ __forceinline__ u32 hdiv(u64 M, u32 x) { return (u32)__umul64hi(M, (u64)x); }
+__device__ __forceinline__ u32 hmod(u64 M, u32 b, u32 x) { return (u32)__umul64hi(M * (u64)x, (u64)b); }
+
+// the same for x < 2^32 / b, with m32 = floor(2^32/b) + 1: x*m32/2^32 exceeds
+// x/b by less than x/2^32 < 1/b, too little to reach the next integer
+__device__ __forceinline__ u32 ndiv(u32 m32, u32 x) { return __umulhi(x, m32); }
+__device__ __forceinline__ u32 nmod(u32 m32, u32 b, u32 x) { return x - __umulhi(x, m32) * b; }
+
+__device__ __forceinline__ u32 dim_mod(const HDim &D, u32 x)
+{
+    return D.wide ? hmod(D.fd_M, D.b, x) : nmod(D.m32, D.b, x);
+}
+
+// ---------------------------------------------------------------- prep
 
 // the dimension whose block (offset `field` of HDim) holds offset off
 template <typename F>
@@ -95,58 +123,36 @@ __device__ __forceinline__ u32 dim_of(const HDim *dims, u64 d, u64 off, F field)
     return lo;
 }
 
-// one thread per (l, j, k, t) word of C, (l, j, t, c) of perms, (l, j, t) of shifts
-__global__ void halton_prep_kernel(HPlanDev P, const PrepDim *pd, u64 total_c, u64 total_p, u64 total_s,
-                                   u32 *C, u32 *perm, u32 *shift, unsigned *flags)
+// one thread per (l, j, k, t) word of C
+__global__ void halton_lms_kernel(HPlanDev P, const PrepDim *pd, u64 total_c, u32 *C)
 {
     const u64 stride = (u64)gridDim.x * blockDim.x;
-    for (u64 w = (u64)blockIdx.x * blockDim.x + threadIdx.x; w < total_c + total_p + total_s; w += stride) {
-        if (w < total_c) {
-            const u64 l = w / P.c_per_l, off = w % P.c_per_l;
-            const u32 j = dim_of(P.dims, P.d, off, [](const HDim &h) { return h.c_off; });
-            const HDim &D = P.dims[j];
-            const u64 loc = off - D.c_off, k = loc / D.tmax, t = loc % D.tmax;
-            const PrepDim &Q = pd[j];
-            if (P.has_lms) {
-                // gdn_linear_matrix_scramble.c:36-42 with d = 1, r_C = 1: sum_c (S[l,t,c]*C[k,c]) % b, no
-                // final mod; the sum is at most tmax*(b-1) and the generation step reduces it anyway
-                const u64 *srow = Q.S + (l * Q.tmax + t) * Q.tmax;
-                const u64 *col = Q.C + k * Q.tmax;
-                u64 acc = 0;
-                for (u64 c = 0; c < Q.tmax; c++) acc += (srow[c] * col[c]) % Q.b;
-                C[w] = (u32)(acc % Q.b);
-            } else {
-                // the generation step multiplies raw entries by digits below b in 64 bits: entries below
-                // 2^32 cannot wrap, so reducing them first gives the same digits
-                const u64 c = Q.C[k * Q.tmax + t];
-                if (c >> 32) atomicOr(P.err, 8u);
-                C[w] = (u32)(c % Q.b);
-            }
-        } else if (w < total_c + total_p) {
-            const u64 v = w - total_c;
-            const u64 l = v / P.p_per_l, off = v % P.p_per_l;
-            const u32 j = dim_of(P.dims, P.d, off, [](const HDim &h) { return h.p_off; });
-            const HDim &D = P.dims[j];
-            const u64 loc = off - D.p_off;  // t * b + c
-            const u64 val = pd[j].perms[l * D.tmax * D.b + loc];
-            if (val >> 32) atomicOr(P.err, 8u);
-            if (!P.has_shift && val >= D.b) atomicOr(flags, 1u);  // float digits not bounded by b-1
-            perm[v] = (u32)val;
+    for (u64 w = (u64)blockIdx.x * blockDim.x + threadIdx.x; w < total_c; w += stride) {
+        const u64 l = w / P.c_per_l, off = w % P.c_per_l;
+        const u32 j = dim_of(P.dims, P.d, off, [](const HDim &h) { return h.c_off; });
+        const HDim &D = P.dims[j];
+        const u64 loc = off - D.c_off, k = loc / D.tmax, t = loc % D.tmax;
+        const PrepDim &Q = pd[j];
+        if (P.has_lms) {
+            // gdn_linear_matrix_scramble.c:36-42 with d = 1, r_C = 1: sum_c (S[l,t,c]*C[k,c]) % b, no final
+            // mod; the sum is at most tmax*(b-1) and the generation step reduces it anyway
+            const u64 *srow = Q.S + (l * Q.tmax + t) * Q.tmax;
+            const u64 *col = Q.C + k * Q.tmax;
+            u64 acc = 0;
+            for (u64 c = 0; c < Q.tmax; c++) acc += (srow[c] * col[c]) % Q.b;
+            C[w] = (u32)(acc % Q.b);
         } else {
-            const u64 v = w - total_c - total_p;
-            const u64 l = v / P.s_per_l, off = v % P.s_per_l;
-            const u32 j = dim_of(P.dims, P.d, off, [](const HDim &h) { return h.s_off; });
-            const HDim &D = P.dims[j];
-            const u64 val = pd[j].shifts[l * D.tmax + (off - D.s_off)];
-            if (val >> 32) atomicOr(P.err, 8u);
-            shift[v] = (u32)val;
+            // the generation step multiplies raw entries by digits below b in 64 bits: entries below
+            // 2^32 cannot wrap, so reducing them first gives the same digits
+            const u64 c = Q.C[k * Q.tmax + t];
+            if (c >> 32) atomicOr(P.err, 8u);
+            C[w] = (u32)(c % Q.b);
         }
     }
 }
 
-// recip_t of gdn_integer_to_float.c:34-38 for every (j, t), and the exponent
-// of the largest term recip_t can contribute, RN(recip_t * (b-1))
-__global__ void halton_recip_kernel(HPlanDev P, u64 *recip, u32 *tail)
+// recip_t of gdn_integer_to_float.c:34-38 for every (j, t)
+__global__ void halton_recip_kernel(HPlanDev P, u64 *recip)
 {
     for (u64 j = (u64)blockIdx.x * blockDim.x + threadIdx.x; j < P.d; j += (u64)gridDim.x * blockDim.x) {
         const HDim &D = P.dims[j];
@@ -154,49 +160,136 @@ __global__ void halton_recip_kernel(HPlanDev P, u64 *recip, u32 *tail)
         double rc = __ddiv_rn(1.0, bd);
         for (u32 t = 0; t < D.tmax; t++) {
             recip[D.s_off + t] = as_bits(rc);
-            tail[D.s_off + t] = (u32)(as_bits(__dmul_rn(rc, (double)(D.b - 1))) >> 52);
             rc = __ddiv_rn(rc, bd);
+        }
+    }
+}
+
+// One warp per term row (l, j, t): Y[g] = RN(recip_t * digit(g)) for g < b,
+// digit(g) = (perm[l,t,g] + shift[l,t]) mod b as gdn_digital_permutation.c:36-39
+// and gdn_digital_shift.c:37-39 compute it (64-bit wrapping add), then
+// (double)digit * recip_t as gdn_integer_to_float.c:36-37.  Lane 0 records
+// the row's largest exponent in tail[l][s_off + t].
+__global__ void halton_terms_kernel(HPlanDev P, const PrepDim *pd, u64 rows, u64 *Y, u32 *tail)
+{
+    const u32 lane = threadIdx.x % 32;
+    const u64 wstride = (u64)gridDim.x * (blockDim.x / 32);
+    for (u64 row = ((u64)blockIdx.x * blockDim.x + threadIdx.x) / 32; row < rows; row += wstride) {
+        const u64 l = row / P.s_per_l, off = row % P.s_per_l;
+        const u32 j = dim_of(P.dims, P.d, off, [](const HDim &h) { return h.s_off; });
+        const HDim &D = P.dims[j];
+        const PrepDim &Q = pd[j];
+        const u64 t = off - D.s_off;
+        const double rc = as_double(P.recip[D.s_off + t]);
+        const u64 sh = P.has_shift ? Q.shifts[l * D.tmax + t] : 0;
+        u64 *yrow = Y + l * P.y_per_l + D.y_off + t * D.b;
+        u64 mx = 0;
+        for (u32 g = lane; g < D.b; g += 32) {
+            const u64 pv = P.has_perm ? Q.perms[(l * D.tmax + t) * D.b + g] : g;
+            const u64 dig = P.has_shift ? (pv + sh) % D.b : pv;
+            const u64 y = dig ? as_bits(__dmul_rn(rc, __ull2double_rn(dig))) : 0;
+            yrow[g] = y;
+            mx = max(mx, y);  // non-negative doubles order like their bits
+        }
+        for (int o = 16; o; o >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+        if (lane == 0) tail[l * P.s_per_l + off] = (u32)(mx >> 52);
+    }
+}
+
+// suffix maximum over t of the row exponents, per (l, j)
+__global__ void halton_tail_kernel(HPlanDev P, u32 *tail)
+{
+    for (u64 w = (u64)blockIdx.x * blockDim.x + threadIdx.x; w < P.r * P.d; w += (u64)gridDim.x * blockDim.x) {
+        const u64 l = w / P.d, j = w % P.d;
+        const HDim &D = P.dims[j];
+        u32 *tl = tail + l * P.s_per_l + D.s_off;
+        u32 m = 0;
+        for (u32 t = D.tmax; t-- > 0;) {
+            m = max(m, tl[t]);
+            tl[t] = m;
         }
     }
 }
 
 // ---------------------------------------------------------------- generation
 
-// RN(v + RN(rc * s)) for the terms the fast form does not take: the general
-// integer routine where it is exact, else the FP64 unit (kept out of line, so
-// the FP64 instructions are not if-converted into the fast path)
-__device__ __noinline__ u64 halton_step_slow(u64 v, u64 rc, u32 s)
+// RN(v + y) for the sums the integer fast form does not take (first term,
+// carry into the next binade, subnormal operands): the FP64 unit, out of line
+__device__ __noinline__ u64 halton_add_slow(u64 v, u64 y) { return as_bits(__dadd_rn(as_double(v), as_double(y))); }
+
+// v = RN(v + y) on the unpacked sum, y = the bits of a non-negative double
+__device__ __forceinline__ void add_term_int(dsum::Sum &v, u64 y)
 {
-    if (dsum::general_ok(v, rc, s)) return dsum::add_bits(v, dsum::mul_bits(rc, s));
-    return as_bits(__dadd_rn(as_double(v), __dmul_rn(as_double(rc), (double)s)));
+    if (dsum::add_fast(v, y) || !y) return;
+    v = dsum::unpack(v.M ? halton_add_slow(dsum::pack(v), y) : y);  // 0 + y = y exactly
 }
 
-// floor(x / b) and x mod b for x < 2^32, b >= 2, from M = floor((2^64-1)/b) + 1
-__device__ __forceinline__ u32 hdiv(u64 M, u32 x) { return (u32)__umul64hi(M, (u64)x); }
-__device__ __forceinline__ u32 hmod(u64 M, u32 b, u32 x) { return (u32)__umul64hi(M * (u64)x, (u64)b); }
-
-// sum over the base-b digits k >= K of the index (the digits of h = index / b^K)
-// of digit * C[k][t], reduced mod b
+// sum over the base-b digits k >= K of h (the digits of index / b^K) of
+// digit * C[k][t], reduced mod b; h < 2^32 / b^K
 __device__ __forceinline__ u32 high_part(const HDim &D, const u32 *Cj, u32 h, u32 t)
 {
     u32 acc = 0;
     for (u32 k = D.K; h && k < D.mmax; k++) {
-        const u32 q = hdiv(D.fd_M, h);
-        acc += (h - q * D.b) * Cj[k * D.tmax + t];  // < mmax * b^2 < 2^32
+        const u32 q = ndiv(D.m32, h);
+        acc += (h - q * D.b) * Cj[k * D.tmax + t];  // < mmax * b^2
         h = q;
     }
-    return hmod(D.fd_M, D.b, acc);
+    return dim_mod(D, acc);
 }
 
-// A CTA owns 32 consecutive points of one randomisation (lane = point) and
-// all d dimensions; warp w runs dimensions order[wstart[w] .. wstart[w+1]).
-// Index split: itrue = hi * b^K + lo with b^K >= 32, so the tile's indices
-// have at most two distinct hi (h0, h0 + 1).  Per chunk of 32 output digits
-// lane c computes the high-digit sums of digit t0 + c for both, packed into
-// one word, and every lane takes its own from lane t - t0 by a shuffle; the
-// K <= 5 low digits are per lane.  Lanes stay converged (shuffles); a lane
-// whose remaining terms are all below half an ulp of its sum idles, and the
-// warp leaves the dimension when all have.
+// The value of dimension D for this lane's point (bits of the double).
+template <u32 ADD>
+__device__ __forceinline__ u64 dim_value(const HDim &D, const u32 *Cj, const u64 *Yj, const u32 *Tj, u32 base,
+                                         u32 itrue, bool active, u32 lane)
+{
+    const u32 h0 = hdiv(D.fdK_M, base);
+    const u32 hi = hdiv(D.fdK_M, itrue);
+    const u32 sel = (hi - h0) * 16;  // 0 or 16: which half of the packed word
+    u32 dl[5];                        // low digits (zero beyond K)
+    {
+        u32 x = itrue - hi * D.bK;    // < b^K < 32 b
+#pragma unroll
+        for (int k = 0; k < 5; k++) {
+            const u32 q = ndiv(D.m32, x);
+            dl[k] = x - q * D.b;
+            x = q;
+        }
+    }
+    bool done = !active;
+    dsum::Sum vi = dsum::unpack(0);  // ADD_INT: the running sum, unpacked
+    double vd = 0.0;                 // ADD_FP64: the running sum
+    for (u32 t0 = 0; t0 < D.tmax; t0 += 32) {
+        if (__all_sync(0xffffffffu, done)) break;
+        u32 packed = 0;
+        if (t0 + lane < D.tmax)
+            packed = high_part(D, Cj, h0, t0 + lane) | (high_part(D, Cj, h0 + 1, t0 + lane) << 16);
+        const u32 tend = min(D.tmax, t0 + 32);
+        for (u32 t = t0; t < tend; t++) {
+            if (__all_sync(0xffffffffu, done)) break;
+            const u32 hp = (__shfl_sync(0xffffffffu, packed, t - t0) >> sel) & 0xFFFFu;
+            if (done) continue;
+            // every remaining term is below 2^(tail - 1022); once that is at most half an ulp of v
+            // (2^(E - 1076)), RN(v + term) = v for the rest of the digits
+            const u32 E = ADD == ADD_INT ? vi.E : (u32)(as_bits(vd) >> 52);
+            if (Tj[t] + 54 <= E) {
+                done = true;
+                continue;
+            }
+            // gdn_gen_natural.c:37-50: raw digit t of the point, mod b
+            u32 acc = hp;
+#pragma unroll
+            for (u32 k = 0; k < 5; k++)
+                if (k < D.Klo) acc += dl[k] * Cj[k * D.tmax + t];
+            const u64 y = Yj[t * D.b + dim_mod(D, acc)];
+            if (ADD == ADD_INT)
+                add_term_int(vi, y);
+            else
+                vd = __dadd_rn(vd, as_double(y));  // gdn_integer_to_float.c:37
+        }
+    }
+    return ADD == ADD_INT ? dsum::pack(vi) : as_bits(vd);
+}
+
 __global__ void __launch_bounds__(HT_THREADS) halton_gen_kernel(HPlanDev P)
 {
     extern __shared__ __align__(16) unsigned char sm[];
@@ -204,80 +297,22 @@ __global__ void __launch_bounds__(HT_THREADS) halton_gen_kernel(HPlanDev P)
     const u32 warp = threadIdx.x / 32, lane = threadIdx.x % 32;
     const u64 tiles_per_l = (P.n + 31) / 32;
     const u64 ntiles = P.r * tiles_per_l;
-    const bool early = !(*P.flags & 1u);
     for (u64 tt = blockIdx.x; tt < ntiles; tt += gridDim.x) {
         const u64 l = tt / tiles_per_l, i0 = (tt % tiles_per_l) * 32;
         const bool active = i0 + lane < P.n;  // lanes past the last point compute nothing
         const u32 base = (u32)(P.n_start + i0);
         const u32 itrue = active ? base + lane : base;  // < 2^32 (checked at plan creation)
         const u32 *Cl = P.C + l * P.c_per_l;
-        const u32 *Pl = P.perm + l * P.p_per_l;
-        const u32 *Sl = P.shift + l * P.s_per_l;
+        const u64 *Yl = P.Y + l * P.y_per_l;
+        const u32 *Tl = P.tail + l * P.s_per_l;
         for (u32 oi = P.wstart[warp]; oi < P.wstart[warp + 1]; oi++) {
             const u32 j = P.order[oi];
             const HDim D = P.dims[j];
-            const u32 *Cj = Cl + D.c_off;
-            const u32 *Pj = Pl + D.p_off;
-            const u32 *Sj = Sl + D.s_off;
-            const u64 *Rj = P.recip + D.s_off;
-            const u32 *Tj = P.tail + D.s_off;
-            const u32 h0 = hdiv(D.fdK_M, base);
-            const u32 hi = hdiv(D.fdK_M, itrue);
-            const u32 sel = (hi - h0) * 16;  // 0 or 16: which half of the packed word
-            u32 dl[5];                        // low digits (zero beyond K)
-            {
-                u32 x = itrue - hi * D.bK;
-#pragma unroll
-                for (int k = 0; k < 5; k++) {
-                    const u32 q = hdiv(D.fd_M, x);
-                    dl[k] = x - q * D.b;
-                    x = q;
-                }
-            }
-            bool done = !active;
-            dsum::Sum v = dsum::unpack(0);  // the running sum of gdn_integer_to_float, unpacked
-            for (u32 t0 = 0; t0 < D.tmax; t0 += 32) {
-                if (__all_sync(0xffffffffu, done)) break;
-                u32 packed = 0;
-                if (t0 + lane < D.tmax)
-                    packed = high_part(D, Cj, h0, t0 + lane) | (high_part(D, Cj, h0 + 1, t0 + lane) << 16);
-                const u32 tend = min(D.tmax, t0 + 32);
-                for (u32 t = t0; t < tend; t++) {
-                    if (__all_sync(0xffffffffu, done)) break;
-                    const u32 hp = (__shfl_sync(0xffffffffu, packed, t - t0) >> sel) & 0xFFFFu;
-                    if (done) continue;
-                    // Every later term is at most RN(recip_t*(b-1)) (recip_t only shrinks); once that
-                    // lies below half an ulp of v (exponent at most exp(v) - 54), RN(v + term) = v for
-                    // the remaining digits.
-                    if (early && v.M && Tj[t] + 54 <= v.E) {
-                        done = true;
-                        continue;
-                    }
-                    // gdn_gen_natural.c:37-50: digit t of the point, mod b
-                    u32 acc = hp;
-#pragma unroll
-                    for (u32 k = 0; k < 5; k++)
-                        if (k < D.Klo) acc += dl[k] * Cj[k * D.tmax + t];
-                    const u32 xd = hmod(D.fd_M, D.b, acc);
-                    const u32 pv = P.has_perm ? Pj[t * D.b + xd] : xd;  // gdn_digital_permutation.c:36-39
-                    u32 sv = pv;
-                    if (P.has_shift) {                                 // gdn_digital_shift.c:37-39
-                        const u64 sum = (u64)pv + Sj[t];
-                        if (sum < 2ull * D.b)
-                            sv = (u32)sum >= D.b ? (u32)sum - D.b : (u32)sum;
-                        else
-                            sv = sum < (1ull << 32) ? hmod(D.fd_M, D.b, (u32)sum) : (u32)(sum % D.b);
-                    }
-                    if (sv) {                                          // gdn_integer_to_float.c:35-38
-                        const u64 rb = Rj[t];
-                        const u32 er = (u32)(rb >> 52);
-                        if (!((v.M >> 52) && sv < 2048 && er - 1u < 2035u &&
-                              dsum::add_term_fast(v, (rb & dsum::FRAC) | dsum::HIDDEN, er, sv)))
-                            v = dsum::unpack(halton_step_slow(dsum::pack(v), rb, sv));
-                    }
-                }
-            }
-            tile[lane * P.d + j] = as_double(dsum::pack(v));
+            const u64 vb = D.add == ADD_INT
+                               ? dim_value<ADD_INT>(D, Cl + D.c_off, Yl + D.y_off, Tl + D.s_off, base, itrue, active, lane)
+                               : dim_value<ADD_FP64>(D, Cl + D.c_off, Yl + D.y_off, Tl + D.s_off, base, itrue, active,
+                                                     lane);
+            tile[lane * P.d + j] = as_double(vb);
         }
         __syncthreads();
         // 32 contiguous rows of the output
@@ -295,14 +330,33 @@ u64 ceil_digits(u64 n_last, u64 b)
     return k;
 }
 
+// The share of the terms (by count) whose adds go to the FP64 unit; the
+// other dimensions add in integer arithmetic.  Dimensions are taken in order
+// of decreasing tmax for the FP64 side.
+void assign_adds(std::vector<HDim> &hd, double share)
+{
+    u64 total = 0;
+    for (const HDim &h : hd) total += h.tmax;
+    std::vector<u32> idx(hd.size());
+    for (u32 j = 0; j < hd.size(); j++) idx[j] = j;
+    std::stable_sort(idx.begin(), idx.end(), [&](u32 a, u32 b) { return hd[a].tmax > hd[b].tmax; });
+    u64 acc = 0;
+    for (u32 j : idx) {
+        const bool fp = (double)acc + hd[j].tmax / 2.0 < share * (double)total;
+        hd[j].add = fp ? ADD_FP64 : ADD_INT;
+        if (fp) acc += hd[j].tmax;
+    }
+}
+
 }  // namespace
 
 struct qmc_halton_plan {
     HPlanDev P{};
-    void *d_dims = nullptr, *d_C = nullptr, *d_perm = nullptr, *d_shift = nullptr, *d_recip = nullptr;
-    void *d_order = nullptr, *d_wstart = nullptr, *d_prep = nullptr, *d_tail = nullptr, *d_flags = nullptr;
+    std::vector<HDim> hd;
+    void *d_dims = nullptr, *d_C = nullptr, *d_Y = nullptr, *d_recip = nullptr, *d_tail = nullptr;
+    void *d_order = nullptr, *d_wstart = nullptr, *d_prep = nullptr;
     std::vector<PrepDim> prep;
-    u64 total_c = 0, total_p = 0, total_s = 0;
+    u64 total_c = 0, rows = 0;
     size_t smem = 0;
     bool prepared = false;
 };
@@ -322,8 +376,9 @@ int qmc_halton_plan_create(uint64_t r, uint64_t n, uint64_t n_start, uint64_t d,
     const bool has_lms = dims[0].S != nullptr, has_perm = dims[0].perms != nullptr,
                has_shift = dims[0].shifts != nullptr;
     qmc_halton_plan *p = new qmc_halton_plan();
-    std::vector<HDim> hd(d);
-    u64 c_off = 0, p_off = 0, s_off = 0;
+    std::vector<HDim> &hd = p->hd;
+    hd.resize(d);
+    u64 c_off = 0, y_off = 0, s_off = 0;
     for (u64 j = 0; j < d; j++) {
         const qmc_gdn_dim &q = dims[j];
         const char *bad = nullptr;
@@ -340,31 +395,36 @@ int qmc_halton_plan_create(uint64_t r, uint64_t n, uint64_t n_start, uint64_t d,
             return q.b < 2 ? QMC_ERR_DOMAIN : QMC_ERR_ARG;
         }
         HDim &h = hd[j];
+        h = HDim{};
         h.b = (u32)q.b;
         h.tmax = (u32)q.tmax;
         h.mmax = (u32)q.mmax;
-        h.c_off = c_off;
-        h.p_off = p_off;
-        h.s_off = s_off;
-        h.fd_M = fastdiv32_make((u32)q.b).M;
         h.K = 1;
-        h.bK = (u32)q.b;
+        h.bK = h.b;
         while (h.bK < 32) {
-            h.bK *= (u32)q.b;
+            h.bK *= h.b;
             h.K++;
         }
+        h.Klo = std::min<u32>(h.K, h.mmax);
+        h.m32 = (u32)((1ull << 32) / h.b + 1);
+        // digit sums stay below (mmax + 6) * b^2; the 32-bit division needs them below 2^32 / b
+        h.wide = (u64)(h.mmax + 6) * h.b * h.b * h.b >= (1ull << 32);
+        h.fd_M = fastdiv32_make(h.b).M;
         h.fdK_M = fastdiv32_make(h.bK).M;
-        h.Klo = std::min<u32>(h.K, (u32)q.mmax);
+        h.c_off = c_off;
+        h.y_off = y_off;
+        h.s_off = s_off;
         c_off += q.mmax * q.tmax;
-        p_off += has_perm ? q.tmax * q.b : 0;
+        y_off += q.tmax * q.b;
         s_off += q.tmax;
         p->prep.push_back(PrepDim{q.b, q.tmax, q.mmax, (const u64 *)q.S, (const u64 *)q.C, (const u64 *)q.perms,
                                   (const u64 *)q.shifts});
     }
+    assign_adds(hd, 0.5);
     // longest-first assignment of dimensions to the warps of a CTA
     std::vector<u32> idx(d);
     for (u32 j = 0; j < d; j++) idx[j] = j;
-    auto cost = [&](u32 j) { return (double)hd[j].tmax * (hd[j].mmax * 2.0 + 40.0); };
+    auto cost = [&](u32 j) { return (double)hd[j].tmax * 40.0 + (double)hd[j].mmax * 20.0; };
     std::sort(idx.begin(), idx.end(), [&](u32 a, u32 b) { return cost(a) > cost(b); });
     std::vector<std::vector<u32>> per(HT_WARPS);
     std::vector<double> load(HT_WARPS, 0.0);
@@ -386,7 +446,7 @@ int qmc_halton_plan_create(uint64_t r, uint64_t n, uint64_t n_start, uint64_t d,
     p->P.n_start = n_start;
     p->P.d = d;
     p->P.c_per_l = c_off;
-    p->P.p_per_l = p_off;
+    p->P.y_per_l = y_off;
     p->P.s_per_l = s_off;
     p->P.has_lms = has_lms;
     p->P.has_perm = has_perm;
@@ -394,8 +454,7 @@ int qmc_halton_plan_create(uint64_t r, uint64_t n, uint64_t n_start, uint64_t d,
     p->P.x = x;
     p->P.err = qmcgb::device_error_ptr();
     p->total_c = r * c_off;
-    p->total_p = r * p_off;
-    p->total_s = has_shift ? r * s_off : 0;
+    p->rows = r * s_off;
     p->smem = smem;
     int rc = 0;
     auto alloc = [&](void **dst, size_t bytes) {
@@ -403,14 +462,12 @@ int qmc_halton_plan_create(uint64_t r, uint64_t n, uint64_t n_start, uint64_t d,
     };
     alloc(&p->d_dims, d * sizeof(HDim));
     alloc(&p->d_C, p->total_c * sizeof(u32));
-    alloc(&p->d_perm, p->total_p * sizeof(u32));
-    alloc(&p->d_shift, p->total_s * sizeof(u32));
+    alloc(&p->d_Y, r * y_off * sizeof(u64));
     alloc(&p->d_recip, s_off * sizeof(u64));
+    alloc(&p->d_tail, r * s_off * sizeof(u32));
     alloc(&p->d_order, d * sizeof(u16));
     alloc(&p->d_wstart, (HT_WARPS + 1) * sizeof(u32));
     alloc(&p->d_prep, d * sizeof(PrepDim));
-    alloc(&p->d_tail, s_off * sizeof(u32));
-    alloc(&p->d_flags, sizeof(unsigned));
     if (!rc) rc = qmcgb::cuda_status(cudaMemcpy(p->d_dims, hd.data(), d * sizeof(HDim), cudaMemcpyHostToDevice), "copy");
     if (!rc) rc = qmcgb::cuda_status(cudaMemcpy(p->d_order, order.data(), d * sizeof(u16), cudaMemcpyHostToDevice), "copy");
     if (!rc)
@@ -424,13 +481,11 @@ int qmc_halton_plan_create(uint64_t r, uint64_t n, uint64_t n_start, uint64_t d,
                                                      (int)smem), "cudaFuncSetAttribute");
     p->P.dims = (const HDim *)p->d_dims;
     p->P.C = (const u32 *)p->d_C;
-    p->P.perm = (const u32 *)p->d_perm;
-    p->P.shift = (const u32 *)p->d_shift;
+    p->P.Y = (const u64 *)p->d_Y;
     p->P.recip = (const u64 *)p->d_recip;
+    p->P.tail = (const u32 *)p->d_tail;
     p->P.order = (const u16 *)p->d_order;
     p->P.wstart = (const u32 *)p->d_wstart;
-    p->P.tail = (const u32 *)p->d_tail;
-    p->P.flags = (const unsigned *)p->d_flags;
     if (rc) {
         qmc_halton_plan_destroy(p);
         return rc;
@@ -443,16 +498,17 @@ int qmc_halton_plan_prepare(qmc_halton_plan *p, qmc_stream_t s)
 {
     QMC_REQUIRE(p, "null plan");
     cudaStream_t st = QMC_STREAM(s);
-    const u64 total = p->total_c + p->total_p + p->total_s;
-    if (int rc = qmcgb::cuda_status(cudaMemsetAsync(p->d_flags, 0, sizeof(unsigned), st), "cudaMemsetAsync"))
-        return rc;
-    halton_prep_kernel<<<qmcgb::grid_for(total, 256, (unsigned)qmcgb::sm_count() * 16), 256, 0, st>>>(
-        p->P, (const PrepDim *)p->d_prep, p->total_c, p->total_p, p->total_s, (u32 *)p->d_C, (u32 *)p->d_perm,
-        (u32 *)p->d_shift, (unsigned *)p->d_flags);
-    if (int rc = qmcgb::launch_status("halton_prep_kernel")) return rc;
-    halton_recip_kernel<<<qmcgb::grid_for(p->P.d, 128, 1024), 128, 0, st>>>(p->P, (u64 *)p->d_recip,
-                                                                           (u32 *)p->d_tail);
+    const unsigned cap = (unsigned)qmcgb::sm_count() * 16;
+    halton_lms_kernel<<<qmcgb::grid_for(p->total_c, 256, cap), 256, 0, st>>>(p->P, (const PrepDim *)p->d_prep,
+                                                                            p->total_c, (u32 *)p->d_C);
+    if (int rc = qmcgb::launch_status("halton_lms_kernel")) return rc;
+    halton_recip_kernel<<<qmcgb::grid_for(p->P.d, 128, 1024), 128, 0, st>>>(p->P, (u64 *)p->d_recip);
     if (int rc = qmcgb::launch_status("halton_recip_kernel")) return rc;
+    halton_terms_kernel<<<qmcgb::grid_for(p->rows * 32, 256, cap), 256, 0, st>>>(
+        p->P, (const PrepDim *)p->d_prep, p->rows, (u64 *)p->d_Y, (u32 *)p->d_tail);
+    if (int rc = qmcgb::launch_status("halton_terms_kernel")) return rc;
+    halton_tail_kernel<<<qmcgb::grid_for(p->P.r * p->P.d, 128, cap), 128, 0, st>>>(p->P, (u32 *)p->d_tail);
+    if (int rc = qmcgb::launch_status("halton_tail_kernel")) return rc;
     p->prepared = true;
     return QMC_OK;
 }
@@ -466,11 +522,18 @@ int qmc_halton_plan_run(qmc_halton_plan *p, qmc_stream_t s)
     return qmcgb::launch_status("halton_gen_kernel");
 }
 
+int qmc_halton_plan_set_fp64_share(qmc_halton_plan *p, double share)
+{
+    QMC_REQUIRE(p && share >= 0.0 && share <= 1.0, "null plan or share outside [0, 1]");
+    assign_adds(p->hd, share);
+    return qmcgb::cuda_status(cudaMemcpy(p->d_dims, p->hd.data(), p->hd.size() * sizeof(HDim), cudaMemcpyHostToDevice),
+                              "copy");
+}
+
 int qmc_halton_plan_destroy(qmc_halton_plan *p)
 {
     if (!p) return QMC_OK;
-    for (void *q : {p->d_dims, p->d_C, p->d_perm, p->d_shift, p->d_recip, p->d_order, p->d_wstart, p->d_prep,
-                    p->d_tail, p->d_flags})
+    for (void *q : {p->d_dims, p->d_C, p->d_Y, p->d_recip, p->d_tail, p->d_order, p->d_wstart, p->d_prep})
         if (q) cudaFree(q);
     delete p;
     return QMC_OK;

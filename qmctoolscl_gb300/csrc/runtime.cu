@@ -76,7 +76,7 @@ int qmc_device_error_check(qmc_stream_t s)
         qmcgb::device_error_reset(st);
         qmcgb::set_error("device error word %u:%s%s%s%s", h, (h & 1u) ? " a table index outside its array;" : "",
                          (h & 2u) ? " a base below 2;" : "", (h & 4u) ? " a tensor-core completion wait ran out;" : "",
-                         (h & 8u) ? " a fused generalized-net input entry at or above 2^32;" : "");
+                         (h & 8u) ? " a fused generalized-net matrix entry at or above 2^32;" : "");
         return QMC_ERR_DEVICE;
     }
     return QMC_OK;

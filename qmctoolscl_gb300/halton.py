@@ -46,8 +46,9 @@ def _lib():
         L.qmc_halton_plan_prepare.argtypes = [_P, _P]
         L.qmc_halton_plan_run.argtypes = [_P, _P]
         L.qmc_halton_plan_destroy.argtypes = [_P]
+        L.qmc_halton_plan_set_fp64_share.argtypes = [_P, _ct.c_double]
         for fn in ("qmc_halton_plan_create", "qmc_halton_plan_prepare", "qmc_halton_plan_run",
-                   "qmc_halton_plan_destroy"):
+                   "qmc_halton_plan_destroy", "qmc_halton_plan_set_fp64_share"):
             getattr(L, fn).restype = _ct.c_int
         L._halton_bound = True
     return L
@@ -125,6 +126,11 @@ class HaltonPlan:
     def run(self, stream=None):
         s = stream if stream is not None else _torch().cuda.current_stream()
         _ffi.check(_lib().qmc_halton_plan_run(self._h, s.cuda_stream), "halton_plan_run")
+
+    def set_fp64_share(self, share):
+        """Share of the digit adds run on the FP64 unit (the rest in integer
+        arithmetic); the results are the same bits either way."""
+        _ffi.check(_lib().qmc_halton_plan_set_fp64_share(self._h, float(share)), "halton_plan_set_fp64_share")
 
     def close(self):
         if getattr(self, "_h", None):

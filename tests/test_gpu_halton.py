@@ -164,10 +164,47 @@ def test_halton_matches_plain_drop_in_chain():
     assert same_bits(run_fused(r, n, n_start, dims), plain)
 
 
-def test_halton_entry_above_32_bits_is_reported():
+def test_halton_wide_shift_and_permutation_values():
+    """Shift and permutation entries far above b (64-bit wrapping sums in the
+    reference) give the same bits."""
     rng = np.random.Generator(np.random.SFC64(1))
-    dims = make_dims(rng, 1, [3], 9)
-    dims[0]["shifts"] = dims[0]["shifts"].copy()
-    dims[0]["shifts"][0, 0, 0] = U(1 << 40)
+    r, n = 2, 100
+    dims = make_dims(rng, r, [3, 7, 113], n - 1)
+    for dm in dims:
+        dm["shifts"] = dm["shifts"] + q.random_tbit_uint64s(rng, 64, dm["shifts"].shape)
+        dm["perms"] = dm["perms"] + (q.random_tbit_uint64s(rng, 40, dm["perms"].shape) // U(dm["b"])) * U(dm["b"])
+    assert same_bits(run_fused(r, n, 0, dims), oracle_chain(r, n, 0, dims))
+
+
+@pytest.mark.parametrize("share", [0.0, 0.3, 1.0])
+def test_halton_fp64_share_same_bits(share):
+    """Any split of the adds between the FP64 unit and integer arithmetic
+    gives the same bits."""
+    import torch
+    rng = np.random.Generator(np.random.SFC64(21))
+    r, n, n_start = 2, 2000, 77
+    dims = make_dims(rng, r, PRIMES[:40], n_start + n - 1)
+    want = oracle_chain(r, n, n_start, dims)
+    dev = lambda a: torch.from_numpy(np.ascontiguousarray(a).reshape(-1).view(np.int64)).cuda()  # noqa: E731
+    ddims = [dict(b=dm["b"], tmax=dm["tmax"], mmax=dm["mmax"], C=dev(dm["C"]), S=dev(dm["S"]), perms=dev(dm["perms"]),
+                  shifts=dev(dm["shifts"])) for dm in dims]
+    x = torch.empty(r * n * len(dims), dtype=torch.float64, device="cuda")
+    plan = halton.HaltonPlan(r, n, n_start, ddims, x)
+    plan.set_fp64_share(share)
+    plan.prepare()
+    plan.run()
+    assert same_bits(x.cpu().numpy().reshape(r, n, -1), want)
+    # a second run of the same plan (tables reused)
+    x.fill_(0)
+    plan.run()
+    assert same_bits(x.cpu().numpy().reshape(r, n, -1), want)
+
+
+def test_halton_matrix_entry_above_32_bits_is_reported():
+    """Without a linear matrix scramble, generating-matrix entries must stay
+    below 2^32 (the kernel reduces them to 32-bit words)."""
+    dims = make_dims(None, 1, [3], 9, lms=False, perm=False, shift=False)
+    dims[0]["C"] = dims[0]["C"].copy()
+    dims[0]["C"][0, 0, 0, 0] = U(1 << 40)
     with pytest.raises(q._ffi.QmcError, match="2\\^32"):
         run_fused(1, 10, 0, dims)
