@@ -53,6 +53,7 @@ constexpr int HT_THREADS = 256;
 constexpr int HT_WARPS = HT_THREADS / 32;
 constexpr u32 HT_MAX_DIMS = 1024;
 constexpr u32 HT_MAX_B = 2048;
+constexpr u32 HT_GROUP = 4;  // output digits whose table reads are issued together
 
 enum : u32 { ADD_FP64 = 0, ADD_INT = 1 };
 
@@ -64,12 +65,12 @@ struct HDim {
     u32 m32;       // floor(2^32 / b) + 1: x / b = umulhi(x, m32) for x < 2^32 / b
     u32 wide;      // 1 when digit sums can reach 2^32 / b: 64-bit remainders instead
     u32 add;       // ADD_FP64 or ADD_INT
-    u32 pad;
+    u32 tpad;      // tmax rounded up to a multiple of HT_GROUP: term rows past tmax hold +0
     u64 fd_M;      // direct-remainder constant for b (any 32-bit x)
     u64 fdK_M;     // the same for b^K
     u64 c_off;     // offset of this dimension's (mmax x tmax) block inside a randomisation's C block
-    u64 y_off;     // offset of its (tmax x b) term rows inside a randomisation's Y block
-    u64 s_off;     // offset of its tmax digits inside the recip / tail blocks
+    u64 y_off;     // offset of its (tpad x b) term rows inside a randomisation's Y block
+    u64 s_off;     // offset of its tpad digits inside the recip / tail blocks
 };
 
 struct HPlanDev {
@@ -92,8 +93,13 @@ struct PrepDim {
     const u64 *S, *C, *perms, *shifts;  // caller's per-dimension arrays
 };
 
-// floor(x / b) and x mod b for any x < 2^32, b >= 2, from M = floor((2^64-1)/b) + 1
-__device__ __forceinline__ u32 hdiv(u64 M, u32 x) { return (u32)__umul64hi(M, (u64)x); }
+// floor(x / b) and x mod b for any x < 2^32, b >= 2, from M = floor((2^64-1)/b) + 1;
+// hdiv is the high word of the 64x32-bit product M*x / 2^64
+__device__ __forceinline__ u32 hdiv(u64 M, u32 x)
+{
+    const u64 lo = (u64)(u32)M * x;
+    return (u32)(((M >> 32) * x + (lo >> 32)) >> 32);
+}
 __device__ __forceinline__ u32 hmod(u64 M, u32 b, u32 x) { return (u32)__umul64hi(M * (u64)x, (u64)b); }
 
 // the same for x < 2^32 / b, with m32 = floor(2^32/b) + 1: x*m32/2^32 exceeds
@@ -158,7 +164,7 @@ __global__ void halton_recip_kernel(HPlanDev P, u64 *recip)
         const HDim &D = P.dims[j];
         const double bd = (double)D.b;
         double rc = __ddiv_rn(1.0, bd);
-        for (u32 t = 0; t < D.tmax; t++) {
+        for (u32 t = 0; t < D.tpad; t++) {
             recip[D.s_off + t] = as_bits(rc);
             rc = __ddiv_rn(rc, bd);
         }
@@ -180,9 +186,14 @@ __global__ void halton_terms_kernel(HPlanDev P, const PrepDim *pd, u64 rows, u64
         const HDim &D = P.dims[j];
         const PrepDim &Q = pd[j];
         const u64 t = off - D.s_off;
+        u64 *yrow = Y + l * P.y_per_l + D.y_off + t * D.b;
+        if (t >= D.tmax) {  // padding row: +0 terms, no tail
+            for (u32 g = lane; g < D.b; g += 32) yrow[g] = 0;
+            if (lane == 0) tail[l * P.s_per_l + off] = 0;
+            continue;
+        }
         const double rc = as_double(P.recip[D.s_off + t]);
         const u64 sh = P.has_shift ? Q.shifts[l * D.tmax + t] : 0;
-        u64 *yrow = Y + l * P.y_per_l + D.y_off + t * D.b;
         u64 mx = 0;
         for (u32 g = lane; g < D.b; g += 32) {
             const u64 pv = P.has_perm ? Q.perms[(l * D.tmax + t) * D.b + g] : g;
@@ -204,7 +215,7 @@ __global__ void halton_tail_kernel(HPlanDev P, u32 *tail)
         const HDim &D = P.dims[j];
         u32 *tl = tail + l * P.s_per_l + D.s_off;
         u32 m = 0;
-        for (u32 t = D.tmax; t-- > 0;) {
+        for (u32 t = D.tpad; t-- > 0;) {
             m = max(m, tl[t]);
             tl[t] = m;
         }
@@ -237,19 +248,29 @@ __device__ __forceinline__ u32 high_part(const HDim &D, const u32 *Cj, u32 h, u3
     return dim_mod(D, acc);
 }
 
-// The value of dimension D for this lane's point (bits of the double).
-template <u32 ADD>
+// The value of dimension D for this lane's point (bits of the double), KL =
+// min(K, mmax) low digits per lane.
+//
+// Output digits go in chunks of 32: lane c holds, for digit t0 + c, the
+// high-digit sums of both hi values (packed), the low-digit matrix entries
+// C[k][t0 + c] (k < KL) and the tail exponent, and every lane takes its own
+// from lane t - t0 by shuffles.  Within a chunk, groups of HT_GROUP digits
+// compute their raw digits and issue their table reads (independent of v),
+// then add the terms in order.  The early stop is tested once per group: an
+// add after the exact stop point leaves v unchanged (the term is below half
+// an ulp), so the group's adds need no test; a stopped lane adds +0.
+template <u32 ADD, u32 KL>
 __device__ __forceinline__ u64 dim_value(const HDim &D, const u32 *Cj, const u64 *Yj, const u32 *Tj, u32 base,
                                          u32 itrue, bool active, u32 lane)
 {
     const u32 h0 = hdiv(D.fdK_M, base);
     const u32 hi = hdiv(D.fdK_M, itrue);
     const u32 sel = (hi - h0) * 16;  // 0 or 16: which half of the packed word
-    u32 dl[5];                        // low digits (zero beyond K)
+    u32 dl[KL];                       // low digits
     {
         u32 x = itrue - hi * D.bK;    // < b^K < 32 b
 #pragma unroll
-        for (int k = 0; k < 5; k++) {
+        for (u32 k = 0; k < KL; k++) {
             const u32 q = ndiv(D.m32, x);
             dl[k] = x - q * D.b;
             x = q;
@@ -258,36 +279,59 @@ __device__ __forceinline__ u64 dim_value(const HDim &D, const u32 *Cj, const u64
     bool done = !active;
     dsum::Sum vi = dsum::unpack(0);  // ADD_INT: the running sum, unpacked
     double vd = 0.0;                 // ADD_FP64: the running sum
-    for (u32 t0 = 0; t0 < D.tmax; t0 += 32) {
+    for (u32 t0 = 0; t0 < D.tpad; t0 += 32) {
         if (__all_sync(0xffffffffu, done)) break;
-        u32 packed = 0;
-        if (t0 + lane < D.tmax)
-            packed = high_part(D, Cj, h0, t0 + lane) | (high_part(D, Cj, h0 + 1, t0 + lane) << 16);
-        const u32 tend = min(D.tmax, t0 + 32);
-        for (u32 t = t0; t < tend; t++) {
-            if (__all_sync(0xffffffffu, done)) break;
-            const u32 hp = (__shfl_sync(0xffffffffu, packed, t - t0) >> sel) & 0xFFFFu;
-            if (done) continue;
+        const u32 tc = t0 + lane;
+        u32 packed = 0, tailc = 0, cl[KL];
+#pragma unroll
+        for (u32 k = 0; k < KL; k++) cl[k] = 0;
+        if (tc < D.tmax) {
+            packed = high_part(D, Cj, h0, tc) | (high_part(D, Cj, h0 + 1, tc) << 16);
+            tailc = Tj[tc];
+#pragma unroll
+            for (u32 k = 0; k < KL; k++) cl[k] = Cj[k * D.tmax + tc];
+        }
+        const u32 tend = min(D.tpad, t0 + 32);
+        for (u32 t = t0; t < tend; t += HT_GROUP) {
             // every remaining term is below 2^(tail - 1022); once that is at most half an ulp of v
             // (2^(E - 1076)), RN(v + term) = v for the rest of the digits
             const u32 E = ADD == ADD_INT ? vi.E : (u32)(as_bits(vd) >> 52);
-            if (Tj[t] + 54 <= E) {
-                done = true;
-                continue;
-            }
-            // gdn_gen_natural.c:37-50: raw digit t of the point, mod b
-            u32 acc = hp;
+            const u32 tl = __shfl_sync(0xffffffffu, tailc, t - t0);  // every lane takes part in the shuffle
+            done = done || tl + 54 <= E;
+            if (__all_sync(0xffffffffu, done)) break;
+            u64 y[HT_GROUP];
 #pragma unroll
-            for (u32 k = 0; k < 5; k++)
-                if (k < D.Klo) acc += dl[k] * Cj[k * D.tmax + t];
-            const u64 y = Yj[t * D.b + dim_mod(D, acc)];
-            if (ADD == ADD_INT)
-                add_term_int(vi, y);
-            else
-                vd = __dadd_rn(vd, as_double(y));  // gdn_integer_to_float.c:37
+            for (u32 u = 0; u < HT_GROUP; u++) {
+                const u32 src = t + u - t0;
+                // gdn_gen_natural.c:37-50: raw digit t + u of the point, mod b (rows past tmax: +0)
+                u32 acc = (__shfl_sync(0xffffffffu, packed, src) >> sel) & 0xFFFFu;
+#pragma unroll
+                for (u32 k = 0; k < KL; k++) acc += dl[k] * __shfl_sync(0xffffffffu, cl[k], src);
+                y[u] = done ? 0ull : Yj[(t + u) * D.b + dim_mod(D, acc)];
+            }
+#pragma unroll
+            for (u32 u = 0; u < HT_GROUP; u++) {
+                if (ADD == ADD_INT)
+                    add_term_int(vi, y[u]);
+                else
+                    vd = __dadd_rn(vd, as_double(y[u]));  // gdn_integer_to_float.c:37
+            }
         }
     }
     return ADD == ADD_INT ? dsum::pack(vi) : as_bits(vd);
+}
+
+template <u32 ADD>
+__device__ __forceinline__ u64 dim_value_k(const HDim &D, const u32 *Cj, const u64 *Yj, const u32 *Tj, u32 base,
+                                           u32 itrue, bool active, u32 lane)
+{
+    switch (D.Klo) {
+    case 1: return dim_value<ADD, 1>(D, Cj, Yj, Tj, base, itrue, active, lane);
+    case 2: return dim_value<ADD, 2>(D, Cj, Yj, Tj, base, itrue, active, lane);
+    case 3: return dim_value<ADD, 3>(D, Cj, Yj, Tj, base, itrue, active, lane);
+    case 4: return dim_value<ADD, 4>(D, Cj, Yj, Tj, base, itrue, active, lane);
+    default: return dim_value<ADD, 5>(D, Cj, Yj, Tj, base, itrue, active, lane);
+    }
 }
 
 __global__ void __launch_bounds__(HT_THREADS) halton_gen_kernel(HPlanDev P)
@@ -308,10 +352,10 @@ __global__ void __launch_bounds__(HT_THREADS) halton_gen_kernel(HPlanDev P)
         for (u32 oi = P.wstart[warp]; oi < P.wstart[warp + 1]; oi++) {
             const u32 j = P.order[oi];
             const HDim D = P.dims[j];
-            const u64 vb = D.add == ADD_INT
-                               ? dim_value<ADD_INT>(D, Cl + D.c_off, Yl + D.y_off, Tl + D.s_off, base, itrue, active, lane)
-                               : dim_value<ADD_FP64>(D, Cl + D.c_off, Yl + D.y_off, Tl + D.s_off, base, itrue, active,
-                                                     lane);
+            const u64 vb =
+                D.add == ADD_INT
+                    ? dim_value_k<ADD_INT>(D, Cl + D.c_off, Yl + D.y_off, Tl + D.s_off, base, itrue, active, lane)
+                    : dim_value_k<ADD_FP64>(D, Cl + D.c_off, Yl + D.y_off, Tl + D.s_off, base, itrue, active, lane);
             tile[lane * P.d + j] = as_double(vb);
         }
         __syncthreads();
@@ -411,12 +455,13 @@ int qmc_halton_plan_create(uint64_t r, uint64_t n, uint64_t n_start, uint64_t d,
         h.wide = (u64)(h.mmax + 6) * h.b * h.b * h.b >= (1ull << 32);
         h.fd_M = fastdiv32_make(h.b).M;
         h.fdK_M = fastdiv32_make(h.bK).M;
+        h.tpad = (h.tmax + HT_GROUP - 1) / HT_GROUP * HT_GROUP;
         h.c_off = c_off;
         h.y_off = y_off;
         h.s_off = s_off;
         c_off += q.mmax * q.tmax;
-        y_off += q.tmax * q.b;
-        s_off += q.tmax;
+        y_off += (u64)h.tpad * q.b;
+        s_off += h.tpad;
         p->prep.push_back(PrepDim{q.b, q.tmax, q.mmax, (const u64 *)q.S, (const u64 *)q.C, (const u64 *)q.perms,
                                   (const u64 *)q.shifts});
     }
