@@ -908,7 +908,9 @@ def run_halton(args):
                                    "(fused plan: prepare + generate)", "r": r, "n": n, "d": d,
                        "l2": "6.7 GB output per step >> 129 MB L2, no flush needed"},
             "roofline": dict(roofline(alg, ms_gen), kernel="halton_gen_kernel",
-                             note="generation kernel alone; integer-throughput bound, see profiles/"),
+                             traffic=profiled_traffic("halton_gen_kernel_r32_n2p18_d100.md"),
+                             note="generation kernel alone; bound by instruction issue (integer + FP64 adds), "
+                                  "not HBM"),
             "generate_only_ms": ms_gen,
             "fp64_share": {"chosen": best_share, "generate_ms_by_share": {str(k): v for k, v in sweep.items()}},
             "plain": {"ms_per_step": ms_plain, "points_per_s": pts / (ms_plain / 1e3), "launches_per_step": 5 * d,
