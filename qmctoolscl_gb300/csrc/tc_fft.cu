@@ -5,6 +5,7 @@
 // D FP32) through tcgen05.mma with the operand layout and descriptors of
 // tc_sm100.cuh; the tests compare it with an exact host product to pin the
 // descriptor encodings every tensor-core kernel here relies on.
+#include "fpconv.cuh"
 #include "tc_sm100.cuh"
 
 namespace {
@@ -127,7 +128,30 @@ constexpr u32 FT_GROUPS = FT_TILE / 16;
 constexpr u32 FT_KS = 192;             // K of the split product: 6 x 32 reals
 constexpr u32 FT_THREADS = 256;
 constexpr u32 TMEM_COLS = 128;         // three 32-column FP32 accumulators
+constexpr u32 FT_PAD = FT_TILE + FT_TILE / 16;  // shared-memory words per component, padded
 enum TcKind { TC_FFT = 0, TC_IFFT = 1, TC_WHT = 2 };
+
+// Shared-memory slot of tile element e: one padding word per 16, so that the
+// 32 groups a warp handles (16 consecutive elements apart in the first step)
+// fall in distinct banks.
+__device__ __forceinline__ u32 slot(u32 e) { return e + (e >> 4); }
+
+// FP64 <-> FP32 at every load and store, in integer arithmetic (fpconv.cuh);
+// the rare values outside its fast range go through the hardware conversion
+__device__ __noinline__ float f64_to_f32_hw(double x) { return __double2float_rn(x); }
+__device__ __noinline__ double f32_to_f64_hw(float x) { return (double)x; }
+
+__device__ __forceinline__ float to_f32(u64 b)
+{
+    u32 o;
+    return fpc::f64_to_f32_bits(b, o) ? __uint_as_float(o) : f64_to_f32_hw(__longlong_as_double((long long)b));
+}
+
+__device__ __forceinline__ void store_f64(double *p, float v)
+{
+    u64 o;
+    *p = fpc::f32_to_f64_bits(__float_as_uint(v), o) ? __longlong_as_double((long long)o) : f32_to_f64_hw(v);
+}
 
 struct TcPassArgs {
     u64 total;       // nvec * n values
@@ -177,10 +201,10 @@ __device__ __forceinline__ float step_matrix(u32 kk, u32 n)
 }
 
 // twiddle exp(sign * 2 pi i * t / 2^bits) in FP32 (t < 2^bits <= 2^24)
-__device__ __forceinline__ void twiddle(u64 t, u32 bits, float sign, float &wr, float &wi)
+__device__ __forceinline__ void twiddle(u32 t, u32 bits, float sign, float &wr, float &wi)
 {
     float s, c;
-    sincospif(ldexpf((float)t, 1 - (int)bits), &s, &c);
+    sincospif(__uint2float_rn(t) * __uint_as_float((128u - bits) << 23), &s, &c);  // t * 2^(1 - bits), exact
     wr = c;
     wi = sign * s;
 }
@@ -189,9 +213,9 @@ template <int KIND>
 __global__ void __launch_bounds__(FT_THREADS) tc_pass_kernel(TcPassArgs a, unsigned *err)
 {
     extern __shared__ __align__(128) unsigned char sm[];
-    float *sr = (float *)sm;                            // [FT_TILE] real parts
-    float *si = sr + FT_TILE;                           // [FT_TILE] imaginary parts
-    unsigned char *sA = (unsigned char *)(si + FT_TILE);  // [128 x FT_KS] bf16 operand A
+    float *sr = (float *)sm;                            // [FT_PAD] real parts (slot(e))
+    float *si = sr + FT_PAD;                            // [FT_PAD] imaginary parts
+    unsigned char *sA = (unsigned char *)(si + FT_PAD);   // [128 x FT_KS] bf16 operand A
     unsigned char *sB = sA + 128 * FT_KS * 2;           // [32 x FT_KS]  bf16 operand B
     __shared__ __align__(8) u64 bar;
     __shared__ u32 tmem_base;
@@ -235,12 +259,26 @@ __global__ void __launch_bounds__(FT_THREADS) tc_pass_kernel(TcPassArgs a, unsig
             const u64 v = tile / tiles_per_vec, rem = tile % tiles_per_vec;
             base = v * n + (rem / cchunks) * (1ull << a.k1) + (rem % cchunks) * ct;
         }
-        // load (zeros beyond the data)
-        for (u32 e = threadIdx.x; e < Q * ct; e += FT_THREADS) {
-            const u64 f = base + ((u64)(e / ct) << a.k0) + (e % ct);
-            const bool in = f < a.total;
-            sr[e] = in ? (float)a.xr[f] : 0.0f;
-            if (KIND != TC_WHT) si[e] = in ? (float)a.xi[f] : 0.0f;
+        // load (zeros beyond the data): eight elements' raw bits in flight per thread, then the
+        // conversions (whose rare out-of-line fallback would otherwise serialise the loads)
+        for (u32 e0 = threadIdx.x; e0 < Q * ct; e0 += 8 * FT_THREADS) {
+            u64 br[8], bi[8];
+#pragma unroll
+            for (u32 i = 0; i < 8; i++) {
+                const u32 e = e0 + i * FT_THREADS;
+                const u64 f = base + ((u64)(e / ct) << a.k0) + (e % ct);
+                const bool in = e < Q * ct && f < a.total;
+                br[i] = in ? (u64)__double_as_longlong(a.xr[f]) : 0ull;
+                bi[i] = (in && KIND != TC_WHT) ? (u64)__double_as_longlong(a.xi[f]) : 0ull;
+            }
+#pragma unroll
+            for (u32 i = 0; i < 8; i++) {
+                const u32 e = e0 + i * FT_THREADS;
+                if (e < Q * ct) {
+                    sr[slot(e)] = to_f32(br[i]);
+                    if (KIND != TC_WHT) si[slot(e)] = to_f32(bi[i]);
+                }
+            }
         }
         __syncthreads();
         // steps over the pass's bits: FFT/WHT low to high, inverse high to low
@@ -262,16 +300,16 @@ __global__ void __launch_bounds__(FT_THREADS) tc_pass_kernel(TcPassArgs a, unsig
                 for (u32 b = threadIdx.x; b < Q * ct / 2; b += FT_THREADS) {
                     const u32 cc = b % ct, pq = b / ct;
                     const u32 q1 = ((pq >> lo) << (lo + 1)) | (pq & ((1u << lo) - 1));
-                    const u32 e1 = q1 * ct + cc, e2 = e1 + (1u << lo) * ct;
+                    const u32 e1 = slot(q1 * ct + cc), e2 = slot(q1 * ct + cc + (1u << lo) * ct);
                     if (KIND == TC_WHT) {
                         const float x1 = sr[e1], x2 = sr[e2];
                         sr[e1] = x1 + x2;
                         sr[e2] = x1 - x2;
                         continue;
                     }
-                    const u64 f1 = base + ((u64)q1 << a.k0) + cc;
+                    const u32 f1 = (u32)base + (q1 << a.k0) + cc;  // only its low k bits are used
                     float wr, wi;
-                    twiddle(f1 & ((1ull << k) - 1), k + 1, tw_sign, wr, wi);
+                    twiddle(f1 & ((1u << k) - 1), k + 1, tw_sign, wr, wi);
                     const float ar = sr[e1], ai = si[e1], br = sr[e2], bi = si[e2];
                     if (KIND == TC_FFT) {
                         const float yr = br * wr - bi * wi, yi = br * wi + bi * wr;
@@ -287,37 +325,51 @@ __global__ void __launch_bounds__(FT_THREADS) tc_pass_kernel(TcPassArgs a, unsig
             }
             // radix-16 step through the tensor cores, two M-tiles of 128 groups
             for (u32 mt = 0; mt < FT_GROUPS / 128 && ok; mt++) {
-                // build A: thread t handles group 128*mt + t%128, members 8*(t/128) .. +7
+                // build A: thread t handles group 128*mt + t%128, members 8*(t/128) .. +7; the
+                // eight members' BF16 terms of one product sit side by side along K (one 16-byte
+                // row of a core matrix), so each (product, component) is a single 16-byte store
                 {
                     const u32 gi = 128 * mt + (threadIdx.x & 127), half = threadIdx.x >> 7;
                     const u32 cc = gi % ct, qq = gi / ct;
                     const u32 qlo = qq & ((1u << lo) - 1), qhi = qq >> lo;
                     const u32 row = threadIdx.x & 127;
+                    u32 pr[3][4], pim[3][4];  // [split][pair of members]: two BF16 per word
+#pragma unroll
                     for (u32 pp = 0; pp < 8; pp++) {
                         const u32 p = half * 8 + pp;
                         const u32 q = qlo | (p << lo) | (qhi << (lo + 4));
-                        const u32 e = q * ct + cc;
+                        const u32 e = slot(q * ct + cc);
                         float xr_ = sr[e], xi_ = (KIND == TC_WHT) ? 0.0f : si[e];
-                        if (KIND == TC_FFT) {  // pre-twiddle w^br(p)
-                            const u64 f = base + ((u64)q << a.k0) + cc;
-                            const u64 c = f & ((1ull << k) - 1);
+                        if (KIND == TC_FFT && k > 0) {  // pre-twiddle w^br(p) (w = 1 on the first step)
+                            const u32 c = ((u32)base + (q << a.k0) + cc) & ((1u << k) - 1);
                             float wr, wi;
-                            twiddle((c * brev4(p)) & ((1ull << (k + 4)) - 1), k + 4, -1.0f, wr, wi);
+                            twiddle((c * brev4(p)) & ((1u << (k + 4)) - 1), k + 4, -1.0f, wr, wi);
                             const float tr = xr_ * wr - xi_ * wi;
                             xi_ = xr_ * wi + xi_ * wr;
                             xr_ = tr;
                         }
-                        __nv_bfloat16 r1, r2, r3, i1, i2, i3;
-                        split3(xr_, r1, r2, r3);
-                        if (KIND != TC_WHT) split3(xi_, i1, i2, i3);
-                        for (u32 j = 0; j < 6; j++) {
-                            const u32 pa = prod_a(j);
-                            *(__nv_bfloat16 *)(sA + tc::kmajor_offset(row, j * KIN + p, KTOT)) =
-                                pa == 0 ? r1 : pa == 1 ? r2 : r3;
-                            if (KIND != TC_WHT)
-                                *(__nv_bfloat16 *)(sA + tc::kmajor_offset(row, j * KIN + 16 + p, KTOT)) =
-                                    pa == 0 ? i1 : pa == 1 ? i2 : i3;
+                        __nv_bfloat16 r[3], im[3];
+                        split3(xr_, r[0], r[1], r[2]);
+                        if (KIND != TC_WHT) split3(xi_, im[0], im[1], im[2]);
+                        const u32 sh = (pp & 1) * 16;
+#pragma unroll
+                        for (u32 z = 0; z < 3; z++) {
+                            const u32 rb = (u32)__bfloat16_as_ushort(r[z]) << sh;
+                            pr[z][pp >> 1] = (pp & 1) ? (pr[z][pp >> 1] | rb) : rb;
+                            if (KIND != TC_WHT) {
+                                const u32 ib = (u32)__bfloat16_as_ushort(im[z]) << sh;
+                                pim[z][pp >> 1] = (pp & 1) ? (pim[z][pp >> 1] | ib) : ib;
+                            }
                         }
+                    }
+#pragma unroll
+                    for (u32 j = 0; j < 6; j++) {
+                        const u32 pa = prod_a(j);
+                        *(uint4 *)(sA + tc::kmajor_offset(row, j * KIN + half * 8, KTOT)) =
+                            make_uint4(pr[pa][0], pr[pa][1], pr[pa][2], pr[pa][3]);
+                        if (KIND != TC_WHT)
+                            *(uint4 *)(sA + tc::kmajor_offset(row, j * KIN + 16 + half * 8, KTOT)) =
+                                make_uint4(pim[pa][0], pim[pa][1], pim[pa][2], pim[pa][3]);
                     }
                 }
                 tc::fence_smem_to_async();
@@ -358,7 +410,7 @@ __global__ void __launch_bounds__(FT_THREADS) tc_pass_kernel(TcPassArgs a, unsig
                             float y = __uint_as_float(v0[m]);
                             if (KIND != TC_WHT) y += __uint_as_float(v1[m]);
                             y += __uint_as_float(v2[m]);
-                            dst[q * ct + cc] = y;
+                            dst[slot(q * ct + cc)] = y;
                         }
                     }
                 }
@@ -372,11 +424,10 @@ __global__ void __launch_bounds__(FT_THREADS) tc_pass_kernel(TcPassArgs a, unsig
                     for (u32 pp = 0; pp < 8; pp++) {
                         const u32 p = half * 8 + pp;
                         const u32 q = qlo | (p << lo) | (qhi << (lo + 4));
-                        const u32 e = q * ct + cc;
-                        const u64 f = base + ((u64)q << a.k0) + cc;
-                        const u64 c = f & ((1ull << k) - 1);
+                        const u32 e = slot(q * ct + cc);
+                        const u32 c = ((u32)base + (q << a.k0) + cc) & ((1u << k) - 1);
                         float wr, wi;
-                        twiddle((c * brev4(p)) & ((1ull << (k + 4)) - 1), k + 4, 1.0f, wr, wi);
+                        twiddle((c * brev4(p)) & ((1u << (k + 4)) - 1), k + 4, 1.0f, wr, wi);
                         const float xr_ = sr[e], xi_ = si[e];
                         sr[e] = xr_ * wr - xi_ * wi;
                         si[e] = xr_ * wi + xi_ * wr;
@@ -391,8 +442,8 @@ __global__ void __launch_bounds__(FT_THREADS) tc_pass_kernel(TcPassArgs a, unsig
         for (u32 e = threadIdx.x; e < Q * ct; e += FT_THREADS) {
             const u64 f = base + ((u64)(e / ct) << a.k0) + (e % ct);
             if (f < a.total) {
-                a.xr[f] = (double)(sr[e] * a.scale);
-                if (KIND != TC_WHT) a.xi[f] = (double)(si[e] * a.scale);
+                store_f64(a.xr + f, sr[slot(e)] * a.scale);
+                if (KIND != TC_WHT) store_f64(a.xi + f, si[slot(e)] * a.scale);
             }
         }
         __syncthreads();
@@ -419,7 +470,7 @@ int run_tc(int kind, u64 d1, u64 d2, u64 n_half, double *xr, double *xi, cudaStr
     int np = 0;
     passes[np++] = {0, L < 12 ? L : 12};
     for (u32 k0 = 12; k0 < L; k0 += 8) passes[np++] = {k0, (k0 + 8 < L) ? k0 + 8 : L};
-    const size_t smem = FT_TILE * 8 + 128 * FT_KS * 2 + 32 * FT_KS * 2;
+    const size_t smem = FT_PAD * 8 + 128 * FT_KS * 2 + 32 * FT_KS * 2;
     const float scale = (float)(1.0 / sqrt((double)n));
     for (int pi = 0; pi < np; pi++) {
         const P p = (kind == TC_IFFT) ? passes[np - 1 - pi] : passes[pi];
