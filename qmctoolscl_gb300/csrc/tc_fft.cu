@@ -147,10 +147,10 @@ __device__ __forceinline__ float to_f32(u64 b)
     return fpc::f64_to_f32_bits(b, o) ? __uint_as_float(o) : f64_to_f32_hw(__longlong_as_double((long long)b));
 }
 
-__device__ __forceinline__ void store_f64(double *p, float v)
+__device__ __forceinline__ double to_f64(float v)
 {
     u64 o;
-    *p = fpc::f32_to_f64_bits(__float_as_uint(v), o) ? __longlong_as_double((long long)o) : f32_to_f64_hw(v);
+    return fpc::f32_to_f64_bits(__float_as_uint(v), o) ? __longlong_as_double((long long)o) : f32_to_f64_hw(v);
 }
 
 struct TcPassArgs {
@@ -165,6 +165,7 @@ struct TcPassArgs {
 
 __device__ __forceinline__ u32 brev4(u32 p) { return __brev(p) >> 28; }
 
+// x = a + b + c, each the RN BF16 of what is left (about 24 significant bits in all)
 __device__ __forceinline__ void split3(float x, __nv_bfloat16 &a, __nv_bfloat16 &b, __nv_bfloat16 &c)
 {
     a = __float2bfloat16_rn(x);
@@ -200,13 +201,37 @@ __device__ __forceinline__ float step_matrix(u32 kk, u32 n)
     return c;                          // Im(x) Re(F)
 }
 
-// twiddle exp(sign * 2 pi i * t / 2^bits) in FP32 (t < 2^bits <= 2^24)
-__device__ __forceinline__ void twiddle(u32 t, u32 bits, float sign, float &wr, float &wi)
+// Twiddle exp(sign * 2 pi i * t / 2^bits) in FP32, t < 2^bits, bits <= 32,
+// from a table of exp(-2 pi i r / 4096), r < 1024 (one quarter turn, filled
+// once per CTA with sincospif): the angle as a 32-bit fraction of a turn J
+// splits into the quarter J >> 30, the table index (J >> 20) mod 1024, and,
+// when bits > 12, a remainder below 2 pi / 4096 whose sine and cosine are
+// two-term series (the next terms are below 2^-40).
+__device__ __forceinline__ void twiddle(const float2 *tab, u32 t, u32 bits, float sign, float &wr, float &wi)
 {
-    float s, c;
-    sincospif(__uint2float_rn(t) * __uint_as_float((128u - bits) << 23), &s, &c);  // t * 2^(1 - bits), exact
+    const u32 J = t << (32 - bits);
+    const float2 e = tab[(J >> 20) & 1023u];  // (cos, -sin) of 2 pi r / 4096
+    float c = e.x, sn = e.y;
+    const u32 quarter = J >> 30;              // times (-i)^quarter
+    if (quarter & 1u) {
+        const float tmp = c;
+        c = sn;
+        sn = -tmp;
+    }
+    if (quarter & 2u) {
+        c = -c;
+        sn = -sn;
+    }
+    if (bits > 12) {
+        const float th = __uint2float_rn(J & 0xFFFFFu) * 1.4629180792671596e-09f;  // 2 pi / 2^32
+        const float th2 = th * th;
+        const float ct = fmaf(-0.5f, th2, 1.0f), st = th * fmaf(th2, -0.16666667f, 1.0f);
+        const float nc = c * ct + sn * st;  // (c + i sn) * (ct - i st)
+        sn = sn * ct - c * st;
+        c = nc;
+    }
     wr = c;
-    wi = sign * s;
+    wi = sign < 0.0f ? sn : -sn;
 }
 
 template <int KIND>
@@ -217,6 +242,7 @@ __global__ void __launch_bounds__(FT_THREADS) tc_pass_kernel(TcPassArgs a, unsig
     float *si = sr + FT_PAD;                            // [FT_PAD] imaginary parts
     unsigned char *sA = (unsigned char *)(si + FT_PAD);   // [128 x FT_KS] bf16 operand A
     unsigned char *sB = sA + 128 * FT_KS * 2;           // [32 x FT_KS]  bf16 operand B
+    float2 *tab = (float2 *)(sB + 32 * FT_KS * 2);      // [1024] exp(-2 pi i r / 4096)
     __shared__ __align__(8) u64 bar;
     __shared__ u32 tmem_base;
     const u32 warp = threadIdx.x / 32, lane = threadIdx.x % 32;
@@ -231,6 +257,11 @@ __global__ void __launch_bounds__(FT_THREADS) tc_pass_kernel(TcPassArgs a, unsig
         split3(step_matrix<KIND>(kk, n), m1, m2, m3);
         const u32 pb = prod_b(j);
         *(__nv_bfloat16 *)(sB + tc::kmajor_offset(n, j * KIN + kk, 6 * KIN)) = pb == 0 ? m1 : pb == 1 ? m2 : m3;
+    }
+    for (u32 r = threadIdx.x; r < 1024; r += FT_THREADS) {
+        float sn, c;
+        sincospif((float)r / 2048.0f, &sn, &c);
+        tab[r] = make_float2(c, -sn);
     }
     if (threadIdx.x == 0) tc::mbar_init(&bar, 1);
     tc::fence_before_sync();
@@ -259,24 +290,31 @@ __global__ void __launch_bounds__(FT_THREADS) tc_pass_kernel(TcPassArgs a, unsig
             const u64 v = tile / tiles_per_vec, rem = tile % tiles_per_vec;
             base = v * n + (rem / cchunks) * (1ull << a.k1) + (rem % cchunks) * ct;
         }
-        // load (zeros beyond the data): eight elements' raw bits in flight per thread, then the
-        // conversions (whose rare out-of-line fallback would otherwise serialise the loads)
-        for (u32 e0 = threadIdx.x; e0 < Q * ct; e0 += 8 * FT_THREADS) {
-            u64 br[8], bi[8];
+        // load (zeros beyond the data): pairs of adjacent elements as 16-byte loads, all of a
+        // thread's raw bits in flight before the conversions (whose rare out-of-line fallback
+        // would otherwise serialise the loads).  Q * ct is even and ct is 1 (pass 1) or even,
+        // so a pair never straddles two rows; a.total is a multiple of n >= 2.
+        {
+            constexpr u32 PAIRS = FT_TILE / (2 * FT_THREADS);  // 8
+            ulonglong2 br[PAIRS], bi[PAIRS];
 #pragma unroll
-            for (u32 i = 0; i < 8; i++) {
-                const u32 e = e0 + i * FT_THREADS;
+            for (u32 i = 0; i < PAIRS; i++) {
+                const u32 e = 2 * (threadIdx.x + i * FT_THREADS);
                 const u64 f = base + ((u64)(e / ct) << a.k0) + (e % ct);
                 const bool in = e < Q * ct && f < a.total;
-                br[i] = in ? (u64)__double_as_longlong(a.xr[f]) : 0ull;
-                bi[i] = (in && KIND != TC_WHT) ? (u64)__double_as_longlong(a.xi[f]) : 0ull;
+                br[i] = in ? *(const ulonglong2 *)(a.xr + f) : make_ulonglong2(0, 0);
+                bi[i] = (in && KIND != TC_WHT) ? *(const ulonglong2 *)(a.xi + f) : make_ulonglong2(0, 0);
             }
 #pragma unroll
-            for (u32 i = 0; i < 8; i++) {
-                const u32 e = e0 + i * FT_THREADS;
+            for (u32 i = 0; i < PAIRS; i++) {
+                const u32 e = 2 * (threadIdx.x + i * FT_THREADS);
                 if (e < Q * ct) {
-                    sr[slot(e)] = to_f32(br[i]);
-                    if (KIND != TC_WHT) si[slot(e)] = to_f32(bi[i]);
+                    sr[slot(e)] = to_f32(br[i].x);
+                    sr[slot(e + 1)] = to_f32(br[i].y);
+                    if (KIND != TC_WHT) {
+                        si[slot(e)] = to_f32(bi[i].x);
+                        si[slot(e + 1)] = to_f32(bi[i].y);
+                    }
                 }
             }
         }
@@ -309,7 +347,7 @@ __global__ void __launch_bounds__(FT_THREADS) tc_pass_kernel(TcPassArgs a, unsig
                     }
                     const u32 f1 = (u32)base + (q1 << a.k0) + cc;  // only its low k bits are used
                     float wr, wi;
-                    twiddle(f1 & ((1u << k) - 1), k + 1, tw_sign, wr, wi);
+                    twiddle(tab, f1 & ((1u << k) - 1), k + 1, tw_sign, wr, wi);
                     const float ar = sr[e1], ai = si[e1], br = sr[e2], bi = si[e2];
                     if (KIND == TC_FFT) {
                         const float yr = br * wr - bi * wi, yi = br * wi + bi * wr;
@@ -325,40 +363,50 @@ __global__ void __launch_bounds__(FT_THREADS) tc_pass_kernel(TcPassArgs a, unsig
             }
             // radix-16 step through the tensor cores, two M-tiles of 128 groups
             for (u32 mt = 0; mt < FT_GROUPS / 128 && ok; mt++) {
-                // build A: thread t handles group 128*mt + t%128, members 8*(t/128) .. +7; the
-                // eight members' BF16 terms of one product sit side by side along K (one 16-byte
-                // row of a core matrix), so each (product, component) is a single 16-byte store
+                // build A: thread t handles group 128*mt + t%128, members 8*(t/128) .. +7 at
+                // elements e0 + pp*S; the eight members' BF16 terms of one product sit side by
+                // side along K (one 16-byte row of a core matrix): one 16-byte store per (product,
+                // component).  Members are split two at a time with packed BF16x2 conversions.
                 {
                     const u32 gi = 128 * mt + (threadIdx.x & 127), half = threadIdx.x >> 7;
                     const u32 cc = gi % ct, qq = gi / ct;
                     const u32 qlo = qq & ((1u << lo) - 1), qhi = qq >> lo;
                     const u32 row = threadIdx.x & 127;
+                    const u32 S = (1u << lo) * ct;
+                    const u32 e0 = (qlo | (qhi << (lo + 4))) * ct + cc + half * 8 * S;
+                    // the group's offset below bit k, the same for all its members
+                    const u32 cgrp = ((u32)base + (qlo << a.k0) + cc) & ((1u << k) - 1);
                     u32 pr[3][4], pim[3][4];  // [split][pair of members]: two BF16 per word
 #pragma unroll
-                    for (u32 pp = 0; pp < 8; pp++) {
-                        const u32 p = half * 8 + pp;
-                        const u32 q = qlo | (p << lo) | (qhi << (lo + 4));
-                        const u32 e = slot(q * ct + cc);
-                        float xr_ = sr[e], xi_ = (KIND == TC_WHT) ? 0.0f : si[e];
-                        if (KIND == TC_FFT && k > 0) {  // pre-twiddle w^br(p) (w = 1 on the first step)
-                            const u32 c = ((u32)base + (q << a.k0) + cc) & ((1u << k) - 1);
-                            float wr, wi;
-                            twiddle((c * brev4(p)) & ((1u << (k + 4)) - 1), k + 4, -1.0f, wr, wi);
-                            const float tr = xr_ * wr - xi_ * wi;
-                            xi_ = xr_ * wi + xi_ * wr;
-                            xr_ = tr;
+                    for (u32 pp = 0; pp < 8; pp += 2) {
+                        float xr2[2], xi2[2];
+#pragma unroll
+                        for (u32 h = 0; h < 2; h++) {
+                            const u32 e = slot(e0 + (pp + h) * S);
+                            xr2[h] = sr[e];
+                            xi2[h] = (KIND == TC_WHT) ? 0.0f : si[e];
+                            if (KIND == TC_FFT && k > 0) {  // pre-twiddle w^br(p) (w = 1 on the first step)
+                                float wr, wi;
+                                twiddle(tab, (cgrp * brev4(half * 8 + pp + h)) & ((1u << (k + 4)) - 1), k + 4, -1.0f,
+                                        wr, wi);
+                                const float tr = xr2[h] * wr - xi2[h] * wi;
+                                xi2[h] = xr2[h] * wi + xi2[h] * wr;
+                                xr2[h] = tr;
+                            }
                         }
-                        __nv_bfloat16 r[3], im[3];
-                        split3(xr_, r[0], r[1], r[2]);
-                        if (KIND != TC_WHT) split3(xi_, im[0], im[1], im[2]);
-                        const u32 sh = (pp & 1) * 16;
+                        // x = x1 + x2 + x3, each RN to BF16 of what is left
+                        float ar = xr2[0], br = xr2[1], ai = xi2[0], bi = xi2[1];
 #pragma unroll
                         for (u32 z = 0; z < 3; z++) {
-                            const u32 rb = (u32)__bfloat16_as_ushort(r[z]) << sh;
-                            pr[z][pp >> 1] = (pp & 1) ? (pr[z][pp >> 1] | rb) : rb;
+                            const __nv_bfloat162 hr = __floats2bfloat162_rn(ar, br);
+                            pr[z][pp >> 1] = *(const u32 *)&hr;
+                            ar -= __low2float(hr);
+                            br -= __high2float(hr);
                             if (KIND != TC_WHT) {
-                                const u32 ib = (u32)__bfloat16_as_ushort(im[z]) << sh;
-                                pim[z][pp >> 1] = (pp & 1) ? (pim[z][pp >> 1] | ib) : ib;
+                                const __nv_bfloat162 hi = __floats2bfloat162_rn(ai, bi);
+                                pim[z][pp >> 1] = *(const u32 *)&hi;
+                                ai -= __low2float(hi);
+                                bi -= __high2float(hi);
                             }
                         }
                     }
@@ -396,6 +444,8 @@ __global__ void __launch_bounds__(FT_THREADS) tc_pass_kernel(TcPassArgs a, unsig
                     const u32 gi = 128 * mt + 32 * (warp & 3) + lane;
                     const u32 cc = gi % ct, qq = gi / ct;
                     const u32 qlo = qq & ((1u << lo) - 1), qhi = qq >> lo;
+                    const u32 S = (1u << lo) * ct;
+                    const u32 e0 = (qlo | (qhi << (lo + 4))) * ct + cc;
                     const u32 col0 = (KIND == TC_WHT) ? 0u : 16u * (warp >> 2);
                     if (KIND != TC_WHT || warp < 4) {
                         const u32 lanes = (32 * (warp & 3)) << 16;
@@ -405,12 +455,12 @@ __global__ void __launch_bounds__(FT_THREADS) tc_pass_kernel(TcPassArgs a, unsig
                         tc::tmem_ld16(tmem + lanes + 64 + col0, v2);
                         tc::tmem_wait_ld();
                         float *dst = (KIND == TC_WHT || warp < 4) ? sr : si;
+#pragma unroll
                         for (u32 m = 0; m < 16; m++) {
-                            const u32 q = qlo | (m << lo) | (qhi << (lo + 4));
                             float y = __uint_as_float(v0[m]);
                             if (KIND != TC_WHT) y += __uint_as_float(v1[m]);
                             y += __uint_as_float(v2[m]);
-                            dst[slot(q * ct + cc)] = y;
+                            dst[slot(e0 + m * S)] = y;
                         }
                     }
                 }
@@ -421,16 +471,19 @@ __global__ void __launch_bounds__(FT_THREADS) tc_pass_kernel(TcPassArgs a, unsig
                     const u32 gi = 128 * mt + (threadIdx.x & 127), half = threadIdx.x >> 7;
                     const u32 cc = gi % ct, qq = gi / ct;
                     const u32 qlo = qq & ((1u << lo) - 1), qhi = qq >> lo;
-                    for (u32 pp = 0; pp < 8; pp++) {
-                        const u32 p = half * 8 + pp;
-                        const u32 q = qlo | (p << lo) | (qhi << (lo + 4));
-                        const u32 e = slot(q * ct + cc);
-                        const u32 c = ((u32)base + (q << a.k0) + cc) & ((1u << k) - 1);
-                        float wr, wi;
-                        twiddle((c * brev4(p)) & ((1u << (k + 4)) - 1), k + 4, 1.0f, wr, wi);
-                        const float xr_ = sr[e], xi_ = si[e];
-                        sr[e] = xr_ * wr - xi_ * wi;
-                        si[e] = xr_ * wi + xi_ * wr;
+                    const u32 S = (1u << lo) * ct;
+                    const u32 e0 = (qlo | (qhi << (lo + 4))) * ct + cc + half * 8 * S;
+                    const u32 cgrp = ((u32)base + (qlo << a.k0) + cc) & ((1u << k) - 1);
+                    if (k > 0) {
+#pragma unroll
+                        for (u32 pp = 0; pp < 8; pp++) {
+                            const u32 e = slot(e0 + pp * S);
+                            float wr, wi;
+                            twiddle(tab, (cgrp * brev4(half * 8 + pp)) & ((1u << (k + 4)) - 1), k + 4, 1.0f, wr, wi);
+                            const float xr_ = sr[e], xi_ = si[e];
+                            sr[e] = xr_ * wr - xi_ * wi;
+                            si[e] = xr_ * wi + xi_ * wr;
+                        }
                     }
                     __syncthreads();
                 }
@@ -438,12 +491,14 @@ __global__ void __launch_bounds__(FT_THREADS) tc_pass_kernel(TcPassArgs a, unsig
             if (!ok) break;
         }
         if (!ok) break;
-        // store
-        for (u32 e = threadIdx.x; e < Q * ct; e += FT_THREADS) {
+        // store, pairs of adjacent elements as 16-byte stores
+        for (u32 e = 2 * threadIdx.x; e < Q * ct; e += 2 * FT_THREADS) {
             const u64 f = base + ((u64)(e / ct) << a.k0) + (e % ct);
             if (f < a.total) {
-                store_f64(a.xr + f, sr[slot(e)] * a.scale);
-                if (KIND != TC_WHT) store_f64(a.xi + f, si[slot(e)] * a.scale);
+                *(double2 *)(a.xr + f) = make_double2(to_f64(sr[slot(e)] * a.scale), to_f64(sr[slot(e + 1)] * a.scale));
+                if (KIND != TC_WHT)
+                    *(double2 *)(a.xi + f) =
+                        make_double2(to_f64(si[slot(e)] * a.scale), to_f64(si[slot(e + 1)] * a.scale));
             }
         }
         __syncthreads();
@@ -461,6 +516,7 @@ int run_tc(int kind, u64 d1, u64 d2, u64 n_half, double *xr, double *xi, cudaStr
     const u64 nvec = d1 * d2, n = 2 * n_half;
     if (nvec == 0) return QMC_OK;
     QMC_REQUIRE(xr && (kind == TC_WHT || xi), "%s: null data pointer", what);
+    QMC_REQUIRE((((uintptr_t)xr | (uintptr_t)xi) & 15) == 0, "%s: data arrays must be 16-byte aligned", what);
     unsigned *err = qmcgb::device_error_ptr();
     QMC_REQUIRE(err, "device error word unavailable");
     u32 L = 0;
@@ -470,7 +526,7 @@ int run_tc(int kind, u64 d1, u64 d2, u64 n_half, double *xr, double *xi, cudaStr
     int np = 0;
     passes[np++] = {0, L < 12 ? L : 12};
     for (u32 k0 = 12; k0 < L; k0 += 8) passes[np++] = {k0, (k0 + 8 < L) ? k0 + 8 : L};
-    const size_t smem = FT_PAD * 8 + 128 * FT_KS * 2 + 32 * FT_KS * 2;
+    const size_t smem = FT_PAD * 8 + 128 * FT_KS * 2 + 32 * FT_KS * 2 + 1024 * 8;
     const float scale = (float)(1.0 / sqrt((double)n));
     for (int pi = 0; pi < np; pi++) {
         const P p = (kind == TC_IFFT) ? passes[np - 1 - pi] : passes[pi];
