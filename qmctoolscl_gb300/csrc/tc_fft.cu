@@ -109,10 +109,10 @@ extern "C" int qmc_tc_mma_probe(const void *A, const void *B, float *D, uint32_t
 // GEMM.  The 256 groups of a tile form two M = 128 tiles.  A group's 16
 // complex inputs are 32 reals; each is split into three BF16 terms
 // x = x1 + x2 + x3 (24 significant bits), and so is each entry of the real
-// 32 x 32 form of the 16-point matrix.  The six products with i + j <= 4
-// (x1m1, x1m2, x2m1, x1m3, x2m2, x3m1) are laid side by side along K, so one
-// M=128, N=32, K=192 product (12 tcgen05.mma, FP32 accumulation in tensor
-// memory) gives the step for 128 groups.  The tensor core's accumulation does
+// 32 x 32 form of the 16-point matrix.  A holds x1 | x2 | x3 and B
+// m1 | m2 | m3 along K; the six products with i + j <= 4 (x1m1, x1m2, x2m1,
+// x1m3, x2m2, x3m1) are 12 tcgen05.mma of M=128, N=32, K=16 over the matching
+// slices (FP32 accumulation in tensor memory), the step for 128 groups.  The tensor core's accumulation does
 // not round to nearest, and chaining all twelve MMAs into one accumulator
 // measured about 1e-6 error per step; so the two MMAs of the dominant x1*m1
 // product each get their own accumulator and the ten small products a third,
@@ -125,7 +125,7 @@ namespace {
 
 constexpr u32 FT_TILE = 4096;          // complex values per tile
 constexpr u32 FT_GROUPS = FT_TILE / 16;
-constexpr u32 FT_KS = 192;             // K of the split product: 6 x 32 reals
+constexpr u32 FT_KS = 96;              // K of the operands: 3 splits x 32 reals
 constexpr u32 FT_THREADS = 256;
 constexpr u32 TMEM_COLS = 128;         // three 32-column FP32 accumulators
 constexpr u32 FT_PAD = FT_TILE + FT_TILE / 16;  // shared-memory words per component, padded
@@ -235,13 +235,13 @@ __device__ __forceinline__ void twiddle(const float2 *tab, u32 t, u32 bits, floa
 }
 
 template <int KIND>
-__global__ void __launch_bounds__(FT_THREADS) tc_pass_kernel(TcPassArgs a, unsigned *err)
+__global__ void __launch_bounds__(FT_THREADS, 3) tc_pass_kernel(TcPassArgs a, unsigned *err)
 {
     extern __shared__ __align__(128) unsigned char sm[];
     float *sr = (float *)sm;                            // [FT_PAD] real parts (slot(e))
     float *si = sr + FT_PAD;                            // [FT_PAD] imaginary parts
-    unsigned char *sA = (unsigned char *)(si + FT_PAD);   // [128 x FT_KS] bf16 operand A
-    unsigned char *sB = sA + 128 * FT_KS * 2;           // [32 x FT_KS]  bf16 operand B
+    unsigned char *sA = (unsigned char *)(si + FT_PAD);   // [128 x FT_KS] bf16 operand A: x1 | x2 | x3
+    unsigned char *sB = sA + 128 * FT_KS * 2;           // [32 x FT_KS]  bf16 operand B: m1 | m2 | m3
     float2 *tab = (float2 *)(sB + 32 * FT_KS * 2);      // [1024] exp(-2 pi i r / 4096)
     __shared__ __align__(8) u64 bar;
     __shared__ u32 tmem_base;
@@ -250,13 +250,12 @@ __global__ void __launch_bounds__(FT_THREADS) tc_pass_kernel(TcPassArgs a, unsig
     const u32 KIN = (KIND == TC_WHT) ? 16u : 32u;       // reals per group and split
 
     if (warp == 0) tc::tmem_alloc(&tmem_base, TMEM_COLS);
-    // operand B: the split step matrix, B[n][32j + kk] = M_b(j)[kk][n]
-    for (u32 e = threadIdx.x; e < NOUT * 6 * KIN; e += FT_THREADS) {
-        const u32 n = e / (6 * KIN), rest = e % (6 * KIN), j = rest / KIN, kk = rest % KIN;
-        __nv_bfloat16 m1, m2, m3;
-        split3(step_matrix<KIND>(kk, n), m1, m2, m3);
-        const u32 pb = prod_b(j);
-        *(__nv_bfloat16 *)(sB + tc::kmajor_offset(n, j * KIN + kk, 6 * KIN)) = pb == 0 ? m1 : pb == 1 ? m2 : m3;
+    // operand B: the split step matrix, B[n][KIN*z + kk] = m_z[kk][n] (z = 0, 1, 2)
+    for (u32 e = threadIdx.x; e < NOUT * 3 * KIN; e += FT_THREADS) {
+        const u32 n = e / (3 * KIN), rest = e % (3 * KIN), z = rest / KIN, kk = rest % KIN;
+        __nv_bfloat16 m[3];
+        split3(step_matrix<KIND>(kk, n), m[0], m[1], m[2]);
+        *(__nv_bfloat16 *)(sB + tc::kmajor_offset(n, z * KIN + kk, 3 * KIN)) = m[z];
     }
     for (u32 r = threadIdx.x; r < 1024; r += FT_THREADS) {
         float sn, c;
@@ -268,7 +267,7 @@ __global__ void __launch_bounds__(FT_THREADS) tc_pass_kernel(TcPassArgs a, unsig
     __syncthreads();
     tc::fence_after_sync();
     const u32 tmem = tmem_base;
-    const u32 KTOT = 6 * KIN;
+    const u32 KTOT = 3 * KIN;
     const u32 idesc = tc::idesc_bf16_f32(128, NOUT);
     const u32 sbo = (KTOT / 8) * 128;
     u32 phase = 0;
@@ -411,13 +410,12 @@ __global__ void __launch_bounds__(FT_THREADS) tc_pass_kernel(TcPassArgs a, unsig
                         }
                     }
 #pragma unroll
-                    for (u32 j = 0; j < 6; j++) {
-                        const u32 pa = prod_a(j);
-                        *(uint4 *)(sA + tc::kmajor_offset(row, j * KIN + half * 8, KTOT)) =
-                            make_uint4(pr[pa][0], pr[pa][1], pr[pa][2], pr[pa][3]);
+                    for (u32 z = 0; z < 3; z++) {
+                        *(uint4 *)(sA + tc::kmajor_offset(row, z * KIN + half * 8, KTOT)) =
+                            make_uint4(pr[z][0], pr[z][1], pr[z][2], pr[z][3]);
                         if (KIND != TC_WHT)
-                            *(uint4 *)(sA + tc::kmajor_offset(row, j * KIN + 16 + half * 8, KTOT)) =
-                                make_uint4(pim[pa][0], pim[pa][1], pim[pa][2], pim[pa][3]);
+                            *(uint4 *)(sA + tc::kmajor_offset(row, z * KIN + 16 + half * 8, KTOT)) =
+                                make_uint4(pim[z][0], pim[z][1], pim[z][2], pim[z][3]);
                     }
                 }
                 tc::fence_smem_to_async();
@@ -425,13 +423,21 @@ __global__ void __launch_bounds__(FT_THREADS) tc_pass_kernel(TcPassArgs a, unsig
                 __syncthreads();
                 tc::fence_after_sync();
                 if (threadIdx.x == 0) {
-                    // accumulators: D0, D1 the two K-slices of x1*m1 (one MMA each),
-                    // D2 the products about 2^-8 smaller; summed in FP32 on read-back
-                    const u32 nmain = (KIND == TC_WHT) ? 1u : 2u;
-                    for (u32 s = 0; s < KTOT / 16; s++) {
-                        const u32 dst = tmem + (s < nmain ? 32u * s : 64u);
-                        tc::mma_bf16(dst, tc::smem_desc(sA + s * 256, 128, sbo), tc::smem_desc(sB + s * 256, 128, sbo),
-                                     idesc, s > nmain ? 1u : 0u);
+                    // the six products x_za * m_zb with za + zb <= 2, each KIN/16 MMAs of K = 16 over
+                    // the matching slices of A and B; accumulators: D0, D1 the two K-slices of
+                    // x1*m1 (one MMA each), D2 the products about 2^-8 smaller; summed in FP32 on
+                    // read-back
+                    const u32 kin16 = KIN / 16;  // MMAs per product: 2 (FFT), 1 (WHT)
+                    u32 issued = 0;
+                    for (u32 j = 0; j < 6; j++) {
+                        const u32 za = prod_a(j), zb = prod_b(j);
+                        for (u32 sl = 0; sl < kin16; sl++) {
+                            const u32 dst = j == 0 ? 32u * sl : 64u;
+                            const u32 acc = j == 0 ? 0u : (issued > kin16 ? 1u : 0u);
+                            tc::mma_bf16(tmem + dst, tc::smem_desc(sA + (za * kin16 + sl) * 256, 128, sbo),
+                                         tc::smem_desc(sB + (zb * kin16 + sl) * 256, 128, sbo), idesc, acc);
+                            issued++;
+                        }
                     }
                     tc::mma_commit(&bar);
                 }
@@ -547,7 +553,7 @@ int run_tc(int kind, u64 d1, u64 d2, u64 n_half, double *xr, double *xi, cudaStr
         A.xi = xi;
         A.scale = (pi == np - 1) ? scale : 1.0f;
         const u64 tiles = (p.k0 == 0) ? (A.total + FT_TILE - 1) / FT_TILE : A.total / (A.Q * (u64)A.ct);
-        const unsigned grid = qmcgb::grid_for(tiles, 1, (unsigned)qmcgb::sm_count() * 2);
+        const unsigned grid = qmcgb::grid_for(tiles, 1, (unsigned)qmcgb::sm_count() * 3);  // 3 CTAs per SM fit
         cudaError_t e;
         if (kind == TC_FFT) {
             e = cudaFuncSetAttribute(tc_pass_kernel<TC_FFT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
