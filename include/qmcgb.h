@@ -11,10 +11,14 @@
  * (e.g. x is r*n*d with d fastest).  Outputs are written in place; the
  * transforms work in place and also fill both twiddle arrays.
  *
- * Every call is stream-ordered and asynchronous, allocates nothing, keeps no
- * host state between calls and is safe to call from several host threads.
- * It returns QMC_OK or a negative status; qmc_last_error() gives the
- * message for the calling thread.
+ * Every per-function entry point (and the fused qmc_lat_gen_shift,
+ * qmc_dnb2_gen_fused, the tensor-core transforms and qmc_net_gen_noalloc) is
+ * stream-ordered and asynchronous, allocates nothing, keeps no host state
+ * between calls and is safe to call from several host threads.  The plan
+ * objects (qmc_*_plan_create) allocate their device tables when created and
+ * free them when destroyed; running a plan allocates nothing.  Every call
+ * returns QMC_OK or a negative status; qmc_last_error() gives the message
+ * for the calling thread.
  *
  * Where the reference's behaviour is undefined (shift counts >= 64 in C,
  * reads past an array) the kernels follow what gcc builds of the reference
@@ -194,7 +198,7 @@ int qmc_tc_mma_probe(const void *A, const void *B, float *D, uint32_t N, uint32_
  * BF16 tensor-core products (three-term BF16 splits of data and matrix, FP32
  * accumulation): relative L2 error about 1e-7 against the FP64 transform
  * instead of FP64 rounding.  No twiddle arrays are written.  n = 2*n_half up
- * to 2^24. */
+ * to 2^24; the data arrays must be 16-byte aligned (QMC_ERR_ARG otherwise). */
 int qmc_tc_fft_bro_1d(uint64_t d1, uint64_t d2, uint64_t n_half, double *xr, double *xi, qmc_stream_t s);
 int qmc_tc_ifft_bro_1d(uint64_t d1, uint64_t d2, uint64_t n_half, double *xr, double *xi, qmc_stream_t s);
 int qmc_tc_fwht_1d(uint64_t d1, uint64_t d2, uint64_t n_half, double *x, qmc_stream_t s);
