@@ -46,6 +46,9 @@ R, LOG2N, D = 16, 20, 64
 PROFILE_LOG2N = 16  # --small: the same kernel on 512 MiB of output, for ncu captures
 SEED = 2
 FALLBACK_HBM_GBS = 6800.0
+# DRAM bytes / algorithmic bytes of the two captured tensor-core FFT passes (n = 2^20):
+# (404.6 + 346.1 + 404.5 + 346.8) MB / (2 x 805.3 MB)
+TC_FFT_TRAFFIC_RATIO = 0.9323
 
 
 def workload_inputs(seed=SEED):
@@ -735,14 +738,17 @@ def run_fft(args):
             "data": "synthetic (np.random.SFC64(5)), N(0,1) complex",
             "config": {"workload": "bit-reversed FFT of %d vectors, log2 n uniform in [10,20]" % len(L),
                        "samples": samples, "lengths": counts},
-            "roofline": dict(roofline(alg_tc, ms["fft_tc"]), note="32 B per complex sample per pass (FP64 read+write)"),
+            "roofline": dict(roofline(alg_tc, ms["fft_tc"]), kernel="tc_pass_kernel<FFT> (all passes of a step)",
+                             traffic=alg_tc * TC_FFT_TRAFFIC_RATIO,
+                             note="32 B per complex sample per pass (FP64 read+write); traffic = algorithmic bytes x "
+                                  "the DRAM/algorithmic ratio of the ncu capture in profiles/tc_pass_kernel_fft_n2p20.md"),
             "fp64": {"fft_ms": ms["fft_fp64"], "fwht_ms": ms["fwht_fp64"],
                      "fft_gsamples_per_s": samples / (ms["fft_fp64"] / 1e3) / 1e9,
                      "fp64_vs_numpy_rel_l2": fp64_vs_numpy},
             "tc": {"fft_ms": ms["fft_tc"], "fwht_ms": ms["fwht_tc"], "fft_speedup_vs_fp64": ms["fft_fp64"] / ms["fft_tc"],
                    "fwht_speedup_vs_fp64": ms["fwht_fp64"] / ms["fwht_tc"], "max_rel_l2_error": worst,
                    "error_by_log2n": err},
-            "gpu_launches": None}
+            "gpu_launches": steps * sum(passes(g["L"]) for g in groups)}
 
 
 def first_primes(k):
