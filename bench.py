@@ -356,6 +356,19 @@ def run_ours(args):
                         "%s" % ("written by the kernel over NVLink-C2C" if best == "direct"
                                 else "staged in HBM and copied back"))
     e2e_line["other"] = {k: v for k, v in e2e.items() if k != best}
+    # the CPU-GPU link's own rate for the same bytes: one device-to-host copy of the result
+    # into the same pinned array (the e2e path cannot beat it)
+    xr_t = torch.from_numpy(xr_host.reshape(-1))
+    xr_t.copy_(xr_d.reshape(-1), non_blocking=True)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    xr_t.copy_(xr_d.reshape(-1), non_blocking=True)
+    torch.cuda.synchronize()
+    t_link = time.perf_counter() - t0
+    link_gbs = 8.0 * R * n * D / t_link / 1e9
+    e2e_line["link"] = {"d2h_copy_ms": 1e3 * t_link, "d2h_gbs": link_gbs,
+                        "e2e_d2h_gbs": e2e_line["d2h_bytes_per_step"] / (e2e_line["ms_per_step"] / 1e3) / 1e9,
+                        "note": "plain device-to-host copy of the same result into the same pinned array"}
 
     if rank != 0:
         return
