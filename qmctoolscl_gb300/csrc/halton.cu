@@ -32,9 +32,11 @@
 // randomisation and all d dimensions.  Each warp takes whole dimensions
 // (assigned longest-first to balance the work), one point per lane, so the
 // 32 lanes share base, digit count and tables.  The index splits as
-// hi * b^K + lo with b^K >= 32: the tile has at most two distinct hi, whose
-// contributions to each output digit the lanes compute together, and K <= 5
-// low digits per lane.  Per output digit t: the raw digit mod b (32-bit
+// hi * b^K + lo with b^K >= the tile's point count (32 or 64): the tile has at
+// most two distinct hi, whose contributions to each output digit the lanes
+// compute together, and K <= 6 low digits per point.  With few enough
+// dimensions each lane carries two points (two independent chains sharing
+// the shuffled per-digit values).  Per output digit t: the raw digit mod b (32-bit
 // multiply-high division), the term from the table, and v = RN(v + term) --
 // on the FP64 unit or in integer arithmetic on the unpacked sum
 // (digit_sum.cuh), chosen per dimension so that the FP64 pipe and the integer
@@ -59,7 +61,7 @@ enum : u32 { ADD_FP64 = 0, ADD_INT = 1 };
 
 struct HDim {
     u32 b, tmax, mmax;
-    u32 K;         // low digits per lane: the smallest K with b^K >= 32
+    u32 K;         // low digits per point: the smallest K with b^K >= points per tile
     u32 Klo;       // min(K, mmax): low digits that can be nonzero (C has mmax rows)
     u32 bK;        // b^K
     u32 m32;       // floor(2^32 / b) + 1: x / b = umulhi(x, m32) for x < 2^32 / b
@@ -248,39 +250,52 @@ __device__ __forceinline__ u32 high_part(const HDim &D, const u32 *Cj, u32 h, u3
     return dim_mod(D, acc);
 }
 
-// The value of dimension D for this lane's point (bits of the double), KL =
-// min(K, mmax) low digits per lane.
+// The values of dimension D for this lane's PPL points (bits of the doubles),
+// KL = min(K, mmax) low digits per point.  The CTA's tile holds 32 * PPL
+// consecutive points (lane c has points c, c + 32, ...), and b^K >= 32 * PPL,
+// so the tile spans at most two values of hi = index / b^K.
 //
 // Output digits go in chunks of 32: lane c holds, for digit t0 + c, the
 // high-digit sums of both hi values (packed), the low-digit matrix entries
 // C[k][t0 + c] (k < KL) and the tail exponent, and every lane takes its own
-// from lane t - t0 by shuffles.  Within a chunk, groups of HT_GROUP digits
-// compute their raw digits and issue their table reads (independent of v),
-// then add the terms in order.  The early stop is tested once per group: an
-// add after the exact stop point leaves v unchanged (the term is below half
-// an ulp), so the group's adds need no test; a stopped lane adds +0.
-template <u32 ADD, u32 KL>
-__device__ __forceinline__ u64 dim_value(const HDim &D, const u32 *Cj, const u64 *Yj, const u32 *Tj, u32 base,
-                                         u32 itrue, bool active, u32 lane)
+// from lane t - t0 by shuffles, shared by its PPL points.  Within a chunk,
+// groups of HT_GROUP digits compute their raw digits and issue their table
+// reads (independent of v), then add the terms in order.  The early stop is
+// tested once per group: an add after the exact stop point leaves v
+// unchanged (the term is below half an ulp), so the group's adds need no
+// test; a stopped point adds +0.
+template <u32 ADD, u32 KL, u32 PPL>
+__device__ __forceinline__ void dim_value(const HDim &D, const u32 *Cj, const u64 *Yj, const u32 *Tj, u32 base,
+                                          const u32 (&itrue)[PPL], const bool (&active)[PPL], u32 lane, u64 (&out)[PPL])
 {
     const u32 h0 = hdiv(D.fdK_M, base);
-    const u32 hi = hdiv(D.fdK_M, itrue);
-    const u32 sel = (hi - h0) * 16;  // 0 or 16: which half of the packed word
-    u32 dl[KL];                       // low digits
-    {
-        u32 x = itrue - hi * D.bK;    // < b^K < 32 b
+    u32 sel[PPL], dl[PPL][KL];
+    bool done[PPL];
+    dsum::Sum vi[PPL];  // ADD_INT: the running sums, unpacked
+    double vd[PPL];     // ADD_FP64: the running sums
+#pragma unroll
+    for (u32 q = 0; q < PPL; q++) {
+        const u32 hi = hdiv(D.fdK_M, itrue[q]);
+        sel[q] = (hi - h0) * 16;  // 0 or 16: which half of the packed word
+        u32 x = itrue[q] - hi * D.bK;  // < b^K < 64 b
 #pragma unroll
         for (u32 k = 0; k < KL; k++) {
-            const u32 q = ndiv(D.m32, x);
-            dl[k] = x - q * D.b;
-            x = q;
+            const u32 qq = ndiv(D.m32, x);
+            dl[q][k] = x - qq * D.b;
+            x = qq;
         }
+        done[q] = !active[q];
+        vi[q] = dsum::unpack(0);
+        vd[q] = 0.0;
     }
-    bool done = !active;
-    dsum::Sum vi = dsum::unpack(0);  // ADD_INT: the running sum, unpacked
-    double vd = 0.0;                 // ADD_FP64: the running sum
+    auto all_done = [&]() {
+        bool a = true;
+#pragma unroll
+        for (u32 q = 0; q < PPL; q++) a = a && done[q];
+        return a;
+    };
     for (u32 t0 = 0; t0 < D.tpad; t0 += 32) {
-        if (__all_sync(0xffffffffu, done)) break;
+        if (__all_sync(0xffffffffu, all_done())) break;
         const u32 tc = t0 + lane;
         u32 packed = 0, tailc = 0, cl[KL];
 #pragma unroll
@@ -295,72 +310,99 @@ __device__ __forceinline__ u64 dim_value(const HDim &D, const u32 *Cj, const u64
         for (u32 t = t0; t < tend; t += HT_GROUP) {
             // every remaining term is below 2^(tail - 1022); once that is at most half an ulp of v
             // (2^(E - 1076)), RN(v + term) = v for the rest of the digits
-            const u32 E = ADD == ADD_INT ? vi.E : (u32)(as_bits(vd) >> 52);
             const u32 tl = __shfl_sync(0xffffffffu, tailc, t - t0);  // every lane takes part in the shuffle
-            done = done || tl + 54 <= E;
-            if (__all_sync(0xffffffffu, done)) break;
-            u64 y[HT_GROUP];
+#pragma unroll
+            for (u32 q = 0; q < PPL; q++) {
+                const u32 E = ADD == ADD_INT ? vi[q].E : (u32)(as_bits(vd[q]) >> 52);
+                done[q] = done[q] || tl + 54 <= E;
+            }
+            if (__all_sync(0xffffffffu, all_done())) break;
+            u64 y[PPL][HT_GROUP];
 #pragma unroll
             for (u32 u = 0; u < HT_GROUP; u++) {
                 const u32 src = t + u - t0;
-                // gdn_gen_natural.c:37-50: raw digit t + u of the point, mod b (rows past tmax: +0)
-                u32 acc = (__shfl_sync(0xffffffffu, packed, src) >> sel) & 0xFFFFu;
+                // gdn_gen_natural.c:37-50: raw digit t + u of each point, mod b (rows past tmax: +0)
+                const u32 pk = __shfl_sync(0xffffffffu, packed, src);
+                u32 c[KL];
 #pragma unroll
-                for (u32 k = 0; k < KL; k++) acc += dl[k] * __shfl_sync(0xffffffffu, cl[k], src);
-                y[u] = done ? 0ull : Yj[(t + u) * D.b + dim_mod(D, acc)];
+                for (u32 k = 0; k < KL; k++) c[k] = __shfl_sync(0xffffffffu, cl[k], src);
+#pragma unroll
+                for (u32 q = 0; q < PPL; q++) {
+                    u32 acc = (pk >> sel[q]) & 0xFFFFu;
+#pragma unroll
+                    for (u32 k = 0; k < KL; k++) acc += dl[q][k] * c[k];
+                    y[q][u] = done[q] ? 0ull : Yj[(t + u) * D.b + dim_mod(D, acc)];
+                }
             }
 #pragma unroll
             for (u32 u = 0; u < HT_GROUP; u++) {
-                if (ADD == ADD_INT)
-                    add_term_int(vi, y[u]);
-                else
-                    vd = __dadd_rn(vd, as_double(y[u]));  // gdn_integer_to_float.c:37
+#pragma unroll
+                for (u32 q = 0; q < PPL; q++) {
+                    if (ADD == ADD_INT)
+                        add_term_int(vi[q], y[q][u]);
+                    else
+                        vd[q] = __dadd_rn(vd[q], as_double(y[q][u]));  // gdn_integer_to_float.c:37
+                }
             }
         }
     }
-    return ADD == ADD_INT ? dsum::pack(vi) : as_bits(vd);
+#pragma unroll
+    for (u32 q = 0; q < PPL; q++) out[q] = ADD == ADD_INT ? dsum::pack(vi[q]) : as_bits(vd[q]);
 }
 
-template <u32 ADD>
-__device__ __forceinline__ u64 dim_value_k(const HDim &D, const u32 *Cj, const u64 *Yj, const u32 *Tj, u32 base,
-                                           u32 itrue, bool active, u32 lane)
+template <u32 ADD, u32 PPL>
+__device__ __forceinline__ void dim_value_k(const HDim &D, const u32 *Cj, const u64 *Yj, const u32 *Tj, u32 base,
+                                            const u32 (&itrue)[PPL], const bool (&active)[PPL], u32 lane,
+                                            u64 (&out)[PPL])
 {
     switch (D.Klo) {
-    case 1: return dim_value<ADD, 1>(D, Cj, Yj, Tj, base, itrue, active, lane);
-    case 2: return dim_value<ADD, 2>(D, Cj, Yj, Tj, base, itrue, active, lane);
-    case 3: return dim_value<ADD, 3>(D, Cj, Yj, Tj, base, itrue, active, lane);
-    case 4: return dim_value<ADD, 4>(D, Cj, Yj, Tj, base, itrue, active, lane);
-    default: return dim_value<ADD, 5>(D, Cj, Yj, Tj, base, itrue, active, lane);
+    case 1: return dim_value<ADD, 1, PPL>(D, Cj, Yj, Tj, base, itrue, active, lane, out);
+    case 2: return dim_value<ADD, 2, PPL>(D, Cj, Yj, Tj, base, itrue, active, lane, out);
+    case 3: return dim_value<ADD, 3, PPL>(D, Cj, Yj, Tj, base, itrue, active, lane, out);
+    case 4: return dim_value<ADD, 4, PPL>(D, Cj, Yj, Tj, base, itrue, active, lane, out);
+    case 5: return dim_value<ADD, 5, PPL>(D, Cj, Yj, Tj, base, itrue, active, lane, out);
+    default: return dim_value<ADD, 6, PPL>(D, Cj, Yj, Tj, base, itrue, active, lane, out);
     }
 }
 
+// A CTA owns tiles of 32 * PPL consecutive points of one randomisation and all d
+// dimensions; the tile of doubles is staged in shared memory ([32 * PPL][d])
+// and stored as contiguous rows.
+template <u32 PPL>
 __global__ void __launch_bounds__(HT_THREADS) halton_gen_kernel(HPlanDev P)
 {
     extern __shared__ __align__(16) unsigned char sm[];
-    double *tile = (double *)sm;  // [32][d]
+    double *tile = (double *)sm;
+    constexpr u32 TP = 32 * PPL;  // points per tile
     const u32 warp = threadIdx.x / 32, lane = threadIdx.x % 32;
-    const u64 tiles_per_l = (P.n + 31) / 32;
+    const u64 tiles_per_l = (P.n + TP - 1) / TP;
     const u64 ntiles = P.r * tiles_per_l;
     for (u64 tt = blockIdx.x; tt < ntiles; tt += gridDim.x) {
-        const u64 l = tt / tiles_per_l, i0 = (tt % tiles_per_l) * 32;
-        const bool active = i0 + lane < P.n;  // lanes past the last point compute nothing
+        const u64 l = tt / tiles_per_l, i0 = (tt % tiles_per_l) * TP;
         const u32 base = (u32)(P.n_start + i0);
-        const u32 itrue = active ? base + lane : base;  // < 2^32 (checked at plan creation)
+        u32 itrue[PPL];
+        bool active[PPL];
+#pragma unroll
+        for (u32 q = 0; q < PPL; q++) {
+            active[q] = i0 + lane + 32 * q < P.n;  // points past the last compute nothing
+            itrue[q] = active[q] ? base + lane + 32 * q : base;  // < 2^32 (checked at plan creation)
+        }
         const u32 *Cl = P.C + l * P.c_per_l;
         const u64 *Yl = P.Y + l * P.y_per_l;
         const u32 *Tl = P.tail + l * P.s_per_l;
         for (u32 oi = P.wstart[warp]; oi < P.wstart[warp + 1]; oi++) {
             const u32 j = P.order[oi];
             const HDim D = P.dims[j];
-            const u64 vb =
-                D.add == ADD_INT
-                    ? dim_value_k<ADD_INT>(D, Cl + D.c_off, Yl + D.y_off, Tl + D.s_off, base, itrue, active, lane)
-                    : dim_value_k<ADD_FP64>(D, Cl + D.c_off, Yl + D.y_off, Tl + D.s_off, base, itrue, active, lane);
-            tile[lane * P.d + j] = as_double(vb);
+            u64 vb[PPL];
+            if (D.add == ADD_INT)
+                dim_value_k<ADD_INT, PPL>(D, Cl + D.c_off, Yl + D.y_off, Tl + D.s_off, base, itrue, active, lane, vb);
+            else
+                dim_value_k<ADD_FP64, PPL>(D, Cl + D.c_off, Yl + D.y_off, Tl + D.s_off, base, itrue, active, lane, vb);
+#pragma unroll
+            for (u32 q = 0; q < PPL; q++) tile[(lane + 32 * q) * P.d + j] = as_double(vb[q]);
         }
         __syncthreads();
-        // 32 contiguous rows of the output
-        const u64 rows = min((u64)32, P.n - i0);
+        const u64 rows = min((u64)TP, P.n - i0);
         double *out = P.x + (l * P.n + i0) * P.d;
         for (u64 e = threadIdx.x; e < rows * P.d; e += HT_THREADS) __stcs(out + e, tile[e]);
         __syncthreads();
@@ -402,6 +444,7 @@ struct qmc_halton_plan {
     std::vector<PrepDim> prep;
     u64 total_c = 0, rows = 0;
     size_t smem = 0;
+    u32 ppl = 1;
     bool prepared = false;
 };
 
@@ -414,8 +457,11 @@ int qmc_halton_plan_create(uint64_t r, uint64_t n, uint64_t n_start, uint64_t d,
     *plan = nullptr;
     QMC_REQUIRE(d >= 1 && d <= HT_MAX_DIMS && r >= 1 && n >= 1, "need 1 <= d <= %u, r >= 1, n >= 1", HT_MAX_DIMS);
     QMC_REQUIRE(n_start + n <= (1ull << 32) && n_start + n > n_start, "indices must stay below 2^32");
-    const u64 smem = 32 * d * sizeof(double);
-    QMC_REQUIRE(smem <= 200 * 1024, "d too large for the shared-memory output tile");
+    QMC_REQUIRE(32 * d * sizeof(double) <= 200 * 1024, "d too large for the shared-memory output tile");
+    // two points per lane (two independent digit chains, shuffles shared) while the 64-point
+    // output tile stays small enough for four CTAs per SM
+    const u32 ppl = 64 * d * sizeof(double) <= 52 * 1024 ? 2 : 1;
+    const u64 smem = 32 * ppl * d * sizeof(double);
     // a step is applied when its array is given, for every dimension alike
     const bool has_lms = dims[0].S != nullptr, has_perm = dims[0].perms != nullptr,
                has_shift = dims[0].shifts != nullptr;
@@ -445,7 +491,7 @@ int qmc_halton_plan_create(uint64_t r, uint64_t n, uint64_t n_start, uint64_t d,
         h.mmax = (u32)q.mmax;
         h.K = 1;
         h.bK = h.b;
-        while (h.bK < 32) {
+        while (h.bK < 32 * ppl) {
             h.bK *= h.b;
             h.K++;
         }
@@ -501,6 +547,7 @@ int qmc_halton_plan_create(uint64_t r, uint64_t n, uint64_t n_start, uint64_t d,
     p->total_c = r * c_off;
     p->rows = r * s_off;
     p->smem = smem;
+    p->ppl = ppl;
     int rc = 0;
     auto alloc = [&](void **dst, size_t bytes) {
         if (!rc) rc = qmcgb::cuda_status(cudaMalloc(dst, bytes ? bytes : 16), "cudaMalloc");
@@ -522,8 +569,11 @@ int qmc_halton_plan_create(uint64_t r, uint64_t n, uint64_t n_start, uint64_t d,
         rc = qmcgb::cuda_status(cudaMemcpy(p->d_prep, p->prep.data(), d * sizeof(PrepDim), cudaMemcpyHostToDevice), "copy");
     if (!rc && !p->P.err) rc = QMC_ERR_CUDA;
     if (!rc && smem > 48 * 1024)
-        rc = qmcgb::cuda_status(cudaFuncSetAttribute(halton_gen_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                     (int)smem), "cudaFuncSetAttribute");
+        rc = qmcgb::cuda_status(ppl == 2 ? cudaFuncSetAttribute(halton_gen_kernel<2>,
+                                                                cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)
+                                         : cudaFuncSetAttribute(halton_gen_kernel<1>,
+                                                                cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
+                                "cudaFuncSetAttribute");
     p->P.dims = (const HDim *)p->d_dims;
     p->P.C = (const u32 *)p->d_C;
     p->P.Y = (const u64 *)p->d_Y;
@@ -561,9 +611,13 @@ int qmc_halton_plan_prepare(qmc_halton_plan *p, qmc_stream_t s)
 int qmc_halton_plan_run(qmc_halton_plan *p, qmc_stream_t s)
 {
     QMC_REQUIRE(p && p->prepared, "null or unprepared plan (call qmc_halton_plan_prepare)");
-    const u64 tiles = p->P.r * ((p->P.n + 31) / 32);
-    halton_gen_kernel<<<qmcgb::grid_for(tiles, 1, (unsigned)qmcgb::sm_count() * 8), HT_THREADS, p->smem,
-                        QMC_STREAM(s)>>>(p->P);
+    const u64 tp = 32ull * p->ppl;
+    const u64 tiles = p->P.r * ((p->P.n + tp - 1) / tp);
+    const unsigned grid = qmcgb::grid_for(tiles, 1, (unsigned)qmcgb::sm_count() * 8);
+    if (p->ppl == 2)
+        halton_gen_kernel<2><<<grid, HT_THREADS, p->smem, QMC_STREAM(s)>>>(p->P);
+    else
+        halton_gen_kernel<1><<<grid, HT_THREADS, p->smem, QMC_STREAM(s)>>>(p->P);
     return qmcgb::launch_status("halton_gen_kernel");
 }
 

@@ -208,3 +208,13 @@ def test_halton_matrix_entry_above_32_bits_is_reported():
     dims[0]["C"][0, 0, 0, 0] = U(1 << 40)
     with pytest.raises(q._ffi.QmcError, match="2\\^32"):
         run_fused(1, 10, 0, dims)
+
+
+def test_halton_many_dimensions_one_point_per_lane():
+    """150 dimensions (bases up to 863): the output tile no longer fits two
+    points per lane, so the kernel runs one; same bits as the oracle."""
+    big_primes = [p for p in range(2, 900) if all(p % k for k in range(2, int(p ** 0.5) + 1))][:150]
+    rng = np.random.Generator(np.random.SFC64(150))
+    r, n, n_start = 1, 97, 31
+    dims = make_dims(rng, r, big_primes, n_start + n - 1)
+    assert same_bits(run_fused(r, n, n_start, dims), oracle_chain(r, n, n_start, dims))
