@@ -49,6 +49,23 @@ __device__ __forceinline__ DimInfo make_dim(u64 b)
     return di;
 }
 
+// x / d for 32-bit x and a divisor fixed for the launch (d >= 1): the high
+// word of the 64x32-bit product M*x with M = floor((2^64-1)/d) + 1
+struct Div32 {
+    u64 M;
+    u32 d;
+};
+
+__host__ __device__ inline Div32 div32_make(u32 d) { return Div32{fastdiv32_make(d).M, d}; }
+__device__ __forceinline__ Div32 div32_dev(u32 d) { return div32_make(d); }
+
+__device__ __forceinline__ u32 div32(const Div32 &v, u32 x)
+{
+    if (v.d == 1) return x;
+    const u64 lo = (u64)(u32)v.M * x;
+    return (u32)(((v.M >> 32) * x + (lo >> 32)) >> 32);
+}
+
 // C entry (k, t) of the current (l, j) block, read the way the reference
 // reads it (flat index), and recorded as an error when that index falls
 // outside the array.
@@ -71,19 +88,24 @@ __device__ u64 gdn_point_digit(const DimInfo &di, u64 itrue, const u64 *C, u64 c
         return 0;
     }
     if (di.small && itrue < (1ull << 32)) {
-        u32 x = (u32)itrue, acc = 0;
+        // The reference reduces after every digit; with digits below 2^16 and matrix entries
+        // below 2^32 each product is below 2^48 and the at most 32 products of a 32-bit index sum
+        // to below 2^53 without wrapping, so one reduction at the end gives the same digit.
+        u32 x = (u32)itrue;
+        const u32 b32 = (u32)di.b;
+        u64 acc = 0;
         bool ok = true;
         for (u64 k = 0; x; k++) {
             const u32 q = fd_div(di.fd, x);
-            const u32 dig = x - q * (u32)di.b;
+            const u32 dig = x - q * b32;
             x = q;
             if (dig) {
                 const u64 cv = read_flat(C, c_off + k * tmax + t, c_total, err);
                 if (cv >> 32) { ok = false; break; }
-                acc = fd_mod(di.fd, acc + dig * fd_mod(di.fd, (u32)cv));  // < b + b^2 < 2^32
+                acc += (u64)dig * cv;
             }
         }
-        if (ok) return acc;
+        if (ok) return acc < (1ull << 32) ? (u64)fd_mod(di.fd, (u32)acc) : acc % di.b;
     }
     const u64 b = di.b;
     u64 out = 0, icp = itrue;
@@ -99,7 +121,36 @@ __device__ u64 gdn_point_digit(const DimInfo &di, u64 itrue, const u64 *C, u64 c
 struct PointGrid {
     u64 rows_per_cta;
     u32 dim_tiles;
+    u32 narrow;  // rows_per_cta * (dims per tile * words per point) < 2^32: 32-bit index arithmetic
 };
+
+// (row within the CTA's run, dimension within the tile, word within the point) of run offset f
+struct RunPos {
+    u64 rr, t;
+    u32 c;
+};
+
+__device__ __forceinline__ RunPos run_pos(u64 f, bool narrow, const Div32 &dv_row, const Div32 &dv_t, u64 per_row,
+                                          u64 words)
+{
+    RunPos p;
+    if (narrow) {  // 32-bit index arithmetic by multiply-high (point_grid checked the range)
+        const u32 r32 = div32(dv_row, (u32)f), rem = (u32)f - r32 * (u32)per_row;
+        p.c = div32(dv_t, rem);
+        p.rr = r32;
+        p.t = rem - p.c * (u32)words;
+    } else {
+        p.rr = f / per_row;
+        const u64 rem = f - p.rr * per_row;
+        p.c = (u32)(rem / words);
+        p.t = rem - (u64)p.c * words;
+    }
+    return p;
+}
+
+// streaming kernels handle RUN_UNROLL elements per thread per iteration, all
+// loads issued before any is used (bytes in flight to cover HBM latency)
+constexpr u32 RUN_UNROLL = 4;
 
 __device__ __forceinline__ void point_block(const PointGrid &pg, u64 d, u64 &l, u64 &j0, u32 &nd)
 {
@@ -129,14 +180,167 @@ __global__ void __launch_bounds__(THREADS) gdn_gen_kernel(u64 r, u64 n, u64 d, u
     const u64 per_row = (u64)nd * tmax;
     const u64 total = rows * per_row;
     const u64 c_total = r * d * mmax * tmax;
+    u64 *out = xdig + l * n * d * tmax + row0 * d * tmax + j0 * tmax;
+    if (pg.narrow) {
+        // the CTA's run fits 32 bits (point_grid): index arithmetic by multiply-high
+        const Div32 dv_row = div32_dev((u32)per_row), dv_t = div32_dev((u32)tmax);  // this CTA's dimension count
+        for (u32 f = threadIdx.x; f < (u32)total; f += THREADS) {
+            const u32 rr = div32(dv_row, f), rem = f - rr * (u32)per_row;
+            const u32 c = div32(dv_t, rem), t = rem - c * (u32)tmax;
+            const u64 i = row0 + rr, j = j0 + c;
+            out[(u64)rr * d * tmax + rem] =
+                gdn_point_digit(dims[c], i + n_start, C, l * d * mmax * tmax + j * mmax * tmax, tmax, t, c_total, err);
+        }
+        return;
+    }
     for (u64 f = threadIdx.x; f < total; f += THREADS) {
         const u64 rr = f / per_row, rem = f - rr * per_row;
         const u32 c = (u32)(rem / tmax);
         const u64 t = rem - (u64)c * tmax;
         const u64 i = row0 + rr, j = j0 + c;
         const u64 c_off = l * d * mmax * tmax + j * mmax * tmax;
-        xdig[l * n * d * tmax + i * d * tmax + j * tmax + t] =
-            gdn_point_digit(dims[c], i + n_start, C, c_off, tmax, t, c_total, err);
+        out[rr * d * tmax + rem] = gdn_point_digit(dims[c], i + n_start, C, c_off, tmax, t, c_total, err);
+    }
+}
+
+// ---------------------------------------------------------------- tiled generation
+//
+// The common case of gdn_gen_natural (and _same_base): base in [2, 4096),
+// indices below 2^32, generating-matrix entries below 2^32, every index with
+// at most mmax base-b digits, mmax * tmax <= GT_MAX_CW, tmax <= GT_MAX_TMAX.
+// A CTA owns one (randomisation, dimension) and a run of 32-point groups; its
+// matrix, reduced mod b, sits in shared memory (with entries below 2^32 a
+// digit times an entry cannot wrap, so reducing first gives the reference's
+// digits).  Per group, the index splits as hi * b^K + lo with b^K >= 32: the
+// 32 points have at most two distinct hi, whose contributions to every
+// output digit the warp computes together; each lane adds its K low digits.
+// Digits are staged per 32-digit chunk in shared memory and written as
+// contiguous runs.  A CTA outside the case runs the per-element code above
+// for its block instead.
+constexpr u32 GT_MAX_CW = 8192;    // matrix words staged per CTA (32 KB as u32)
+constexpr u32 GT_MAX_TMAX = 256;
+constexpr u32 GT_WARPS = THREADS / 32;
+
+inline size_t gt_smem(u64 mmax, u64 tmax)
+{
+    return (mmax * tmax + GT_WARPS * 2 * tmax + GT_WARPS * 32 * 33) * sizeof(u32);
+}
+
+__global__ void __launch_bounds__(THREADS) gdn_gen_tiled_kernel(u64 r, u64 n, u64 d, u64 r_b, u64 mmax, u64 tmax,
+                                                                u64 n_start, const u64 *bases, u64 common_b,
+                                                                const u64 *C, u64 *xdig, u64 groups_per_cta,
+                                                                u64 unit_off, unsigned *err)
+{
+    extern __shared__ __align__(16) u32 gsm[];
+    u32 *Cs = gsm;                                  // [mmax][tmax] entries mod b
+    u32 *hi_tab = Cs + mmax * tmax;                 // [warp][2][tmax]
+    u32 *stage = hi_tab + GT_WARPS * 2 * tmax;      // [warp][32][33]
+    __shared__ u32 big;
+    const u64 unit = unit_off + blockIdx.y;         // = l * d + j
+    if (unit >= r * d) return;
+    const u64 l = unit / d, j = unit % d;
+    const u64 b = bases ? bases[(l % r_b) * d + j] : common_b;
+    const u64 g0 = (u64)blockIdx.x * groups_per_cta;
+    const u64 ngroups = (n + 31) / 32;
+    if (g0 >= ngroups) return;
+    const u64 g1 = min(ngroups, g0 + groups_per_cta);
+    const u64 c_total = r * d * mmax * tmax, c_off = l * d * mmax * tmax + j * mmax * tmax;
+    u64 *out = xdig + l * n * d * tmax + j * tmax;  // point i, digit t at out[i * d * tmax + t]
+    const u32 warp = threadIdx.x / 32, lane = threadIdx.x % 32;
+
+    // is this block in the tiled case?
+    bool tiled = b >= 2 && b < 4096 && n_start + n <= (1ull << 32);
+    if (tiled) {  // the last index has at most mmax base-b digits (else the reference reads past the block)
+        u64 x = n_start + n - 1, k = 0;
+        while (x) {
+            x /= b;
+            k++;
+        }
+        tiled = k <= mmax;
+    }
+    if (threadIdx.x == 0) big = 0;
+    __syncthreads();
+    if (tiled)
+        for (u32 w = threadIdx.x; w < mmax * tmax; w += THREADS) {
+            const u64 cv = C[c_off + w];
+            if (cv >> 32) big = 1;
+            Cs[w] = (u32)(cv % b);
+        }
+    __syncthreads();
+    if (!tiled || big) {
+        // the per-element code (reference order, 64-bit where needed), this CTA's points and dimension
+        __shared__ DimInfo di_s;
+        if (threadIdx.x == 0) di_s = make_dim(b);
+        __syncthreads();
+        const u64 i0 = g0 * 32, i1 = min(n, g1 * 32);
+        for (u64 f = threadIdx.x; f < (i1 - i0) * tmax; f += THREADS) {
+            const u64 i = i0 + f / tmax, t = f % tmax;
+            out[i * d * tmax + t] = gdn_point_digit(di_s, i + n_start, C, c_off, tmax, t, c_total, err);
+        }
+        return;
+    }
+    const u32 b32 = (u32)b, T = (u32)tmax, M = (u32)mmax;
+    const FastDiv32 fb = fastdiv32_make(b32);
+    u32 K = 1, bK = b32;
+    while (bK < 32) {
+        bK *= b32;
+        K++;
+    }
+    const FastDiv32 fK = fastdiv32_make(bK);
+    const u32 KL = K < M ? K : M;  // low digits that can be nonzero (indices below b^mmax)
+    u32 *ht = hi_tab + warp * 2 * T;
+    u32 *sg = stage + warp * 32 * 33;
+    for (u64 g = g0 + warp; g < g1; g += GT_WARPS) {
+        const u64 i0 = g * 32;
+        const u32 base = (u32)(n_start + i0);
+        const bool active = i0 + lane < n;
+        const u32 itrue = active ? base + lane : base;
+        const u32 h0 = fd_div(fK, base), hi = fd_div(fK, itrue);
+        const u32 sel = hi - h0;  // 0 or 1
+        u32 dl[5];
+        {
+            u32 x = itrue - hi * bK;
+#pragma unroll
+            for (u32 k = 0; k < 5; k++) {
+                const u32 q = fd_div(fb, x);
+                dl[k] = x - q * b32;
+                x = q;
+            }
+        }
+        // high-digit sums of both hi values for every output digit (gdn_gen_natural.c:37-50 for k >= K)
+        __syncwarp();
+        for (u32 t = lane; t < T; t += 32) {
+#pragma unroll
+            for (u32 s = 0; s < 2; s++) {
+                u32 h = h0 + s, acc = 0;
+                for (u32 k = K; h && k < M; k++) {
+                    const u32 q = fd_div(fb, h);
+                    acc += (h - q * b32) * Cs[k * T + t];  // < 64 * 4096^2 = 2^30
+                    h = q;
+                }
+                ht[s * T + t] = fd_mod(fb, acc);
+            }
+        }
+        __syncwarp();
+        const u32 npts = (u32)min((u64)32, n - i0);
+        for (u32 t0 = 0; t0 < T; t0 += 32) {
+            const u32 tw = min(32u, T - t0);
+            for (u32 tt = 0; tt < tw; tt++) {
+                const u32 t = t0 + tt;
+                u32 acc = ht[sel * T + t];
+#pragma unroll
+                for (u32 k = 0; k < 5; k++)
+                    if (k < KL) acc += dl[k] * Cs[k * T + t];  // < 4096 + 5 * 4096^2 < 2^27
+                sg[lane * 33 + tt] = fd_mod(fb, acc);
+            }
+            __syncwarp();
+            // the npts x tw block: contiguous runs of tw words per point
+            for (u32 e = lane; e < npts * tw; e += 32) {
+                const u32 p = e / tw, tt = e - p * tw;
+                out[(i0 + p) * d * tmax + t0 + tt] = sg[p * 33 + tt];
+            }
+            __syncwarp();
+        }
     }
 }
 
@@ -158,40 +362,84 @@ __global__ void __launch_bounds__(THREADS) gdn_shift_kernel(u64 r, u64 n, u64 d,
     const u64 rows = min(pg.rows_per_cta, n - row0);
     const u64 per_row = (u64)nd * tmax_new;
     const u64 total = rows * per_row;
-    for (u64 f = threadIdx.x; f < total; f += THREADS) {
-        const u64 rr = f / per_row, rem = f - rr * per_row;
-        const u32 c = (u32)(rem / tmax_new);
-        const u64 t = rem - (u64)c * tmax_new;
-        const u64 i = row0 + rr, j = j0 + c;
-        const u64 sh = shifts[l * d * tmax_new + j * tmax_new + t];
-        u64 v;
-        if (t < tmax) {
-            const u64 sum = xdig[(l % r_x) * n * d * tmax + i * d * tmax + j * tmax + t] + sh;  // wraps as in C
-            const DimInfo &di = dims[c];
-            if (di.b == 0) {
-                atomicOr(err, 2u);
-                v = 0;
-            } else {
-                v = (di.small && sum < (1ull << 32)) ? (u64)fd_mod(di.fd, (u32)sum) : sum % di.b;
-            }
-        } else {
-            v = sh;
+    const Div32 dv_row = div32_dev(pg.narrow ? (u32)per_row : 1u), dv_t = div32_dev(pg.narrow ? (u32)tmax_new : 1u);
+    for (u64 f0 = threadIdx.x; f0 < total; f0 += RUN_UNROLL * THREADS) {
+        RunPos ps[RUN_UNROLL];
+        u64 sh[RUN_UNROLL], xv[RUN_UNROLL];
+#pragma unroll
+        for (u32 u = 0; u < RUN_UNROLL; u++) {
+            const u64 f = f0 + u * THREADS;
+            sh[u] = xv[u] = 0;
+            if (f >= total) continue;
+            ps[u] = run_pos(f, pg.narrow, dv_row, dv_t, per_row, tmax_new);
+            const u64 i = row0 + ps[u].rr, j = j0 + ps[u].c;
+            sh[u] = shifts[l * d * tmax_new + j * tmax_new + ps[u].t];
+            if (ps[u].t < tmax) xv[u] = xdig[(l % r_x) * n * d * tmax + i * d * tmax + j * tmax + ps[u].t];
         }
-        xdig_new[l * n * d * tmax_new + i * d * tmax_new + j * tmax_new + t] = v;
+#pragma unroll
+        for (u32 u = 0; u < RUN_UNROLL; u++) {
+            const u64 f = f0 + u * THREADS;
+            if (f >= total) continue;
+            const u64 i = row0 + ps[u].rr, j = j0 + ps[u].c, t = ps[u].t;
+            u64 v;
+            if (t < tmax) {
+                const u64 sum = xv[u] + sh[u];  // wraps as in C
+                const DimInfo &di = dims[ps[u].c];
+                if (di.b == 0) {
+                    atomicOr(err, 2u);
+                    v = 0;
+                } else {
+                    v = (di.small && sum < (1ull << 32)) ? (u64)fd_mod(di.fd, (u32)sum) : sum % di.b;
+                }
+            } else {
+                v = sh[u];
+            }
+            xdig_new[l * n * d * tmax_new + i * d * tmax_new + j * tmax_new + t] = v;
+        }
     }
 }
 
 __global__ void __launch_bounds__(THREADS) gdn_perm_kernel(u64 r, u64 n, u64 d, u64 r_x, u64 tmax, u64 tmax_new,
                                                            u64 bmax, const u64 *perms, const u64 *xdig,
-                                                           u64 *xdig_new, unsigned *err)
+                                                           u64 *xdig_new, PointGrid pg, u64 l_off, unsigned *err)
 {
-    const u64 total = r * n * d * tmax_new, p_total = r * d * tmax_new * bmax;
-    for (u64 f = (u64)blockIdx.x * blockDim.x + threadIdx.x; f < total; f += (u64)gridDim.x * blockDim.x) {
-        const u64 t = f % tmax_new, j = (f / tmax_new) % d, i = (f / (tmax_new * d)) % n;
-        const u64 l = f / (tmax_new * d * n);
-        const u64 p = t < tmax ? xdig[(l % r_x) * n * d * tmax + i * d * tmax + j * tmax + t] : 0;
-        const u64 flat = l * d * tmax_new * bmax + j * tmax_new * bmax + t * bmax + p;
-        xdig_new[f] = read_flat(perms, flat, p_total, err);
+    u64 l, j0;
+    u32 nd;
+    point_block(pg, d, l, j0, nd);
+    l += l_off;
+    if (l >= r) return;
+    const u64 row0 = (u64)blockIdx.x * pg.rows_per_cta;
+    if (row0 >= n) return;
+    const u64 rows = min(pg.rows_per_cta, n - row0);
+    const u64 per_row = (u64)nd * tmax_new;
+    const u64 total = rows * per_row, p_total = r * d * tmax_new * bmax;
+    const Div32 dv_row = div32_dev(pg.narrow ? (u32)per_row : 1u), dv_t = div32_dev(pg.narrow ? (u32)tmax_new : 1u);
+    for (u64 f0 = threadIdx.x; f0 < total; f0 += RUN_UNROLL * THREADS) {
+        RunPos ps[RUN_UNROLL];
+        u64 pv[RUN_UNROLL];
+#pragma unroll
+        for (u32 u = 0; u < RUN_UNROLL; u++) {
+            const u64 f = f0 + u * THREADS;
+            pv[u] = 0;
+            if (f >= total) continue;
+            ps[u] = run_pos(f, pg.narrow, dv_row, dv_t, per_row, tmax_new);
+            const u64 i = row0 + ps[u].rr, j = j0 + ps[u].c;
+            if (ps[u].t < tmax) pv[u] = xdig[(l % r_x) * n * d * tmax + i * d * tmax + j * tmax + ps[u].t];
+        }
+#pragma unroll
+        for (u32 u = 0; u < RUN_UNROLL; u++) {
+            const u64 f = f0 + u * THREADS;
+            if (f >= total) continue;
+            const u64 flat = l * d * tmax_new * bmax + (j0 + ps[u].c) * tmax_new * bmax + ps[u].t * bmax + pv[u];
+            pv[u] = read_flat(perms, flat, p_total, err);
+        }
+#pragma unroll
+        for (u32 u = 0; u < RUN_UNROLL; u++) {
+            const u64 f = f0 + u * THREADS;
+            if (f >= total) continue;
+            const u64 i = row0 + ps[u].rr, j = j0 + ps[u].c;
+            xdig_new[l * n * d * tmax_new + i * d * tmax_new + j * tmax_new + ps[u].t] = pv[u];
+        }
     }
 }
 
@@ -213,20 +461,27 @@ __device__ __noinline__ u64 digit_step_hw(u64 v, double rc, u64 dg)
     return as_bits(__dadd_rn(as_double(v), __dmul_rn(rc, __ull2double_rn(dg))));
 }
 
-// v = sum_t recip_t * digit_t with the reference's rounding sequence
+// v = sum_t recip_t * digit_t with the reference's rounding sequence; the
+// digits are read four at a time (independent loads in flight)
 __device__ __forceinline__ double digits_to_double(const double *rc, const u64 *dig, u64 tmax)
 {
     u64 v = 0;  // bits of a non-negative double
-    for (u64 t = 0; t < tmax; t++) {
-        const u64 dg = dig[t];
-        if (dg == 0) continue;  // adds +0: v unchanged
-        const u64 rb = as_bits(rc[t]);
-        const u32 er = (u32)(rb >> 52);
-        if (dg < 2048 && er >= 1 && er < 2036 && ((v >> 52) < 2000)) {
-            const u64 p = dmul_small_bits(rb, (u32)dg);
-            v = dadd_pos_bits(v, p);
-        } else {
-            v = digit_step_hw(v, rc[t], dg);
+    for (u64 t0 = 0; t0 < tmax; t0 += 4) {
+        u64 dg4[4];
+#pragma unroll
+        for (u32 u = 0; u < 4; u++) dg4[u] = t0 + u < tmax ? dig[t0 + u] : 0;
+#pragma unroll
+        for (u32 u = 0; u < 4; u++) {
+            const u64 dg = dg4[u], t = t0 + u;
+            if (dg == 0) continue;  // adds +0: v unchanged (and past tmax)
+            const u64 rb = as_bits(rc[t]);
+            const u32 er = (u32)(rb >> 52);
+            if (dg < 2048 && er >= 1 && er < 2036 && ((v >> 52) < 2000)) {
+                const u64 p = dmul_small_bits(rb, (u32)dg);
+                v = dadd_pos_bits(v, p);
+            } else {
+                v = digit_step_hw(v, rc[t], dg);
+            }
         }
     }
     return as_double(v);
@@ -252,8 +507,9 @@ __global__ void __launch_bounds__(THREADS) gdn_to_float_kernel(u64 r, u64 n, u64
     if (row0 >= n) return;
     const u64 rows = min(rows_per_cta, n - row0);
     const u64 total = rows * nd;
+    const Div32 dv_nd = div32_dev(nd);
     for (u64 f = threadIdx.x; f < total; f += THREADS) {
-        const u64 rr = f / nd;
+        const u64 rr = total < (1ull << 32) ? (u64)div32(dv_nd, (u32)f) : f / nd;
         const u32 c = (u32)(f - rr * nd);
         const u64 i = row0 + rr, j = j0 + c;
         const u64 *dg = xdig + l * n * d * tmax + i * d * tmax + j * tmax;
@@ -354,6 +610,7 @@ PointGrid point_grid(u64 r, u64 n, u64 d, u64 per_point, u32 dim_tile, u64 *spli
     if (splits < 1) splits = 1;
     pg.rows_per_cta = (n + splits - 1) / splits;
     *splits_out = splits;
+    pg.narrow = per_row < (1ull << 32) && pg.rows_per_cta * per_row < (1ull << 32) ? 1u : 0u;
     return pg;
 }
 
@@ -370,6 +627,34 @@ int launch_points(u64 r, u32 dim_tiles, F &&launch_chunk, const char *what)
     return QMC_OK;
 }
 
+// grid of the tiled generation: y = (randomisation, dimension) units in chunks of 65535, x = runs of
+// 32-point groups sized so the whole launch has about 8 CTAs per SM
+int gen_tiled(u64 r, u64 n, u64 d, u64 r_b, u64 mmax, u64 tmax, u64 n_start, const u64 *bases, u64 common_b,
+              const u64 *C, u64 *xdig, cudaStream_t st, unsigned *err, const char *what)
+{
+    const u64 units = r * d, ngroups = (n + 31) / 32;
+    const u64 want = (u64)qmcgb::sm_count() * 8;
+    u64 splits = (want + units - 1) / units;
+    if (splits > ngroups) splits = ngroups;
+    if (splits < 1) splits = 1;
+    const u64 groups_per_cta = (ngroups + splits - 1) / splits;
+    const u64 nx = (ngroups + groups_per_cta - 1) / groups_per_cta;
+    const size_t smem = gt_smem(mmax, tmax);
+    if (smem > 48 * 1024) {
+        if (int rc = qmcgb::cuda_status(cudaFuncSetAttribute(gdn_gen_tiled_kernel,
+                                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
+                                        what))
+            return rc;
+    }
+    for (u64 u0 = 0; u0 < units; u0 += 65535) {
+        const unsigned cnt = (unsigned)(units - u0 < 65535 ? units - u0 : 65535);
+        gdn_gen_tiled_kernel<<<dim3((unsigned)nx, cnt, 1), THREADS, smem, st>>>(
+            r, n, d, r_b, mmax, tmax, n_start, bases, common_b, C, xdig, groups_per_cta, u0, err);
+        if (int rc = qmcgb::launch_status(what)) return rc;
+    }
+    return QMC_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -381,6 +666,9 @@ int qmc_gdn_gen_natural(uint64_t r, uint64_t n, uint64_t d, uint64_t r_b, uint64
     QMC_REQUIRE(r_b > 0 && bases && C && xdig, "bad r_b or null array pointer");
     unsigned *err = qmcgb::device_error_ptr();
     QMC_REQUIRE(err, "device error word unavailable");
+    if (mmax * tmax <= GT_MAX_CW && tmax <= GT_MAX_TMAX)
+        return gen_tiled(r, n, d, r_b, mmax, tmax, n_start, (const u64 *)bases, 0, (const u64 *)C, (u64 *)xdig,
+                         QMC_STREAM(s), err, "gdn_gen_natural");
     u64 splits;
     const PointGrid pg = point_grid(r, n, d, tmax, DIM_TILE, &splits);
     return launch_points(r, pg.dim_tiles, [&](u64 l0, unsigned cnt) {
@@ -398,6 +686,9 @@ int qmc_gdn_gen_natural_same_base(uint64_t r, uint64_t n, uint64_t d, uint64_t m
                        (unsigned long long)b);
     unsigned *err = qmcgb::device_error_ptr();
     QMC_REQUIRE(err, "device error word unavailable");
+    if (mmax * tmax <= GT_MAX_CW && tmax <= GT_MAX_TMAX)
+        return gen_tiled(r, n, d, 1, mmax, tmax, n_start, nullptr, b, (const u64 *)C, (u64 *)xdig, QMC_STREAM(s), err,
+                         "gdn_gen_natural_same_base");
     u64 splits;
     const PointGrid pg = point_grid(r, n, d, tmax, DIM_TILE, &splits);
     return launch_points(r, pg.dim_tiles, [&](u64 l0, unsigned cnt) {
@@ -431,10 +722,12 @@ int qmc_gdn_digital_permutation(uint64_t r, uint64_t n, uint64_t d, uint64_t r_x
     QMC_REQUIRE(r_x > 0 && perms && xdig_new && (tmax == 0 || xdig), "bad r_x or null array pointer");
     unsigned *err = qmcgb::device_error_ptr();
     QMC_REQUIRE(err, "device error word unavailable");
-    gdn_perm_kernel<<<flat_grid(total), 256, 0, QMC_STREAM(s)>>>(r, n, d, r_x, tmax, tmax_new, bmax,
-                                                                 (const u64 *)perms, (const u64 *)xdig,
-                                                                 (u64 *)xdig_new, err);
-    return qmcgb::launch_status("gdn_digital_permutation");
+    u64 splits;
+    const PointGrid pg = point_grid(r, n, d, tmax_new, DIM_TILE, &splits);
+    return launch_points(r, pg.dim_tiles, [&](u64 l0, unsigned cnt) {
+        gdn_perm_kernel<<<dim3((unsigned)splits, cnt, 1), THREADS, 0, QMC_STREAM(s)>>>(
+            r, n, d, r_x, tmax, tmax_new, bmax, (const u64 *)perms, (const u64 *)xdig, (u64 *)xdig_new, pg, l0, err);
+    }, "gdn_digital_permutation");
 }
 
 int qmc_gdn_digital_shift(uint64_t r, uint64_t n, uint64_t d, uint64_t r_x, uint64_t r_b, uint64_t tmax,
