@@ -20,9 +20,11 @@
 // Digits to float.  The reference sums recip_t*digit_t with recip_0 = 1/b
 // and recip_{t+1} = recip_t/b, every operation rounded separately.  The
 // recip_t depend only on (b, t): each CTA computes them once per dimension
-// into shared memory.  The per-digit multiply and add are emulated with
-// integer operations (dmul_small_bits, dadd_pos_bits) so the FP64 unit,
-// slow on GB300, is not on the per-digit path.
+// into shared memory.  The per-digit multiply and add are the FP64
+// operations themselves (__dmul_rn, __dadd_rn): their integer emulation
+// (dmul_small_bits, dadd_pos_bits) measured about a hundred ALU instructions
+// per digit with the ALU pipe 91% busy, while two FP64 operations per digit
+// leave this kernel bound by HBM reads.
 //
 // Layout in HBM: xdig is r*n*d*tmax (digit t fastest), C is r*d*mmax*tmax,
 // S is r*d*tmax_new*tmax, perms r*d*tmax_new*bmax.  Per-point kernels walk
@@ -347,7 +349,7 @@ __global__ void __launch_bounds__(THREADS) gdn_gen_tiled_kernel(u64 r, u64 n, u6
 __global__ void __launch_bounds__(THREADS) gdn_shift_kernel(u64 r, u64 n, u64 d, u64 r_x, u64 r_b, u64 tmax,
                                                             u64 tmax_new, const u64 *bases, const u64 *shifts,
                                                             const u64 *xdig, u64 *xdig_new, PointGrid pg,
-                                                            u64 l_off, unsigned *err)
+                                                            u64 l_off, u32 lin, unsigned *err)
 {
     __shared__ DimInfo dims[DIM_TILE];
     u64 l, j0;
@@ -363,6 +365,75 @@ __global__ void __launch_bounds__(THREADS) gdn_shift_kernel(u64 r, u64 n, u64 d,
     const u64 per_row = (u64)nd * tmax_new;
     const u64 total = rows * per_row;
     const Div32 dv_row = div32_dev(pg.narrow ? (u32)per_row : 1u), dv_t = div32_dev(pg.narrow ? (u32)tmax_new : 1u);
+    if (lin == 1) {
+        // host-checked: the tile holds every dimension, tmax == tmax_new, per_row even, arrays 16-byte
+        // aligned, the run below 2^32 words: input and output are contiguous runs, read and written
+        // two words at a time; word f of the run is digit sidx = f mod per_row of its point
+        const ulonglong2 *src = (const ulonglong2 *)(xdig + (l % r_x) * n * d * tmax + row0 * per_row);
+        ulonglong2 *dst = (ulonglong2 *)(xdig_new + l * n * d * tmax + row0 * per_row);
+        const u64 *shl = shifts + l * per_row;
+        const u32 npair = (u32)(total / 2);
+        for (u32 q0 = threadIdx.x; q0 < npair; q0 += RUN_UNROLL * THREADS) {
+            ulonglong2 xv[RUN_UNROLL];
+#pragma unroll
+            for (u32 u = 0; u < RUN_UNROLL; u++) {
+                const u32 q = q0 + u * THREADS;
+                if (q < npair) xv[u] = src[q];
+            }
+#pragma unroll
+            for (u32 u = 0; u < RUN_UNROLL; u++) {
+                const u32 q = q0 + u * THREADS;
+                if (q >= npair) continue;
+                const u32 sidx = 2 * q - div32(dv_row, 2 * q) * (u32)per_row;  // even, sidx + 1 < per_row
+                u64 v[2];
+#pragma unroll
+                for (u32 h = 0; h < 2; h++) {
+                    const u32 c = div32(dv_t, sidx + h);
+                    const u64 sum = (h ? xv[u].y : xv[u].x) + shl[sidx + h];  // wraps as in C
+                    const DimInfo &di = dims[c];
+                    if (di.b == 0) {
+                        atomicOr(err, 2u);
+                        v[h] = 0;
+                    } else {
+                        v[h] = (di.small && sum < (1ull << 32)) ? (u64)fd_mod(di.fd, (u32)sum) : sum % di.b;
+                    }
+                }
+                dst[q] = make_ulonglong2(v[0], v[1]);
+            }
+        }
+        return;
+    }
+    if (lin == 2) {
+        // contiguous runs read and written one word at a time (odd words per point or unaligned arrays)
+        const u64 *src = xdig + (l % r_x) * n * d * tmax + row0 * per_row;
+        u64 *dst = xdig_new + l * n * d * tmax + row0 * per_row;
+        const u64 *shl = shifts + l * per_row;
+        for (u32 f0 = threadIdx.x; f0 < (u32)total; f0 += RUN_UNROLL * THREADS) {
+            u64 xv[RUN_UNROLL];
+#pragma unroll
+            for (u32 u = 0; u < RUN_UNROLL; u++) {
+                const u32 f = f0 + u * THREADS;
+                if (f < (u32)total) xv[u] = src[f];
+            }
+#pragma unroll
+            for (u32 u = 0; u < RUN_UNROLL; u++) {
+                const u32 f = f0 + u * THREADS;
+                if (f >= (u32)total) continue;
+                const u32 sidx = f - div32(dv_row, f) * (u32)per_row;
+                const u64 sum = xv[u] + shl[sidx];  // wraps as in C
+                const DimInfo &di = dims[div32(dv_t, sidx)];
+                u64 v;
+                if (di.b == 0) {
+                    atomicOr(err, 2u);
+                    v = 0;
+                } else {
+                    v = (di.small && sum < (1ull << 32)) ? (u64)fd_mod(di.fd, (u32)sum) : sum % di.b;
+                }
+                dst[f] = v;
+            }
+        }
+        return;
+    }
     for (u64 f0 = threadIdx.x; f0 < total; f0 += RUN_UNROLL * THREADS) {
         RunPos ps[RUN_UNROLL];
         u64 sh[RUN_UNROLL], xv[RUN_UNROLL];
@@ -401,7 +472,8 @@ __global__ void __launch_bounds__(THREADS) gdn_shift_kernel(u64 r, u64 n, u64 d,
 
 __global__ void __launch_bounds__(THREADS) gdn_perm_kernel(u64 r, u64 n, u64 d, u64 r_x, u64 tmax, u64 tmax_new,
                                                            u64 bmax, const u64 *perms, const u64 *xdig,
-                                                           u64 *xdig_new, PointGrid pg, u64 l_off, unsigned *err)
+                                                           u64 *xdig_new, PointGrid pg, u64 l_off, u32 lin,
+                                                           unsigned *err)
 {
     u64 l, j0;
     u32 nd;
@@ -414,6 +486,63 @@ __global__ void __launch_bounds__(THREADS) gdn_perm_kernel(u64 r, u64 n, u64 d, 
     const u64 per_row = (u64)nd * tmax_new;
     const u64 total = rows * per_row, p_total = r * d * tmax_new * bmax;
     const Div32 dv_row = div32_dev(pg.narrow ? (u32)per_row : 1u), dv_t = div32_dev(pg.narrow ? (u32)tmax_new : 1u);
+    if (lin == 1) {
+        // host-checked as in gdn_shift_kernel: contiguous runs, two words at a time; the table row of
+        // digit sidx of the point starts at (l * d * tmax + sidx) * bmax
+        const ulonglong2 *src = (const ulonglong2 *)(xdig + (l % r_x) * n * d * tmax + row0 * per_row);
+        ulonglong2 *dst = (ulonglong2 *)(xdig_new + l * n * d * tmax + row0 * per_row);
+        const u64 prow0 = l * per_row * bmax;
+        const u32 npair = (u32)(total / 2);
+        for (u32 q0 = threadIdx.x; q0 < npair; q0 += RUN_UNROLL * THREADS) {
+            ulonglong2 xv[RUN_UNROLL];
+#pragma unroll
+            for (u32 u = 0; u < RUN_UNROLL; u++) {
+                const u32 q = q0 + u * THREADS;
+                if (q < npair) xv[u] = src[q];
+            }
+#pragma unroll
+            for (u32 u = 0; u < RUN_UNROLL; u++) {
+                const u32 q = q0 + u * THREADS;
+                if (q >= npair) continue;
+                const u32 sidx = 2 * q - div32(dv_row, 2 * q) * (u32)per_row;
+                xv[u].x = read_flat(perms, prow0 + (u64)sidx * bmax + xv[u].x, p_total, err);
+                xv[u].y = read_flat(perms, prow0 + (u64)(sidx + 1) * bmax + xv[u].y, p_total, err);
+            }
+#pragma unroll
+            for (u32 u = 0; u < RUN_UNROLL; u++) {
+                const u32 q = q0 + u * THREADS;
+                if (q < npair) dst[q] = xv[u];
+            }
+        }
+        return;
+    }
+    if (lin == 2) {
+        // contiguous runs one word at a time (odd words per point or unaligned arrays)
+        const u64 *src = xdig + (l % r_x) * n * d * tmax + row0 * per_row;
+        u64 *dst = xdig_new + l * n * d * tmax + row0 * per_row;
+        const u64 prow0 = l * per_row * bmax;
+        for (u32 f0 = threadIdx.x; f0 < (u32)total; f0 += RUN_UNROLL * THREADS) {
+            u64 xv[RUN_UNROLL];
+#pragma unroll
+            for (u32 u = 0; u < RUN_UNROLL; u++) {
+                const u32 f = f0 + u * THREADS;
+                if (f < (u32)total) xv[u] = src[f];
+            }
+#pragma unroll
+            for (u32 u = 0; u < RUN_UNROLL; u++) {
+                const u32 f = f0 + u * THREADS;
+                if (f >= (u32)total) continue;
+                const u32 sidx = f - div32(dv_row, f) * (u32)per_row;
+                xv[u] = read_flat(perms, prow0 + (u64)sidx * bmax + xv[u], p_total, err);
+            }
+#pragma unroll
+            for (u32 u = 0; u < RUN_UNROLL; u++) {
+                const u32 f = f0 + u * THREADS;
+                if (f < (u32)total) dst[f] = xv[u];
+            }
+        }
+        return;
+    }
     for (u64 f0 = threadIdx.x; f0 < total; f0 += RUN_UNROLL * THREADS) {
         RunPos ps[RUN_UNROLL];
         u64 pv[RUN_UNROLL];
@@ -461,28 +590,53 @@ __device__ __noinline__ u64 digit_step_hw(u64 v, double rc, u64 dg)
     return as_bits(__dadd_rn(as_double(v), __dmul_rn(rc, __ull2double_rn(dg))));
 }
 
+// (double)dg for dg < 2^53 (exact), built in integer arithmetic
+__device__ __forceinline__ double small_u64_to_double(u64 dg)
+{
+    if (dg == 0) return 0.0;
+    const u32 lz = (u32)__clzll((long long)dg);
+    return as_double(((u64)(1086 - lz) << 52) + ((dg << lz) >> 11) - (1ull << 52));
+}
+
+// one term of the sum: v = RN(v + RN(recip * digit)), the FP64 operations of
+// gdn_integer_to_float.c:36-37 (the integer emulation of dmul_small_bits /
+// dadd_pos_bits costs about a hundred ALU instructions per digit, and in this
+// kernel the ALU pipe, not the FP64 pipe, is the bottleneck)
+__device__ __forceinline__ u64 digit_term(u64 v, double rc, u64 dg)
+{
+    if (dg == 0) return v;  // adds +0: v unchanged
+    if (dg >> 53) return digit_step_hw(v, rc, dg);
+    return as_bits(__dadd_rn(as_double(v), __dmul_rn(rc, small_u64_to_double(dg))));
+}
+
 // v = sum_t recip_t * digit_t with the reference's rounding sequence; the
-// digits are read four at a time (independent loads in flight)
+// digits are read eight at a time (16-byte loads when the run is 16-byte
+// aligned and of even length), independent loads in flight
 __device__ __forceinline__ double digits_to_double(const double *rc, const u64 *dig, u64 tmax)
 {
     u64 v = 0;  // bits of a non-negative double
+    if ((tmax & 1) == 0 && ((uintptr_t)dig & 15) == 0) {
+        const ulonglong2 *d2 = (const ulonglong2 *)dig;
+        for (u64 t0 = 0; t0 < tmax; t0 += 8) {
+            ulonglong2 q[4];
+#pragma unroll
+            for (u32 u = 0; u < 4; u++) q[u] = t0 + 2 * u < tmax ? d2[t0 / 2 + u] : make_ulonglong2(0, 0);
+#pragma unroll
+            for (u32 u = 0; u < 4; u++) {
+                if (t0 + 2 * u >= tmax) break;
+                v = digit_term(v, rc[t0 + 2 * u], q[u].x);
+                v = digit_term(v, rc[t0 + 2 * u + 1], q[u].y);
+            }
+        }
+        return as_double(v);
+    }
     for (u64 t0 = 0; t0 < tmax; t0 += 4) {
         u64 dg4[4];
 #pragma unroll
         for (u32 u = 0; u < 4; u++) dg4[u] = t0 + u < tmax ? dig[t0 + u] : 0;
 #pragma unroll
-        for (u32 u = 0; u < 4; u++) {
-            const u64 dg = dg4[u], t = t0 + u;
-            if (dg == 0) continue;  // adds +0: v unchanged (and past tmax)
-            const u64 rb = as_bits(rc[t]);
-            const u32 er = (u32)(rb >> 52);
-            if (dg < 2048 && er >= 1 && er < 2036 && ((v >> 52) < 2000)) {
-                const u64 p = dmul_small_bits(rb, (u32)dg);
-                v = dadd_pos_bits(v, p);
-            } else {
-                v = digit_step_hw(v, rc[t], dg);
-            }
-        }
+        for (u32 u = 0; u < 4; u++)
+            if (t0 + u < tmax) v = digit_term(v, rc[t0 + u], dg4[u]);
     }
     return as_double(v);
 }
@@ -627,6 +781,15 @@ int launch_points(u64 r, u32 dim_tiles, F &&launch_chunk, const char *what)
     return QMC_OK;
 }
 
+// the digit-wise kernels' contiguous-run form: 0 = no (several dimension tiles, digit counts that
+// differ, runs of 2^32 words or more), 1 = pairs of words (an even number of words per point,
+// 16-byte aligned arrays), 2 = single words
+u32 linear_run(const PointGrid &pg, u64 d, u64 tmax, u64 tmax_new, const void *in, const void *out)
+{
+    if (!(pg.narrow && pg.dim_tiles == 1 && d <= DIM_TILE && tmax == tmax_new)) return 0u;
+    return (d * tmax) % 2 == 0 && (((uintptr_t)in | (uintptr_t)out) & 15) == 0 ? 1u : 2u;
+}
+
 // grid of the tiled generation: y = (randomisation, dimension) units in chunks of 65535, x = runs of
 // 32-point groups sized so the whole launch has about 8 CTAs per SM
 int gen_tiled(u64 r, u64 n, u64 d, u64 r_b, u64 mmax, u64 tmax, u64 n_start, const u64 *bases, u64 common_b,
@@ -724,9 +887,11 @@ int qmc_gdn_digital_permutation(uint64_t r, uint64_t n, uint64_t d, uint64_t r_x
     QMC_REQUIRE(err, "device error word unavailable");
     u64 splits;
     const PointGrid pg = point_grid(r, n, d, tmax_new, DIM_TILE, &splits);
+    const u32 lin = linear_run(pg, d, tmax, tmax_new, xdig, xdig_new);
     return launch_points(r, pg.dim_tiles, [&](u64 l0, unsigned cnt) {
         gdn_perm_kernel<<<dim3((unsigned)splits, cnt, 1), THREADS, 0, QMC_STREAM(s)>>>(
-            r, n, d, r_x, tmax, tmax_new, bmax, (const u64 *)perms, (const u64 *)xdig, (u64 *)xdig_new, pg, l0, err);
+            r, n, d, r_x, tmax, tmax_new, bmax, (const u64 *)perms, (const u64 *)xdig, (u64 *)xdig_new, pg, l0, lin,
+            err);
     }, "gdn_digital_permutation");
 }
 
@@ -741,10 +906,11 @@ int qmc_gdn_digital_shift(uint64_t r, uint64_t n, uint64_t d, uint64_t r_x, uint
     QMC_REQUIRE(err, "device error word unavailable");
     u64 splits;
     const PointGrid pg = point_grid(r, n, d, tmax_new, DIM_TILE, &splits);
+    const u32 lin = linear_run(pg, d, tmax, tmax_new, xdig, xdig_new);
     return launch_points(r, pg.dim_tiles, [&](u64 l0, unsigned cnt) {
         gdn_shift_kernel<<<dim3((unsigned)splits, cnt, 1), THREADS, 0, QMC_STREAM(s)>>>(
             r, n, d, r_x, r_b, tmax, tmax_new, (const u64 *)bases, (const u64 *)shifts, (const u64 *)xdig,
-            (u64 *)xdig_new, pg, l0, err);
+            (u64 *)xdig_new, pg, l0, lin, err);
     }, "gdn_digital_shift");
 }
 
