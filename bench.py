@@ -952,7 +952,80 @@ def run_halton(args):
                              "seconds": t_cpu}}
 
 
-WORKLOADS = {"net_plain": run_net_plain, "net_lms": run_net_lms, "fft": run_fft, "halton": run_halton}
+def run_gdn_plain(args):
+    """The plain drop-in generalized-net functions, one call each through the
+    C ABI, at the per-dimension shape of the randomised Halton workload
+    (r=32, n=2^18, d=1, tmax = ceil(64/log2 b), mmax = ceil(18/log2 b)) for
+    bases 2, 3 and 541: gdn_linear_matrix_scramble -> gdn_gen_natural ->
+    gdn_digital_permutation -> gdn_digital_shift -> gdn_integer_to_float,
+    each timed alone with its HBM bytes (digits are u64 words)."""
+    import math
+    import torch
+    import qmctoolscl_gb300 as q
+    from qmctoolscl_gb300 import _ffi
+    lib = _ffi.lib()
+    r, n = 32, 1 << 18
+    st = torch.cuda.current_stream()
+    h = st.cuda_stream
+    U = np.uint64
+    peak, _src = measured_peak()
+    res, total_ms = {}, 0.0
+    for b in (2, 3, 541):
+        tmax, mmax = math.ceil(64 / math.log2(b)), math.ceil(18 / math.log2(b))
+        rng = np.random.Generator(np.random.SFC64(b))
+        bb = np.array([[b]], U)
+        C = np.ascontiguousarray(q.gdn_get_halton_generating_matrix(1, 1, max(mmax, tmax))[:, :, :mmax, :tmax])
+        S = q.gdn_get_linear_scramble_matrix(rng, r, 1, tmax, tmax, 1, bb)
+        P = q.gdn_get_digital_permutations(rng, r, 1, tmax, 1, bb)
+        H = q.gdn_get_digital_shifts(rng, r, 1, tmax, 1, bb)
+        Cd, Sd, Pd, Hd, bd = dev_tensor(C), dev_tensor(S), dev_tensor(P), dev_tensor(H), dev_tensor(bb)
+        Cl = torch.empty(r * mmax * tmax, dtype=torch.int64, device="cuda")
+        xd = torch.empty(r * n * tmax, dtype=torch.int64, device="cuda")
+        xp, xs = torch.empty_like(xd), torch.empty_like(xd)
+        x = torch.empty(r * n, dtype=torch.float64, device="cuda")
+        calls = {
+            "gdn_linear_matrix_scramble": lambda: lib.qmc_gdn_linear_matrix_scramble(
+                r, 1, mmax, 1, 1, tmax, tmax, bd.data_ptr(), Sd.data_ptr(), Cd.data_ptr(), Cl.data_ptr(), h),
+            "gdn_gen_natural": lambda: lib.qmc_gdn_gen_natural(r, n, 1, 1, mmax, tmax, 0, bd.data_ptr(), Cl.data_ptr(),
+                                                               xd.data_ptr(), h),
+            "gdn_digital_permutation": lambda: lib.qmc_gdn_digital_permutation(
+                r, n, 1, r, 1, tmax, tmax, b, Pd.data_ptr(), xd.data_ptr(), xp.data_ptr(), h),
+            "gdn_digital_shift": lambda: lib.qmc_gdn_digital_shift(r, n, 1, r, 1, tmax, tmax, bd.data_ptr(),
+                                                                   Hd.data_ptr(), xp.data_ptr(), xs.data_ptr(), h),
+            "gdn_integer_to_float": lambda: lib.qmc_gdn_integer_to_float(r, n, 1, 1, tmax, bd.data_ptr(),
+                                                                         xs.data_ptr(), x.data_ptr(), h),
+        }
+        words = 8.0 * r * n * tmax
+        alg = {"gdn_linear_matrix_scramble": 8.0 * r * mmax * tmax, "gdn_gen_natural": words,
+               "gdn_digital_permutation": 2 * words, "gdn_digital_shift": 2 * words,
+               "gdn_integer_to_float": words + 8.0 * r * n}
+        per = {}
+        for name, fn in calls.items():
+            _ffi.check(fn(), name)
+        for name, fn in calls.items():
+            ms = gpu_ms(fn, args.steps, args.warmup, st)
+            per[name] = {"ms": ms, "alg_bytes": alg[name], "gbs": alg[name] / (ms / 1e3) / 1e9,
+                         "frac": alg[name] / (ms / 1e3) / 1e9 / peak}
+            total_ms += ms
+        # bit-exact: the last randomisation's first 1024 points against the oracle chain
+        want = halton_oracle([dict(b=b, tmax=tmax, mmax=mmax, C=C, S=S, perms=P, shifts=H)], r - 1, 0, 1024)
+        got = x.view(r, n)[r - 1, :1024].cpu().numpy()
+        assert np.array_equal(got.view(U), want[:, 0].view(U)), "plain gdn chain differs from the oracle"
+        res["b=%d (tmax=%d, mmax=%d)" % (b, tmax, mmax)] = per
+    pts = 3 * r * n
+    return {"metric": METRIC, "value": pts / (total_ms / 1e3), "unit": "points/s (one dimension per base)",
+            "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u64 digits, f64",
+            "data": "synthetic (np.random.SFC64(b)): reference generators",
+            "config": {"workload": "plain gdn chain per dimension, r=32, n=2^18, d=1, bases 2, 3, 541",
+                       "l2": "digit arrays 0.5-4.3 GB >> 129 MB L2"},
+            "roofline": dict(roofline(sum(v["alg_bytes"] for p_ in res.values() for v in p_.values()), total_ms),
+                             kernel="the five plain gdn kernels, all bases"),
+            "kernels": res, "gpu_launches": 15 * args.steps}
+
+
+WORKLOADS = {"net_plain": run_net_plain, "net_lms": run_net_lms, "fft": run_fft, "halton": run_halton,
+             "gdn_plain": run_gdn_plain}
 
 
 def main():
