@@ -1012,20 +1012,81 @@ def run_gdn_plain(args):
         got = x.view(r, n)[r - 1, :1024].cpu().numpy()
         assert np.array_equal(got.view(U), want[:, 0].view(U)), "plain gdn chain differs from the oracle"
         res["b=%d (tmax=%d, mmax=%d)" % (b, tmax, mmax)] = per
+    gdn_ms = total_ms
+    # the other plain families at their benchmark shapes: base-2 nets (r=64, n=2^20, d=32, from the
+    # LMS + interlacing inputs) and rank-1 lattices (r=16, n=2^20, d=64)
+    rng3 = np.random.Generator(np.random.SFC64(3))
+    r3, d_pre, alpha, m, C3, S3, sh3 = cfg3_uniform_inputs(rng3)
+    d3, n3 = d_pre // alpha, 1 << m
+    C3d, S3d, sh3d = dev_tensor(C3), dev_tensor(S3), dev_tensor(sh3)
+    lsh, tms = dev_tensor(np.zeros(r3, U)), dev_tensor(np.full(r3, 64, U))
+    C_lms = torch.empty(r3 * d_pre * m, dtype=torch.int64, device="cuda")
+    C_a = torch.empty(r3 * d3 * m, dtype=torch.int64, device="cuda")
+    xb = torch.empty(r3 * n3 * d3, dtype=torch.int64, device="cuda")
+    xrb, xf = torch.empty_like(xb), torch.empty(r3 * n3 * d3, dtype=torch.float64, device="cuda")
+    w3 = 8.0 * r3 * n3 * d3
+    g2, s2 = workload_inputs()
+    g2d, s2d = dev_tensor(g2), torch.from_numpy(s2).cuda()
+    xl = torch.empty(R * (1 << LOG2N) * D, dtype=torch.float64, device="cuda")
+    xlr = torch.empty_like(xl)
+    w2, n2 = 8.0 * R * (1 << LOG2N) * D, 1 << LOG2N
+    other = [
+        ("dnb2_linear_matrix_scramble", lambda: lib.qmc_dnb2_linear_matrix_scramble(
+            r3, d_pre, m, 1, 64, S3d.data_ptr(), C3d.data_ptr(), C_lms.data_ptr(), h), 8.0 * r3 * d_pre * m),
+        ("dnb2_interlace", lambda: lib.qmc_dnb2_interlace(r3, d3, m, d_pre, 64, 64, alpha, C_lms.data_ptr(),
+                                                          C_a.data_ptr(), h), 8.0 * r3 * d3 * m),
+        ("dnb2_gen_natural", lambda: lib.qmc_dnb2_gen_natural(r3, n3, d3, 0, m, C_a.data_ptr(), xb.data_ptr(), h), w3),
+        ("dnb2_gen_gray", lambda: lib.qmc_dnb2_gen_gray(r3, n3, d3, 0, m, C_a.data_ptr(), xb.data_ptr(), h), w3),
+        ("dnb2_digital_shift", lambda: lib.qmc_dnb2_digital_shift(r3, n3, d3, r3, lsh.data_ptr(), xb.data_ptr(),
+                                                                  sh3d.data_ptr(), xrb.data_ptr(), h), 2 * w3),
+        ("dnb2_integer_to_float", lambda: lib.qmc_dnb2_integer_to_float(r3, n3, d3, tms.data_ptr(), xrb.data_ptr(),
+                                                                        xf.data_ptr(), h), 2 * w3),
+        ("lat_gen_gray", lambda: lib.qmc_lat_gen_gray(R, n2, D, 0, g2d.data_ptr(), xl.data_ptr(), h), w2),
+        ("lat_gen_natural", lambda: lib.qmc_lat_gen_natural(R, n2, D, 0, g2d.data_ptr(), xl.data_ptr(), h), w2),
+        ("lat_gen_linear", lambda: lib.qmc_lat_gen_linear(R, n2, D, g2d.data_ptr(), xl.data_ptr(), h), w2),
+        ("lat_shift_mod_1", lambda: lib.qmc_lat_shift_mod_1(R, n2, D, R, xl.data_ptr(), s2d.data_ptr(),
+                                                            xlr.data_ptr(), h), 2 * w2),
+    ]
+    fam = {}
+    for name, fn, by in other:
+        _ffi.check(fn(), name)
+        ms = gpu_ms(fn, args.steps, args.warmup, st)
+        fam[name] = {"ms": ms, "alg_bytes": by, "gbs": by / (ms / 1e3) / 1e9, "frac": by / (ms / 1e3) / 1e9 / peak}
+    # parity of the last outputs: base-2 net and lattice slices against the oracle
+    import oracle
+    nn = 1 << 10
+    ob = np.empty((1, nn, d3), U)
+    Cl = np.empty((1, d_pre, m), U)
+    oracle.call("dnb2_linear_matrix_scramble", U(1), U(d_pre), U(m), U(1), U(64), np.ascontiguousarray(S3[:1]), C3, Cl)
+    Ca = np.empty((1, d3, m), U)
+    oracle.call("dnb2_interlace", U(1), U(d3), U(m), U(d_pre), U(64), U(64), U(alpha), Cl, Ca)
+    oracle.call("dnb2_gen_gray", U(1), U(nn), U(d3), U(0), U(m), Ca, ob)
+    assert np.array_equal(xb[:nn * d3].cpu().numpy().view(U), ob.reshape(-1)), "dnb2 plain differs from the oracle"
+    _ffi.check(lib.qmc_lat_gen_gray(R, n2, D, 0, g2d.data_ptr(), xl.data_ptr(), h), "lat_gen_gray")
+    _ffi.check(lib.qmc_lat_shift_mod_1(R, n2, D, R, xl.data_ptr(), s2d.data_ptr(), xlr.data_ptr(), h), "shift")
+    torch.cuda.synchronize()
+    _t, xr_s = cpu_pipeline(g2, s2, nn, host_threads())
+    assert np.array_equal(xlr.view(R, n2, D)[:, :nn].cpu().numpy().view(U), xr_s.view(U)), \
+        "lattice plain differs from the oracle"
+    res["base-2 nets r=64, n=2^20, d=32 and lattices r=16, n=2^20, d=64"] = fam
     pts = 3 * r * n
-    return {"metric": METRIC, "value": pts / (total_ms / 1e3), "unit": "points/s (one dimension per base)",
-            "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms,
+    return {"metric": METRIC, "value": pts / (gdn_ms / 1e3), "unit": "points/s (gdn chain, one dimension per base)",
+            "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": gdn_ms,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u64 digits, f64",
-            "data": "synthetic (np.random.SFC64(b)): reference generators",
-            "config": {"workload": "plain gdn chain per dimension, r=32, n=2^18, d=1, bases 2, 3, 541",
-                       "l2": "digit arrays 0.5-4.3 GB >> 129 MB L2"},
-            "roofline": dict(roofline(sum(v["alg_bytes"] for p_ in res.values() for v in p_.values()), total_ms),
-                             kernel="the five plain gdn kernels, all bases"),
-            "kernels": res, "gpu_launches": 15 * args.steps}
+            "data": "synthetic (seeded np.random.SFC64): reference generators",
+            "config": {"workload": "every plain drop-in kernel one call at a time: gdn chain per dimension "
+                                   "(r=32, n=2^18, d=1, bases 2, 3, 541), base-2 nets (r=64, n=2^20, d=32), "
+                                   "lattices (r=16, n=2^20, d=64)",
+                       "l2": "arrays 0.5-17 GB >> 129 MB L2"},
+            "roofline": dict(roofline(sum(v["alg_bytes"] for k_, p_ in res.items() if k_.startswith("b=")
+                                          for v in p_.values()), gdn_ms),
+                             kernel="the five plain gdn kernels, all bases (value); every kernel's own fraction "
+                                    "under kernels"),
+            "kernels": res, "gpu_launches": (15 + len(other)) * args.steps}
 
 
 WORKLOADS = {"net_plain": run_net_plain, "net_lms": run_net_lms, "fft": run_fft, "halton": run_halton,
-             "gdn_plain": run_gdn_plain}
+             "plain": run_gdn_plain, "gdn_plain": run_gdn_plain}
 
 
 def main():
