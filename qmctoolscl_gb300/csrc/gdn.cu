@@ -337,9 +337,19 @@ __global__ void __launch_bounds__(THREADS) gdn_gen_tiled_kernel(u64 r, u64 n, u6
             }
             __syncwarp();
             // the npts x tw block: contiguous runs of tw words per point
-            for (u32 e = lane; e < npts * tw; e += 32) {
-                const u32 p = e / tw, tt = e - p * tw;
-                out[(i0 + p) * d * tmax + t0 + tt] = sg[p * 33 + tt];
+            if (tw == 32) {
+                for (u32 p = 0; p < npts; p++) out[(i0 + p) * d * tmax + t0 + lane] = sg[p * 33 + lane];
+            } else if ((tw & (tw - 1)) == 0) {  // a power of two: index by shift and mask
+                const u32 sh = 31 - __clz((int)tw);
+                for (u32 e = lane; e < npts * tw; e += 32) {
+                    const u32 p = e >> sh, tt = e & (tw - 1);
+                    out[(i0 + p) * d * tmax + t0 + tt] = sg[p * 33 + tt];
+                }
+            } else {
+                for (u32 e = lane; e < npts * tw; e += 32) {
+                    const u32 p = e / tw, tt = e - p * tw;
+                    out[(i0 + p) * d * tmax + t0 + tt] = sg[p * 33 + tt];
+                }
             }
             __syncwarp();
         }
