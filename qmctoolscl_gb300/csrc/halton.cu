@@ -72,23 +72,53 @@ struct HDim {
     u64 fdK_M;     // the same for b^K
     u64 c_off;     // offset of this dimension's (mmax x tmax) block inside a randomisation's C block
     u64 y_off;     // offset of its (tpad x b) term rows inside a randomisation's Y block
-    u64 s_off;     // offset of its tpad digits inside the recip / tail blocks
+    u64 s_off;     // offset of its tpad digits inside the request's tail blocks
+    u64 r_off;     // offset of its tpad recip_t in the plan's recip array
+};
+
+// One request of a batch (device copy): r randomisations of n points from
+// index n_start, d dimensions (dims[dim0 ..]), output x (r x n x d).  Its
+// tables sit at request-relative bases inside the plan's shared arrays.
+struct HReq {
+    u64 r, n, n_start, d;
+    u64 dim0;              // first HDim / PrepDim of the request
+    u64 c_base, c_per_l;   // C words: randomisation l of this request at c_base + l * c_per_l
+    u64 y_base, y_per_l;   // term-table words
+    u64 t_base, s_per_l;   // tail words (t_base + l * s_per_l + s_off); also the term-row prefix
+    u64 tl_base;           // prefix of (l, j) items of the tail kernel
+    u64 tile0, tiles_per_l;  // generation tiles
+    u32 o_base, pad;       // dimension order of the warps: order[o_base + wstart[q * (HT_WARPS + 1) + w] ...]
+    u32 has_lms, has_perm, has_shift, pad2;
+    double *x;
 };
 
 struct HPlanDev {
-    u64 r, n, n_start, d;
-    u64 c_per_l, y_per_l, s_per_l;  // words per randomisation
-    u32 has_lms, has_perm, has_shift, pad;
-    const HDim *dims;
-    const u32 *C;        // r * c_per_l: scrambled matrices mod b
-    const u64 *Y;        // r * y_per_l: term bits RN(recip_t * digit)
-    const u64 *recip;    // s_per_l: bits of recip_t, per (j, t)
-    const u32 *tail;     // r * s_per_l: largest biased exponent among the terms of digits t.. of (l, j)
-    const u16 *order;    // d dimension ids: warp w runs order[wstart[w] .. wstart[w+1])
-    const u32 *wstart;   // HT_WARPS + 1
-    double *x;
+    u64 nreq, total_c, rows, titems, ntiles, ndims;
+    const HReq *req;
+    const HDim *dims;    // all requests' dimensions
+    const u32 *C;        // scrambled matrices mod b
+    const u64 *Y;        // term bits RN(recip_t * digit)
+    const u64 *recip;    // bits of recip_t at HDim::r_off + t
+    const u32 *tail;     // largest biased exponent among the terms of digits t.. of (l, j)
+    const u16 *order;    // per request, its dimension ids (request-relative) grouped by warp
+    const u32 *wstart;   // per request, HT_WARPS + 1 offsets into its order
     unsigned *err;
 };
+
+// the request whose prefix field (a non-decreasing u64 member of HReq) holds key
+template <typename F>
+__device__ __forceinline__ u32 req_of(const HReq *req, u64 nreq, u64 key, F field)
+{
+    u32 lo = 0, hi = (u32)nreq - 1;
+    while (lo < hi) {
+        const u32 mid = (lo + hi + 1) >> 1;
+        if (field(req[mid]) <= key)
+            lo = mid;
+        else
+            hi = mid - 1;
+    }
+    return lo;
+}
 
 struct PrepDim {
     u64 b, tmax, mmax;
@@ -116,7 +146,7 @@ __device__ __forceinline__ u32 dim_mod(const HDim &D, u32 x)
 
 // ---------------------------------------------------------------- prep
 
-// the dimension whose block (offset `field` of HDim) holds offset off
+// the dimension (of dims[0 .. d)) whose block (offset `field` of HDim) holds offset off
 template <typename F>
 __device__ __forceinline__ u32 dim_of(const HDim *dims, u64 d, u64 off, F field)
 {
@@ -131,17 +161,19 @@ __device__ __forceinline__ u32 dim_of(const HDim *dims, u64 d, u64 off, F field)
     return lo;
 }
 
-// one thread per (l, j, k, t) word of C
-__global__ void halton_lms_kernel(HPlanDev P, const PrepDim *pd, u64 total_c, u32 *C)
+// one thread per (request, l, j, k, t) word of C
+__global__ void halton_lms_kernel(HPlanDev P, const PrepDim *pd, u32 *C)
 {
     const u64 stride = (u64)gridDim.x * blockDim.x;
-    for (u64 w = (u64)blockIdx.x * blockDim.x + threadIdx.x; w < total_c; w += stride) {
-        const u64 l = w / P.c_per_l, off = w % P.c_per_l;
-        const u32 j = dim_of(P.dims, P.d, off, [](const HDim &h) { return h.c_off; });
-        const HDim &D = P.dims[j];
+    for (u64 w = (u64)blockIdx.x * blockDim.x + threadIdx.x; w < P.total_c; w += stride) {
+        const HReq &R = P.req[req_of(P.req, P.nreq, w, [](const HReq &q) { return q.c_base; })];
+        const u64 loc0 = w - R.c_base, l = loc0 / R.c_per_l, off = loc0 % R.c_per_l;
+        const HDim *dims = P.dims + R.dim0;
+        const u32 j = dim_of(dims, R.d, off, [](const HDim &h) { return h.c_off; });
+        const HDim &D = dims[j];
         const u64 loc = off - D.c_off, k = loc / D.tmax, t = loc % D.tmax;
-        const PrepDim &Q = pd[j];
-        if (P.has_lms) {
+        const PrepDim &Q = pd[R.dim0 + j];
+        if (R.has_lms) {
             // gdn_linear_matrix_scramble.c:36-42 with d = 1, r_C = 1: sum_c (S[l,t,c]*C[k,c]) % b, no final
             // mod; the sum is at most tmax*(b-1) and the generation step reduces it anyway
             const u64 *srow = Q.S + (l * Q.tmax + t) * Q.tmax;
@@ -159,63 +191,67 @@ __global__ void halton_lms_kernel(HPlanDev P, const PrepDim *pd, u64 total_c, u3
     }
 }
 
-// recip_t of gdn_integer_to_float.c:34-38 for every (j, t)
+// recip_t of gdn_integer_to_float.c:34-38 for every dimension of every request
 __global__ void halton_recip_kernel(HPlanDev P, u64 *recip)
 {
-    for (u64 j = (u64)blockIdx.x * blockDim.x + threadIdx.x; j < P.d; j += (u64)gridDim.x * blockDim.x) {
-        const HDim &D = P.dims[j];
+    for (u64 g = (u64)blockIdx.x * blockDim.x + threadIdx.x; g < P.ndims; g += (u64)gridDim.x * blockDim.x) {
+        const HDim &D = P.dims[g];
         const double bd = (double)D.b;
         double rc = __ddiv_rn(1.0, bd);
         for (u32 t = 0; t < D.tpad; t++) {
-            recip[D.s_off + t] = as_bits(rc);
+            recip[D.r_off + t] = as_bits(rc);
             rc = __ddiv_rn(rc, bd);
         }
     }
 }
 
-// One warp per term row (l, j, t): Y[g] = RN(recip_t * digit(g)) for g < b,
-// digit(g) = (perm[l,t,g] + shift[l,t]) mod b as gdn_digital_permutation.c:36-39
-// and gdn_digital_shift.c:37-39 compute it (64-bit wrapping add), then
-// (double)digit * recip_t as gdn_integer_to_float.c:36-37.  Lane 0 records
-// the row's largest exponent in tail[l][s_off + t].
-__global__ void halton_terms_kernel(HPlanDev P, const PrepDim *pd, u64 rows, u64 *Y, u32 *tail)
+// One warp per term row (request, l, j, t): Y[g] = RN(recip_t * digit(g)) for
+// g < b, digit(g) = (perm[l,t,g] + shift[l,t]) mod b as
+// gdn_digital_permutation.c:36-39 and gdn_digital_shift.c:37-39 compute it
+// (64-bit wrapping add), then (double)digit * recip_t as
+// gdn_integer_to_float.c:36-37.  Lane 0 records the row's largest exponent in
+// the tail table (whose words are numbered exactly like the rows).
+__global__ void halton_terms_kernel(HPlanDev P, const PrepDim *pd, u64 *Y, u32 *tail)
 {
     const u32 lane = threadIdx.x % 32;
     const u64 wstride = (u64)gridDim.x * (blockDim.x / 32);
-    for (u64 row = ((u64)blockIdx.x * blockDim.x + threadIdx.x) / 32; row < rows; row += wstride) {
-        const u64 l = row / P.s_per_l, off = row % P.s_per_l;
-        const u32 j = dim_of(P.dims, P.d, off, [](const HDim &h) { return h.s_off; });
-        const HDim &D = P.dims[j];
-        const PrepDim &Q = pd[j];
+    for (u64 row = ((u64)blockIdx.x * blockDim.x + threadIdx.x) / 32; row < P.rows; row += wstride) {
+        const HReq &R = P.req[req_of(P.req, P.nreq, row, [](const HReq &q) { return q.t_base; })];
+        const u64 loc = row - R.t_base, l = loc / R.s_per_l, off = loc % R.s_per_l;
+        const HDim *dims = P.dims + R.dim0;
+        const u32 j = dim_of(dims, R.d, off, [](const HDim &h) { return h.s_off; });
+        const HDim &D = dims[j];
+        const PrepDim &Q = pd[R.dim0 + j];
         const u64 t = off - D.s_off;
-        u64 *yrow = Y + l * P.y_per_l + D.y_off + t * D.b;
+        u64 *yrow = Y + R.y_base + l * R.y_per_l + D.y_off + t * D.b;
         if (t >= D.tmax) {  // padding row: +0 terms, no tail
             for (u32 g = lane; g < D.b; g += 32) yrow[g] = 0;
-            if (lane == 0) tail[l * P.s_per_l + off] = 0;
+            if (lane == 0) tail[row] = 0;
             continue;
         }
-        const double rc = as_double(P.recip[D.s_off + t]);
-        const u64 sh = P.has_shift ? Q.shifts[l * D.tmax + t] : 0;
+        const double rc = as_double(P.recip[D.r_off + t]);
+        const u64 sh = R.has_shift ? Q.shifts[l * D.tmax + t] : 0;
         u64 mx = 0;
         for (u32 g = lane; g < D.b; g += 32) {
-            const u64 pv = P.has_perm ? Q.perms[(l * D.tmax + t) * D.b + g] : g;
-            const u64 dig = P.has_shift ? (pv + sh) % D.b : pv;
+            const u64 pv = R.has_perm ? Q.perms[(l * D.tmax + t) * D.b + g] : g;
+            const u64 dig = R.has_shift ? (pv + sh) % D.b : pv;
             const u64 y = dig ? as_bits(__dmul_rn(rc, __ull2double_rn(dig))) : 0;
             yrow[g] = y;
             mx = max(mx, y);  // non-negative doubles order like their bits
         }
         for (int o = 16; o; o >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
-        if (lane == 0) tail[l * P.s_per_l + off] = (u32)(mx >> 52);
+        if (lane == 0) tail[row] = (u32)(mx >> 52);
     }
 }
 
-// suffix maximum over t of the row exponents, per (l, j)
+// suffix maximum over t of the row exponents, per (request, l, j)
 __global__ void halton_tail_kernel(HPlanDev P, u32 *tail)
 {
-    for (u64 w = (u64)blockIdx.x * blockDim.x + threadIdx.x; w < P.r * P.d; w += (u64)gridDim.x * blockDim.x) {
-        const u64 l = w / P.d, j = w % P.d;
-        const HDim &D = P.dims[j];
-        u32 *tl = tail + l * P.s_per_l + D.s_off;
+    for (u64 w = (u64)blockIdx.x * blockDim.x + threadIdx.x; w < P.titems; w += (u64)gridDim.x * blockDim.x) {
+        const HReq &R = P.req[req_of(P.req, P.nreq, w, [](const HReq &q) { return q.tl_base; })];
+        const u64 loc = w - R.tl_base, l = loc / R.d, j = loc % R.d;
+        const HDim &D = P.dims[R.dim0 + j];
+        u32 *tl = tail + R.t_base + l * R.s_per_l + D.s_off;
         u32 m = 0;
         for (u32 t = D.tpad; t-- > 0;) {
             m = max(m, tl[t]);
@@ -365,46 +401,51 @@ __device__ __forceinline__ void dim_value_k(const HDim &D, const u32 *Cj, const 
     }
 }
 
-// A CTA owns tiles of 32 * PPL consecutive points of one randomisation and all d
-// dimensions; the tile of doubles is staged in shared memory ([32 * PPL][d])
-// and stored as contiguous rows.
-template <u32 PPL>
-__global__ void __launch_bounds__(HT_THREADS) halton_gen_kernel(HPlanDev P)
+// A CTA owns tiles of 32 * PPL consecutive points of one randomisation of one
+// request and all its d dimensions; tiles of all requests form one list.  The
+// tile of doubles is staged in shared memory ([32 * PPL][d]) and stored as
+// contiguous rows.  With one request (ONE) its descriptor is a kernel
+// parameter (the constant bank, no registers held for it).
+template <u32 PPL, bool ONE>
+__global__ void __launch_bounds__(HT_THREADS, 3) halton_gen_kernel(HPlanDev P, HReq R1)
 {
     extern __shared__ __align__(16) unsigned char sm[];
     double *tile = (double *)sm;
     constexpr u32 TP = 32 * PPL;  // points per tile
     const u32 warp = threadIdx.x / 32, lane = threadIdx.x % 32;
-    const u64 tiles_per_l = (P.n + TP - 1) / TP;
-    const u64 ntiles = P.r * tiles_per_l;
-    for (u64 tt = blockIdx.x; tt < ntiles; tt += gridDim.x) {
-        const u64 l = tt / tiles_per_l, i0 = (tt % tiles_per_l) * TP;
-        const u32 base = (u32)(P.n_start + i0);
+    for (u64 tt = blockIdx.x; tt < P.ntiles; tt += gridDim.x) {
+        const u32 q = ONE ? 0u : req_of(P.req, P.nreq, tt, [](const HReq &r_) { return r_.tile0; });
+        const HReq R = ONE ? R1 : P.req[q];  // by value: the output stores may not alias it
+        const u64 loc = tt - R.tile0, l = loc / R.tiles_per_l, i0 = (loc % R.tiles_per_l) * TP;
+        const u32 base = (u32)(R.n_start + i0);
         u32 itrue[PPL];
         bool active[PPL];
 #pragma unroll
-        for (u32 q = 0; q < PPL; q++) {
-            active[q] = i0 + lane + 32 * q < P.n;  // points past the last compute nothing
-            itrue[q] = active[q] ? base + lane + 32 * q : base;  // < 2^32 (checked at plan creation)
+        for (u32 k = 0; k < PPL; k++) {
+            active[k] = i0 + lane + 32 * k < R.n;  // points past the last compute nothing
+            itrue[k] = active[k] ? base + lane + 32 * k : base;  // < 2^32 (checked at plan creation)
         }
-        const u32 *Cl = P.C + l * P.c_per_l;
-        const u64 *Yl = P.Y + l * P.y_per_l;
-        const u32 *Tl = P.tail + l * P.s_per_l;
-        for (u32 oi = P.wstart[warp]; oi < P.wstart[warp + 1]; oi++) {
-            const u32 j = P.order[oi];
-            const HDim D = P.dims[j];
+        const u32 *Cl = P.C + R.c_base + l * R.c_per_l;
+        const u64 *Yl = P.Y + R.y_base + l * R.y_per_l;
+        const u32 *Tl = P.tail + R.t_base + l * R.s_per_l;
+        const HDim *dims = P.dims + R.dim0;
+        const u16 *order = P.order + R.o_base;
+        const u32 *ws = P.wstart + (u64)q * (HT_WARPS + 1);
+        for (u32 oi = ws[warp]; oi < ws[warp + 1]; oi++) {
+            const u32 j = order[oi];
+            const HDim D = dims[j];
             u64 vb[PPL];
             if (D.add == ADD_INT)
                 dim_value_k<ADD_INT, PPL>(D, Cl + D.c_off, Yl + D.y_off, Tl + D.s_off, base, itrue, active, lane, vb);
             else
                 dim_value_k<ADD_FP64, PPL>(D, Cl + D.c_off, Yl + D.y_off, Tl + D.s_off, base, itrue, active, lane, vb);
 #pragma unroll
-            for (u32 q = 0; q < PPL; q++) tile[(lane + 32 * q) * P.d + j] = as_double(vb[q]);
+            for (u32 k = 0; k < PPL; k++) tile[(lane + 32 * k) * R.d + j] = as_double(vb[k]);
         }
         __syncthreads();
-        const u64 rows = min((u64)TP, P.n - i0);
-        double *out = P.x + (l * P.n + i0) * P.d;
-        for (u64 e = threadIdx.x; e < rows * P.d; e += HT_THREADS) __stcs(out + e, tile[e]);
+        const u64 rows = min((u64)TP, R.n - i0);
+        double *out = R.x + (l * R.n + i0) * R.d;
+        for (u64 e = threadIdx.x; e < rows * R.d; e += HT_THREADS) __stcs(out + e, tile[e]);
         __syncthreads();
     }
 }
@@ -439,141 +480,235 @@ void assign_adds(std::vector<HDim> &hd, double share)
 struct qmc_halton_plan {
     HPlanDev P{};
     std::vector<HDim> hd;
-    void *d_dims = nullptr, *d_C = nullptr, *d_Y = nullptr, *d_recip = nullptr, *d_tail = nullptr;
-    void *d_order = nullptr, *d_wstart = nullptr, *d_prep = nullptr;
+    std::vector<HReq> hreq;
     std::vector<PrepDim> prep;
-    u64 total_c = 0, rows = 0;
+    void *d_req = nullptr, *d_dims = nullptr, *d_C = nullptr, *d_Y = nullptr, *d_recip = nullptr, *d_tail = nullptr;
+    void *d_order = nullptr, *d_wstart = nullptr, *d_prep = nullptr;
     size_t smem = 0;
     u32 ppl = 1;
     bool prepared = false;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
 };
+
+namespace {
+
+void drop_graph(qmc_halton_plan *p)
+{
+    if (p->exec) cudaGraphExecDestroy(p->exec);
+    if (p->graph) cudaGraphDestroy(p->graph);
+    p->exec = nullptr;
+    p->graph = nullptr;
+}
+
+int prepare_launch(qmc_halton_plan *p, cudaStream_t st)
+{
+    const unsigned cap = (unsigned)qmcgb::sm_count() * 16;
+    halton_lms_kernel<<<qmcgb::grid_for(p->P.total_c, 256, cap), 256, 0, st>>>(p->P, (const PrepDim *)p->d_prep,
+                                                                              (u32 *)p->d_C);
+    if (int rc = qmcgb::launch_status("halton_lms_kernel")) return rc;
+    halton_recip_kernel<<<qmcgb::grid_for(p->P.ndims, 128, 1024), 128, 0, st>>>(p->P, (u64 *)p->d_recip);
+    if (int rc = qmcgb::launch_status("halton_recip_kernel")) return rc;
+    halton_terms_kernel<<<qmcgb::grid_for(p->P.rows * 32, 256, cap), 256, 0, st>>>(p->P, (const PrepDim *)p->d_prep,
+                                                                                  (u64 *)p->d_Y, (u32 *)p->d_tail);
+    if (int rc = qmcgb::launch_status("halton_terms_kernel")) return rc;
+    halton_tail_kernel<<<qmcgb::grid_for(p->P.titems, 128, cap), 128, 0, st>>>(p->P, (u32 *)p->d_tail);
+    return qmcgb::launch_status("halton_tail_kernel");
+}
+
+int run_launch(qmc_halton_plan *p, cudaStream_t st)
+{
+    const unsigned grid = qmcgb::grid_for(p->P.ntiles, 1, (unsigned)qmcgb::sm_count() * 8);
+    const HReq &R1 = p->hreq[0];
+    const bool one = p->hreq.size() == 1;
+    if (p->ppl == 2) {
+        if (one)
+            halton_gen_kernel<2, true><<<grid, HT_THREADS, p->smem, st>>>(p->P, R1);
+        else
+            halton_gen_kernel<2, false><<<grid, HT_THREADS, p->smem, st>>>(p->P, R1);
+    } else {
+        if (one)
+            halton_gen_kernel<1, true><<<grid, HT_THREADS, p->smem, st>>>(p->P, R1);
+        else
+            halton_gen_kernel<1, false><<<grid, HT_THREADS, p->smem, st>>>(p->P, R1);
+    }
+    return qmcgb::launch_status("halton_gen_kernel");
+}
+
+template <u32 PPL>
+int gen_smem_attr(size_t smem)
+{
+    const int v = (int)smem;
+    cudaError_t e = cudaFuncSetAttribute(halton_gen_kernel<PPL, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, v);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(halton_gen_kernel<PPL, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, v);
+    return qmcgb::cuda_status(e, "cudaFuncSetAttribute");
+}
+
+}  // namespace
 
 extern "C" {
 
-int qmc_halton_plan_create(uint64_t r, uint64_t n, uint64_t n_start, uint64_t d, const qmc_gdn_dim *dims, double *x,
-                           qmc_halton_plan **plan)
+int qmc_halton_batch_create(const qmc_halton_request *reqs, int nreq, qmc_halton_plan **plan)
 {
-    QMC_REQUIRE(plan && dims && x, "null argument");
+    QMC_REQUIRE(plan && reqs && nreq >= 1, "null argument or empty batch");
     *plan = nullptr;
-    QMC_REQUIRE(d >= 1 && d <= HT_MAX_DIMS && r >= 1 && n >= 1, "need 1 <= d <= %u, r >= 1, n >= 1", HT_MAX_DIMS);
-    QMC_REQUIRE(n_start + n <= (1ull << 32) && n_start + n > n_start, "indices must stay below 2^32");
-    QMC_REQUIRE(32 * d * sizeof(double) <= 200 * 1024, "d too large for the shared-memory output tile");
+    u64 maxd = 0;
+    for (int q = 0; q < nreq; q++) {
+        const qmc_halton_request &R = reqs[q];
+        QMC_REQUIRE(R.dims && R.x, "request %d: null dims or x", q);
+        QMC_REQUIRE(R.d >= 1 && R.d <= HT_MAX_DIMS && R.r >= 1 && R.n >= 1,
+                    "request %d: need 1 <= d <= %u, r >= 1, n >= 1", q, HT_MAX_DIMS);
+        QMC_REQUIRE(R.n_start + R.n <= (1ull << 32) && R.n_start + R.n > R.n_start,
+                    "request %d: indices must stay below 2^32", q);
+        maxd = std::max<u64>(maxd, R.d);
+    }
+    QMC_REQUIRE(32 * maxd * sizeof(double) <= 200 * 1024, "d too large for the shared-memory output tile");
     // two points per lane (two independent digit chains, shuffles shared) while the 64-point
     // output tile stays small enough for four CTAs per SM
-    const u32 ppl = 64 * d * sizeof(double) <= 52 * 1024 ? 2 : 1;
-    const u64 smem = 32 * ppl * d * sizeof(double);
-    // a step is applied when its array is given, for every dimension alike
-    const bool has_lms = dims[0].S != nullptr, has_perm = dims[0].perms != nullptr,
-               has_shift = dims[0].shifts != nullptr;
+    const u32 ppl = 64 * maxd * sizeof(double) <= 52 * 1024 ? 2 : 1;
+    const u64 tp = 32ull * ppl;
     qmc_halton_plan *p = new qmc_halton_plan();
-    std::vector<HDim> &hd = p->hd;
-    hd.resize(d);
-    u64 c_off = 0, y_off = 0, s_off = 0;
-    for (u64 j = 0; j < d; j++) {
-        const qmc_gdn_dim &q = dims[j];
-        const char *bad = nullptr;
-        if (q.b < 2 || q.b >= HT_MAX_B) bad = "base outside [2, 2048)";
-        else if (q.tmax == 0 || q.tmax > 256 || q.mmax == 0 || q.mmax > 64) bad = "tmax in [1,256] and mmax in [1,64]";
-        else if (!q.C) bad = "null generating matrix";
-        else if ((q.S != nullptr) != has_lms || (q.perms != nullptr) != has_perm ||
-                 (q.shifts != nullptr) != has_shift)
-            bad = "S, perms and shifts must be given for all dimensions or for none";
-        else if (ceil_digits(n_start + n - 1, q.b) > q.mmax) bad = "mmax smaller than the base-b digits of the last index";
-        if (bad) {
-            delete p;
-            qmcgb::set_error("dimension %llu: %s", (unsigned long long)j, bad);
-            return q.b < 2 ? QMC_ERR_DOMAIN : QMC_ERR_ARG;
-        }
-        HDim &h = hd[j];
-        h = HDim{};
-        h.b = (u32)q.b;
-        h.tmax = (u32)q.tmax;
-        h.mmax = (u32)q.mmax;
-        h.K = 1;
-        h.bK = h.b;
-        while (h.bK < 32 * ppl) {
-            h.bK *= h.b;
-            h.K++;
-        }
-        h.Klo = std::min<u32>(h.K, h.mmax);
-        h.m32 = (u32)((1ull << 32) / h.b + 1);
-        // digit sums stay below (mmax + 6) * b^2; the 32-bit division needs them below 2^32 / b
-        h.wide = (u64)(h.mmax + 6) * h.b * h.b * h.b >= (1ull << 32);
-        h.fd_M = fastdiv32_make(h.b).M;
-        h.fdK_M = fastdiv32_make(h.bK).M;
-        h.tpad = (h.tmax + HT_GROUP - 1) / HT_GROUP * HT_GROUP;
-        h.c_off = c_off;
-        h.y_off = y_off;
-        h.s_off = s_off;
-        c_off += q.mmax * q.tmax;
-        y_off += (u64)h.tpad * q.b;
-        s_off += h.tpad;
-        p->prep.push_back(PrepDim{q.b, q.tmax, q.mmax, (const u64 *)q.S, (const u64 *)q.C, (const u64 *)q.perms,
-                                  (const u64 *)q.shifts});
-    }
-    assign_adds(hd, 0.5);
-    // longest-first assignment of dimensions to the warps of a CTA
-    std::vector<u32> idx(d);
-    for (u32 j = 0; j < d; j++) idx[j] = j;
-    auto cost = [&](u32 j) { return (double)hd[j].tmax * 40.0 + (double)hd[j].mmax * 20.0; };
-    std::sort(idx.begin(), idx.end(), [&](u32 a, u32 b) { return cost(a) > cost(b); });
-    std::vector<std::vector<u32>> per(HT_WARPS);
-    std::vector<double> load(HT_WARPS, 0.0);
-    for (u32 j : idx) {
-        const int w = (int)(std::min_element(load.begin(), load.end()) - load.begin());
-        per[w].push_back(j);
-        load[w] += cost(j);
-    }
-    std::vector<u16> order;
-    std::vector<u32> wstart(HT_WARPS + 1, 0);
-    for (int w = 0; w < HT_WARPS; w++) {
-        wstart[w] = (u32)order.size();
-        for (u32 j : per[w]) order.push_back((u16)j);
-    }
-    wstart[HT_WARPS] = (u32)order.size();
-
-    p->P.r = r;
-    p->P.n = n;
-    p->P.n_start = n_start;
-    p->P.d = d;
-    p->P.c_per_l = c_off;
-    p->P.y_per_l = y_off;
-    p->P.s_per_l = s_off;
-    p->P.has_lms = has_lms;
-    p->P.has_perm = has_perm;
-    p->P.has_shift = has_shift;
-    p->P.x = x;
-    p->P.err = qmcgb::device_error_ptr();
-    p->total_c = r * c_off;
-    p->rows = r * s_off;
-    p->smem = smem;
     p->ppl = ppl;
+    p->smem = tp * maxd * sizeof(double);
+    std::vector<u16> order;
+    std::vector<u32> wstart;
+    u64 c_base = 0, y_base = 0, t_base = 0, tl_base = 0, tile0 = 0, r_base = 0;
+    for (int q = 0; q < nreq; q++) {
+        const qmc_halton_request &Rq = reqs[q];
+        const qmc_gdn_dim *dims = Rq.dims;
+        const u64 d = Rq.d;
+        // a step is applied when its array is given, for every dimension of the request alike
+        const bool has_lms = dims[0].S != nullptr, has_perm = dims[0].perms != nullptr,
+                   has_shift = dims[0].shifts != nullptr;
+        HReq R{};
+        R.r = Rq.r;
+        R.n = Rq.n;
+        R.n_start = Rq.n_start;
+        R.d = d;
+        R.dim0 = p->hd.size();
+        R.has_lms = has_lms;
+        R.has_perm = has_perm;
+        R.has_shift = has_shift;
+        R.x = Rq.x;
+        u64 c_off = 0, y_off = 0, s_off = 0;
+        for (u64 j = 0; j < d; j++) {
+            const qmc_gdn_dim &g = dims[j];
+            const char *bad = nullptr;
+            if (g.b < 2 || g.b >= HT_MAX_B) bad = "base outside [2, 2048)";
+            else if (g.tmax == 0 || g.tmax > 256 || g.mmax == 0 || g.mmax > 64) bad = "tmax in [1,256] and mmax in [1,64]";
+            else if (!g.C) bad = "null generating matrix";
+            else if ((g.S != nullptr) != has_lms || (g.perms != nullptr) != has_perm ||
+                     (g.shifts != nullptr) != has_shift)
+                bad = "S, perms and shifts must be given for all dimensions or for none";
+            else if (ceil_digits(Rq.n_start + Rq.n - 1, g.b) > g.mmax)
+                bad = "mmax smaller than the base-b digits of the last index";
+            if (bad) {
+                delete p;
+                qmcgb::set_error("request %d, dimension %llu: %s", q, (unsigned long long)j, bad);
+                return g.b < 2 ? QMC_ERR_DOMAIN : QMC_ERR_ARG;
+            }
+            HDim h{};
+            h.b = (u32)g.b;
+            h.tmax = (u32)g.tmax;
+            h.mmax = (u32)g.mmax;
+            h.K = 1;
+            h.bK = h.b;
+            while (h.bK < tp) {
+                h.bK *= h.b;
+                h.K++;
+            }
+            h.Klo = std::min<u32>(h.K, h.mmax);
+            h.m32 = (u32)((1ull << 32) / h.b + 1);
+            // digit sums stay below (mmax + 6) * b^2; the 32-bit division needs them below 2^32 / b
+            h.wide = (u64)(h.mmax + 6) * h.b * h.b * h.b >= (1ull << 32);
+            h.fd_M = fastdiv32_make(h.b).M;
+            h.fdK_M = fastdiv32_make(h.bK).M;
+            h.tpad = (h.tmax + HT_GROUP - 1) / HT_GROUP * HT_GROUP;
+            h.c_off = c_off;
+            h.y_off = y_off;
+            h.s_off = s_off;
+            h.r_off = r_base + s_off;
+            c_off += g.mmax * g.tmax;
+            y_off += (u64)h.tpad * g.b;
+            s_off += h.tpad;
+            p->hd.push_back(h);
+            p->prep.push_back(PrepDim{g.b, g.tmax, g.mmax, (const u64 *)g.S, (const u64 *)g.C, (const u64 *)g.perms,
+                                      (const u64 *)g.shifts});
+        }
+        R.c_base = c_base;
+        R.c_per_l = c_off;
+        R.y_base = y_base;
+        R.y_per_l = y_off;
+        R.t_base = t_base;
+        R.s_per_l = s_off;
+        R.tl_base = tl_base;
+        R.tile0 = tile0;
+        R.tiles_per_l = (Rq.n + tp - 1) / tp;
+        R.o_base = (u32)order.size();
+        c_base += Rq.r * c_off;
+        y_base += Rq.r * y_off;
+        t_base += Rq.r * s_off;
+        tl_base += Rq.r * d;
+        tile0 += Rq.r * R.tiles_per_l;
+        r_base += s_off;
+        // longest-first assignment of the request's dimensions to the warps of a CTA
+        std::vector<u32> idx(d);
+        for (u32 j = 0; j < d; j++) idx[j] = j;
+        const HDim *hj = p->hd.data() + R.dim0;
+        auto cost = [&](u32 j) { return (double)hj[j].tmax * 40.0 + (double)hj[j].mmax * 20.0; };
+        std::sort(idx.begin(), idx.end(), [&](u32 a, u32 b) { return cost(a) > cost(b); });
+        std::vector<std::vector<u32>> per(HT_WARPS);
+        std::vector<double> load(HT_WARPS, 0.0);
+        for (u32 j : idx) {
+            const int w = (int)(std::min_element(load.begin(), load.end()) - load.begin());
+            per[w].push_back(j);
+            load[w] += cost(j);
+        }
+        u32 pos = 0;
+        for (int w = 0; w < HT_WARPS; w++) {
+            wstart.push_back(pos);
+            for (u32 j : per[w]) {
+                order.push_back((u16)j);
+                pos++;
+            }
+        }
+        wstart.push_back(pos);
+        p->hreq.push_back(R);
+    }
+    assign_adds(p->hd, 1.0);
+    const u64 ndims = p->hd.size();
+    p->P.nreq = (u64)nreq;
+    p->P.total_c = c_base;
+    p->P.rows = t_base;
+    p->P.titems = tl_base;
+    p->P.ntiles = tile0;
+    p->P.ndims = ndims;
+    p->P.err = qmcgb::device_error_ptr();
     int rc = 0;
     auto alloc = [&](void **dst, size_t bytes) {
         if (!rc) rc = qmcgb::cuda_status(cudaMalloc(dst, bytes ? bytes : 16), "cudaMalloc");
     };
-    alloc(&p->d_dims, d * sizeof(HDim));
-    alloc(&p->d_C, p->total_c * sizeof(u32));
-    alloc(&p->d_Y, r * y_off * sizeof(u64));
-    alloc(&p->d_recip, s_off * sizeof(u64));
-    alloc(&p->d_tail, r * s_off * sizeof(u32));
-    alloc(&p->d_order, d * sizeof(u16));
-    alloc(&p->d_wstart, (HT_WARPS + 1) * sizeof(u32));
-    alloc(&p->d_prep, d * sizeof(PrepDim));
-    if (!rc) rc = qmcgb::cuda_status(cudaMemcpy(p->d_dims, hd.data(), d * sizeof(HDim), cudaMemcpyHostToDevice), "copy");
-    if (!rc) rc = qmcgb::cuda_status(cudaMemcpy(p->d_order, order.data(), d * sizeof(u16), cudaMemcpyHostToDevice), "copy");
-    if (!rc)
-        rc = qmcgb::cuda_status(cudaMemcpy(p->d_wstart, wstart.data(), wstart.size() * sizeof(u32), cudaMemcpyHostToDevice),
-                                "copy");
-    if (!rc)
-        rc = qmcgb::cuda_status(cudaMemcpy(p->d_prep, p->prep.data(), d * sizeof(PrepDim), cudaMemcpyHostToDevice), "copy");
+    auto put = [&](void *dst, const void *src, size_t bytes) {
+        if (!rc && bytes) rc = qmcgb::cuda_status(cudaMemcpy(dst, src, bytes, cudaMemcpyHostToDevice), "copy");
+    };
+    alloc(&p->d_req, nreq * sizeof(HReq));
+    alloc(&p->d_dims, ndims * sizeof(HDim));
+    alloc(&p->d_C, c_base * sizeof(u32));
+    alloc(&p->d_Y, y_base * sizeof(u64));
+    alloc(&p->d_recip, r_base * sizeof(u64));
+    alloc(&p->d_tail, t_base * sizeof(u32));
+    alloc(&p->d_order, order.size() * sizeof(u16));
+    alloc(&p->d_wstart, wstart.size() * sizeof(u32));
+    alloc(&p->d_prep, ndims * sizeof(PrepDim));
+    put(p->d_req, p->hreq.data(), nreq * sizeof(HReq));
+    put(p->d_dims, p->hd.data(), ndims * sizeof(HDim));
+    put(p->d_order, order.data(), order.size() * sizeof(u16));
+    put(p->d_wstart, wstart.data(), wstart.size() * sizeof(u32));
+    put(p->d_prep, p->prep.data(), ndims * sizeof(PrepDim));
     if (!rc && !p->P.err) rc = QMC_ERR_CUDA;
-    if (!rc && smem > 48 * 1024)
-        rc = qmcgb::cuda_status(ppl == 2 ? cudaFuncSetAttribute(halton_gen_kernel<2>,
-                                                                cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)
-                                         : cudaFuncSetAttribute(halton_gen_kernel<1>,
-                                                                cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
-                                "cudaFuncSetAttribute");
+    if (!rc && p->smem > 48 * 1024) rc = ppl == 2 ? gen_smem_attr<2>(p->smem) : gen_smem_attr<1>(p->smem);
+    p->P.req = (const HReq *)p->d_req;
     p->P.dims = (const HDim *)p->d_dims;
     p->P.C = (const u32 *)p->d_C;
     p->P.Y = (const u64 *)p->d_Y;
@@ -589,21 +724,17 @@ int qmc_halton_plan_create(uint64_t r, uint64_t n, uint64_t n_start, uint64_t d,
     return QMC_OK;
 }
 
+int qmc_halton_plan_create(uint64_t r, uint64_t n, uint64_t n_start, uint64_t d, const qmc_gdn_dim *dims, double *x,
+                           qmc_halton_plan **plan)
+{
+    const qmc_halton_request one{r, n, n_start, d, dims, x};
+    return qmc_halton_batch_create(&one, 1, plan);
+}
+
 int qmc_halton_plan_prepare(qmc_halton_plan *p, qmc_stream_t s)
 {
     QMC_REQUIRE(p, "null plan");
-    cudaStream_t st = QMC_STREAM(s);
-    const unsigned cap = (unsigned)qmcgb::sm_count() * 16;
-    halton_lms_kernel<<<qmcgb::grid_for(p->total_c, 256, cap), 256, 0, st>>>(p->P, (const PrepDim *)p->d_prep,
-                                                                            p->total_c, (u32 *)p->d_C);
-    if (int rc = qmcgb::launch_status("halton_lms_kernel")) return rc;
-    halton_recip_kernel<<<qmcgb::grid_for(p->P.d, 128, 1024), 128, 0, st>>>(p->P, (u64 *)p->d_recip);
-    if (int rc = qmcgb::launch_status("halton_recip_kernel")) return rc;
-    halton_terms_kernel<<<qmcgb::grid_for(p->rows * 32, 256, cap), 256, 0, st>>>(
-        p->P, (const PrepDim *)p->d_prep, p->rows, (u64 *)p->d_Y, (u32 *)p->d_tail);
-    if (int rc = qmcgb::launch_status("halton_terms_kernel")) return rc;
-    halton_tail_kernel<<<qmcgb::grid_for(p->P.r * p->P.d, 128, cap), 128, 0, st>>>(p->P, (u32 *)p->d_tail);
-    if (int rc = qmcgb::launch_status("halton_tail_kernel")) return rc;
+    if (int rc = prepare_launch(p, QMC_STREAM(s))) return rc;
     p->prepared = true;
     return QMC_OK;
 }
@@ -611,20 +742,43 @@ int qmc_halton_plan_prepare(qmc_halton_plan *p, qmc_stream_t s)
 int qmc_halton_plan_run(qmc_halton_plan *p, qmc_stream_t s)
 {
     QMC_REQUIRE(p && p->prepared, "null or unprepared plan (call qmc_halton_plan_prepare)");
-    const u64 tp = 32ull * p->ppl;
-    const u64 tiles = p->P.r * ((p->P.n + tp - 1) / tp);
-    const unsigned grid = qmcgb::grid_for(tiles, 1, (unsigned)qmcgb::sm_count() * 8);
-    if (p->ppl == 2)
-        halton_gen_kernel<2><<<grid, HT_THREADS, p->smem, QMC_STREAM(s)>>>(p->P);
-    else
-        halton_gen_kernel<1><<<grid, HT_THREADS, p->smem, QMC_STREAM(s)>>>(p->P);
-    return qmcgb::launch_status("halton_gen_kernel");
+    return run_launch(p, QMC_STREAM(s));
+}
+
+int qmc_halton_plan_graph_launch(qmc_halton_plan *p, qmc_stream_t s)
+{
+    QMC_REQUIRE(p, "null plan");
+    QMC_REQUIRE(s != nullptr, "graph capture needs a stream other than the legacy default stream");
+    cudaStream_t st = QMC_STREAM(s);
+    if (!p->exec) {
+        if (int rc = qmcgb::cuda_status(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal), "capture"))
+            return rc;
+        int lrc = prepare_launch(p, st);
+        if (!lrc) lrc = run_launch(p, st);
+        cudaGraph_t g = nullptr;
+        const cudaError_t e = cudaStreamEndCapture(st, &g);
+        if (lrc) {
+            if (g) cudaGraphDestroy(g);
+            return lrc;
+        }
+        if (int rc = qmcgb::cuda_status(e, "end capture")) return rc;
+        p->graph = g;
+        if (int rc = qmcgb::cuda_status(cudaGraphInstantiate(&p->exec, g, 0), "instantiate")) {
+            drop_graph(p);
+            return rc;
+        }
+        p->prepared = true;
+    }
+    return qmcgb::cuda_status(cudaGraphLaunch(p->exec, st), "cudaGraphLaunch");
 }
 
 int qmc_halton_plan_set_fp64_share(qmc_halton_plan *p, double share)
 {
     QMC_REQUIRE(p && share >= 0.0 && share <= 1.0, "null plan or share outside [0, 1]");
     assign_adds(p->hd, share);
+    // the previous run may still read the descriptors
+    if (int rc = qmcgb::cuda_status(cudaDeviceSynchronize(), "synchronise before rewriting the descriptors"))
+        return rc;
     return qmcgb::cuda_status(cudaMemcpy(p->d_dims, p->hd.data(), p->hd.size() * sizeof(HDim), cudaMemcpyHostToDevice),
                               "copy");
 }
@@ -632,7 +786,8 @@ int qmc_halton_plan_set_fp64_share(qmc_halton_plan *p, double share)
 int qmc_halton_plan_destroy(qmc_halton_plan *p)
 {
     if (!p) return QMC_OK;
-    for (void *q : {p->d_dims, p->d_C, p->d_Y, p->d_recip, p->d_tail, p->d_order, p->d_wstart, p->d_prep})
+    drop_graph(p);
+    for (void *q : {p->d_req, p->d_dims, p->d_C, p->d_Y, p->d_recip, p->d_tail, p->d_order, p->d_wstart, p->d_prep})
         if (q) cudaFree(q);
     delete p;
     return QMC_OK;

@@ -39,16 +39,24 @@ class GdnDim(_ct.Structure):
     _fields_ = [("b", _U64), ("tmax", _U64), ("mmax", _U64), ("S", _P), ("C", _P), ("perms", _P), ("shifts", _P)]
 
 
+class HaltonRequest(_ct.Structure):
+    """qmc_halton_request (include/qmcgb.h)."""
+    _fields_ = [("r", _U64), ("n", _U64), ("n_start", _U64), ("d", _U64), ("dims", _ct.POINTER(GdnDim)), ("x", _P)]
+
+
 def _lib():
     L = _ffi.lib()
     if not getattr(L, "_halton_bound", False):
         L.qmc_halton_plan_create.argtypes = [_U64, _U64, _U64, _U64, _ct.POINTER(GdnDim), _P, _ct.POINTER(_P)]
+        L.qmc_halton_batch_create.argtypes = [_ct.POINTER(HaltonRequest), _ct.c_int, _ct.POINTER(_P)]
         L.qmc_halton_plan_prepare.argtypes = [_P, _P]
         L.qmc_halton_plan_run.argtypes = [_P, _P]
+        L.qmc_halton_plan_graph_launch.argtypes = [_P, _P]
         L.qmc_halton_plan_destroy.argtypes = [_P]
         L.qmc_halton_plan_set_fp64_share.argtypes = [_P, _ct.c_double]
-        for fn in ("qmc_halton_plan_create", "qmc_halton_plan_prepare", "qmc_halton_plan_run",
-                   "qmc_halton_plan_destroy", "qmc_halton_plan_set_fp64_share"):
+        for fn in ("qmc_halton_plan_create", "qmc_halton_batch_create", "qmc_halton_plan_prepare",
+                   "qmc_halton_plan_run", "qmc_halton_plan_graph_launch", "qmc_halton_plan_destroy",
+                   "qmc_halton_plan_set_fp64_share"):
             getattr(L, fn).restype = _ct.c_int
         L._halton_bound = True
     return L
@@ -77,47 +85,72 @@ def _create(r, n, n_start, structs, x_ptr):
     return h
 
 
-class HaltonPlan:
-    """One fused generalized-net generation over device tensors.  The plan
-    keeps the tensors alive; prepare() reads S, C, perms and shifts (call it
-    again after changing them), run() writes x.  x may also be a pinned
-    float64 numpy array (batch.pinned_empty): the kernel then writes the
-    points straight into host memory."""
+def _x_pointer(x, count):
+    torch = _torch()
+    if isinstance(x, np.ndarray):
+        if x.dtype != np.float64 or not x.flags["C_CONTIGUOUS"] or x.size < count:
+            raise ValueError("x must be a C-contiguous float64 array of at least r*n*d elements")
+        ptr = _ffi.device_pointer_of_host(x.ctypes.data)
+        if ptr is None:
+            raise ValueError("a numpy x must be pinned host memory (batch.pinned_empty)")
+        return ptr
+    _check_tensor(x, "x", count, (torch.float64,))
+    return x.data_ptr()
 
-    def __init__(self, r, n, n_start, dims, x):
-        torch = _torch()
-        r, n, n_start = int(r), int(n), int(n_start)
-        ints = (torch.int64, torch.uint64)
-        if not dims:
-            raise ValueError("need at least one dimension")
-        d = len(dims)
-        if isinstance(x, np.ndarray):
-            if x.dtype != np.float64 or not x.flags["C_CONTIGUOUS"] or x.size < r * n * d:
-                raise ValueError("x must be a C-contiguous float64 array of at least r*n*d elements")
-            x_ptr = _ffi.device_pointer_of_host(x.ctypes.data)
-            if x_ptr is None:
-                raise ValueError("a numpy x must be pinned host memory (batch.pinned_empty)")
-        else:
-            _check_tensor(x, "x", r * n * d, (torch.float64,))
-            x_ptr = x.data_ptr()
-        structs, keep = [], [x]
-        for j, q in enumerate(dims):
-            b, tmax, mmax = int(q["b"]), int(q["tmax"]), int(q["mmax"])
-            _check_tensor(q["C"], "dims[%d].C" % j, mmax * tmax, ints)
-            ptrs = {"C": q["C"].data_ptr()}
-            for key, count in (("S", r * tmax * tmax), ("perms", r * tmax * b), ("shifts", r * tmax)):
-                t = q.get(key)
-                if t is None:
-                    ptrs[key] = None
-                else:
-                    _check_tensor(t, "dims[%d].%s" % (j, key), count, ints)
-                    ptrs[key] = t.data_ptr()
-                    keep.append(t)
-            keep.append(q["C"])
-            structs.append(GdnDim(b=b, tmax=tmax, mmax=mmax, **ptrs))
-        self._h = _create(r, n, n_start, structs, x_ptr)
+
+def _dim_structs(r, dims, keep, tag):
+    torch = _torch()
+    ints = (torch.int64, torch.uint64)
+    if not dims:
+        raise ValueError("%s: need at least one dimension" % tag)
+    structs = []
+    for j, q in enumerate(dims):
+        b, tmax, mmax = int(q["b"]), int(q["tmax"]), int(q["mmax"])
+        _check_tensor(q["C"], "%sdims[%d].C" % (tag, j), mmax * tmax, ints)
+        ptrs = {"C": q["C"].data_ptr()}
+        for key, count in (("S", r * tmax * tmax), ("perms", r * tmax * b), ("shifts", r * tmax)):
+            t = q.get(key)
+            if t is None:
+                ptrs[key] = None
+            else:
+                _check_tensor(t, "%sdims[%d].%s" % (tag, j, key), count, ints)
+                ptrs[key] = t.data_ptr()
+                keep.append(t)
+        keep.append(q["C"])
+        structs.append(GdnDim(b=b, tmax=tmax, mmax=mmax, **ptrs))
+    return (GdnDim * len(structs))(*structs)
+
+
+class HaltonBatch:
+    """Many generalized-net requests of uneven (r, n, n_start, d, bases, digit
+    counts) in one plan: preparation and generation each one launch over all
+    requests.  Each request is a dict(r, n, n_start=0, dims=[...], x=...) with
+    the arrays of HaltonPlan.  The plan keeps the tensors alive; prepare()
+    reads S, C, perms and shifts (call it again after changing them), run()
+    writes every request's x; graph_launch(stream) does both from a CUDA graph
+    captured at the first call."""
+
+    def __init__(self, requests):
+        if not requests:
+            raise ValueError("need at least one request")
+        keep, structs, dim_arrays = [], [], []
+        for k, q in enumerate(requests):
+            r, n = int(q["r"]), int(q["n"])
+            d = len(q["dims"])
+            arr = _dim_structs(r, q["dims"], keep, "requests[%d]." % k)
+            dim_arrays.append(arr)
+            x = q["x"]
+            keep.append(x)
+            structs.append(HaltonRequest(r=r, n=n, n_start=int(q.get("n_start", 0)), d=d, dims=arr,
+                                         x=_x_pointer(x, r * n * d)))
+        reqs = (HaltonRequest * len(structs))(*structs)
+        h = _P()
+        _ffi.check(_lib().qmc_halton_batch_create(reqs, len(structs), _ct.byref(h)), "halton_batch_create")
+        self._h = h
         self._keep = keep
-        self.r, self.n, self.d = r, n, d
+        self.nreq = len(structs)
+        self.coords = sum(int(q["r"]) * int(q["n"]) * len(q["dims"]) for q in requests)
+        self.share = 1.0
 
     def prepare(self, stream=None):
         s = stream if stream is not None else _torch().cuda.current_stream()
@@ -127,10 +160,38 @@ class HaltonPlan:
         s = stream if stream is not None else _torch().cuda.current_stream()
         _ffi.check(_lib().qmc_halton_plan_run(self._h, s.cuda_stream), "halton_plan_run")
 
+    def graph_launch(self, stream):
+        _ffi.check(_lib().qmc_halton_plan_graph_launch(self._h, stream.cuda_stream), "halton_plan_graph_launch")
+
     def set_fp64_share(self, share):
         """Share of the digit adds run on the FP64 unit (the rest in integer
         arithmetic); the results are the same bits either way."""
         _ffi.check(_lib().qmc_halton_plan_set_fp64_share(self._h, float(share)), "halton_plan_set_fp64_share")
+        self.share = float(share)
+
+    def tune(self, stream=None, shares=(0.0, 0.5, 0.75, 1.0), reps=3, use_cache=True):
+        """Time run() at each FP64 share, keep the fastest, remember it for plans of the same
+        shape class (the autotuner cache of qmctoolscl_gb300.batch).  Returns (share, ms)."""
+        from . import batch
+        torch = _torch()
+        stream = stream if stream is not None else torch.cuda.current_stream()
+        key = "halton|coords2^%d|req2^%d|%s" % (int(np.log2(max(self.coords, 1))), int(np.log2(max(self.nreq, 1))),
+                                               batch._device_name())
+        if use_cache:
+            hit = batch._load_cache().get(key)
+            if hit:
+                self.set_fp64_share(hit[0])
+                return tuple(hit)
+        self.prepare(stream)
+        best = None
+        for sh in shares:
+            self.set_fp64_share(sh)
+            ms = batch.time_plan(self, stream, reps)
+            if best is None or ms < best[1]:
+                best = (sh, ms)
+        self.set_fp64_share(best[0])
+        batch._store_cache(key, list(best))
+        return best
 
     def close(self):
         if getattr(self, "_h", None):
@@ -142,6 +203,17 @@ class HaltonPlan:
             self.close()
         except Exception:
             pass
+
+
+class HaltonPlan(HaltonBatch):
+    """One fused generalized-net generation over device tensors (a batch of
+    one request).  x may also be a pinned float64 numpy array
+    (batch.pinned_empty): the kernel then writes the points straight into host
+    memory."""
+
+    def __init__(self, r, n, n_start, dims, x):
+        super().__init__([dict(r=r, n=n, n_start=n_start, dims=dims, x=x)])
+        self.r, self.n, self.d = int(r), int(n), len(dims)
 
 
 def generalized_net_fused(r, n, n_start, dims, x, check=True, stream=None):

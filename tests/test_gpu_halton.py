@@ -218,3 +218,59 @@ def test_halton_many_dimensions_one_point_per_lane():
     r, n, n_start = 1, 97, 31
     dims = make_dims(rng, r, big_primes, n_start + n - 1)
     assert same_bits(run_fused(r, n, n_start, dims), oracle_chain(r, n, n_start, dims))
+
+
+def _dev_dims(dims):
+    import torch
+    dev = lambda a: None if a is None else torch.from_numpy(np.ascontiguousarray(a).reshape(-1).view(np.int64)).cuda()  # noqa: E731
+    return [dict(b=dm["b"], tmax=dm["tmax"], mmax=dm["mmax"], C=dev(dm["C"]), S=dev(dm.get("S")),
+                 perms=dev(dm.get("perms")), shifts=dev(dm.get("shifts"))) for dm in dims]
+
+
+def test_halton_batch_of_uneven_requests():
+    """Requests of different r, n, n_start, dimension count, bases, digit
+    counts and randomisation steps in one plan (one preparation launch set,
+    one generation launch); each request's points equal its oracle chain.
+    Replayed from a CUDA graph, twice, with the same bits."""
+    import torch
+    rng = np.random.Generator(np.random.SFC64(77))
+    specs = [  # r, n, n_start, bases, lms, perm, shift
+        (2, 300, 5, [2, 3, 5, 7], True, True, True),
+        (1, 1000, 0, PRIMES[:40], True, False, True),
+        (3, 65, 2 ** 16 - 3, [541, 13, 2], False, True, False),
+        (1, 1, 7, [97], True, True, True),
+    ]
+    reqs, wants = [], []
+    for (r, n, n_start, bases, lms, perm, shift) in specs:
+        dims = make_dims(rng, r, bases, n_start + n - 1, lms=lms, perm=perm, shift=shift)
+        wants.append(oracle_chain(r, n, n_start, dims))
+        reqs.append(dict(r=r, n=n, n_start=n_start, dims=_dev_dims(dims),
+                         x=torch.full((r * n * len(bases),), float("nan"), dtype=torch.float64, device="cuda")))
+    plan = halton.HaltonBatch(reqs)
+    st = torch.cuda.Stream()
+    for _ in range(2):
+        for q in reqs:
+            q["x"].fill_(float("nan"))
+        plan.graph_launch(st)
+        st.synchronize()
+        for q, want, (r, n, _ns, bases, *_rest) in zip(reqs, wants, specs):
+            assert same_bits(q["x"].cpu().numpy().reshape(r, n, len(bases)), want)
+    plan.close()
+
+
+def test_halton_batch_tune_keeps_bits(tmp_path, monkeypatch):
+    """The tuner picks an FP64 share by timing; every share gives the same bits."""
+    import torch
+    monkeypatch.setenv("QMCGB_TUNE_CACHE", str(tmp_path / "tune.json"))
+    rng = np.random.Generator(np.random.SFC64(78))
+    r, n, n_start = 2, 4000, 11
+    dims = make_dims(rng, r, PRIMES[:24], n_start + n - 1)
+    want = oracle_chain(r, n, n_start, dims)
+    x = torch.empty(r * n * len(dims), dtype=torch.float64, device="cuda")
+    plan = halton.HaltonPlan(r, n, n_start, _dev_dims(dims), x)
+    share, ms = plan.tune(reps=2)
+    assert 0.0 <= share <= 1.0 and ms > 0
+    plan.prepare()
+    plan.run()
+    assert same_bits(x.cpu().numpy().reshape(r, n, -1), want)
+    assert plan.tune(reps=2)[0] == share  # cached
