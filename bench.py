@@ -914,6 +914,44 @@ def run_halton(args):
     t_e2e = (time.perf_counter() - t0) / e2e_steps
     assert np.array_equal(xh.view(np.uint64), x.cpu().numpy().view(np.uint64))
 
+    # uneven batch: 64 requests of random r (1-4), n (2^10-2^16), n_start, d (4-100, first d primes);
+    # one plan (graph replay: preparation + one generation launch) against one plan per request
+    urng = np.random.Generator(np.random.SFC64(44))
+    ureqs, uplans = [], []
+    upoints = ucoords = 0
+    for k in range(64):
+        ur, un = int(urng.integers(1, 5)), 1 << int(urng.integers(10, 17))
+        udim, ustart = int(urng.integers(4, 101)), int(urng.integers(0, 1 << 20))
+        udims = halton_inputs(ur, 21, udim, seed=1000 + k)  # mmax for indices below 2^21
+        dd = [dict(b=dm["b"], tmax=dm["tmax"], mmax=dm["mmax"], C=dev_tensor(dm["C"]), S=dev_tensor(dm["S"]),
+                   perms=dev_tensor(dm["perms"]), shifts=dev_tensor(dm["shifts"])) for dm in udims]
+        ux = torch.empty(ur * un * udim, dtype=torch.float64, device="cuda")
+        ureqs.append(dict(r=ur, n=un, n_start=ustart, dims=dd, x=ux))
+        upoints += ur * un
+        ucoords += ur * un * udim
+    ust = torch.cuda.Stream()
+    ubatch = halton.HaltonBatch(ureqs)
+    ms_u_graph = gpu_ms(lambda: ubatch.graph_launch(ust), args.steps, args.warmup, ust)
+    with torch.cuda.stream(ust):
+        singles = [halton.HaltonPlan(q_["r"], q_["n"], q_["n_start"], q_["dims"], q_["x"]) for q_ in ureqs]
+
+        def per_request():
+            for pl in singles:
+                pl.prepare(ust)
+                pl.run(ust)
+
+        ms_u_single = gpu_ms(per_request, max(3, args.steps // 2), 2, ust)
+    torch.cuda.synchronize()
+    # parity: the last request's first 256 points of randomisation 0 against the oracle
+    lq = ureqs[-1]
+    lw = halton_oracle(halton_inputs(lq["r"], 21, len(lq["dims"]), seed=1000 + 63), 0, lq["n_start"], 256)
+    lg = lq["x"].view(lq["r"], lq["n"], -1)[0, :256].cpu().numpy()
+    assert np.array_equal(lg.view(np.uint64), lw.view(np.uint64)), "Halton batch differs from the oracle"
+    for pl in singles:
+        pl.close()
+    ubatch.close()
+    del ureqs, singles
+
     # CPU: the oracle chain on a sample of randomisation 0, all host threads
     threads = host_threads()
     pieces = [(0, k * 4096, 4096) for k in range(2 * threads)]
@@ -938,6 +976,10 @@ def run_halton(args):
                              note="generation kernel alone; bound by instruction issue (integer + FP64 adds), "
                                   "not HBM"),
             "generate_only_ms": ms_gen,
+            "uneven_batch": {"requests": 64, "points": upoints, "coords": ucoords, "graph_ms": ms_u_graph,
+                             "per_request_plans_ms": ms_u_single, "speedup": ms_u_single / ms_u_graph,
+                             "launches": {"graph": 5, "per_request": 5 * 64},
+                             "achieved_gbs": 8.0 * ucoords / (ms_u_graph / 1e3) / 1e9},
             "fp64_share": {"chosen": best_share, "generate_ms_by_share": {str(k): v for k, v in sweep.items()}},
             "plain": {"ms_per_step": ms_plain, "points_per_s": pts / (ms_plain / 1e3), "launches_per_step": 5 * d,
                       "digit_tensor_bytes": digit_bytes, "fused_speedup": ms_plain / ms_fused},

@@ -444,9 +444,7 @@ int qmc_net_plan_create(const qmc_net_request *reqs, int nreq, qmc_plan **plan)
             R.C = p->d_scratch + (uintptr_t)R.C;
             R.pad = 0;
         }
-    if (!rc && p->smem > 48 * 1024)
-        rc = qmcgb::cuda_status(cudaFuncSetAttribute(net_batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                     (int)p->smem), "cudaFuncSetAttribute");
+    if (!rc) rc = qmcgb::raise_smem_limit((const void *)net_batch_kernel, p->smem, "net_batch_kernel smem");
     if (!rc) rc = layout_tiles(p);
     if (rc) {
         qmc_plan_destroy(p);

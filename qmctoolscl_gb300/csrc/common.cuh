@@ -206,6 +206,12 @@ inline unsigned grid_for(u64 work, unsigned per_block, unsigned cap)
 
 int sm_count();
 
+// Raise the kernel's dynamic shared-memory limit to at least `bytes` (no-op up
+// to the default 48 KB).  The limit is one attribute per kernel and device:
+// it is only ever raised (a high-water mark kept under a lock), so a launch
+// prepared for one size is never broken by a later, smaller setting.
+int raise_smem_limit(const void *func, size_t bytes, const char *what);
+
 // base-2 net generation with optional fused digital shift / float output
 // (dnb2.cu); stream-ordered, allocates nothing
 int dnb2_gen_fused(u64 r, u64 n, u64 d, u64 n_start, u64 mmax, const u64 *C, u64 r_C, int gray,

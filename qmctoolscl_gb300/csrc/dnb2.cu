@@ -269,10 +269,7 @@ int launch_gen(GenArgs a, cudaStream_t s, const char *what)
     a.rows_per_cta = (a.n + splits - 1) / splits;
     const size_t smem = net::table_words(a.K, a.mmax, ncols) * sizeof(u64);
     auto kern = dnb2_gen_kernel<GRAY>;
-    if (smem > 48 * 1024) {
-        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess) return qmcgb::cuda_status(e, what);
-    }
+    if (int rc = qmcgb::raise_smem_limit((const void *)kern, smem, what)) return rc;
     // blockIdx.y enumerates (randomisation, column tile), at most 65535 per launch
     const u64 l_per_launch = 65535 / a.col_tiles;
     for (u64 l0 = 0; l0 < a.r; l0 += l_per_launch) {

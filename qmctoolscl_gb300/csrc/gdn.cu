@@ -813,12 +813,7 @@ int gen_tiled(u64 r, u64 n, u64 d, u64 r_b, u64 mmax, u64 tmax, u64 n_start, con
     const u64 groups_per_cta = (ngroups + splits - 1) / splits;
     const u64 nx = (ngroups + groups_per_cta - 1) / groups_per_cta;
     const size_t smem = gt_smem(mmax, tmax);
-    if (smem > 48 * 1024) {
-        if (int rc = qmcgb::cuda_status(cudaFuncSetAttribute(gdn_gen_tiled_kernel,
-                                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
-                                        what))
-            return rc;
-    }
+    if (int rc = qmcgb::raise_smem_limit((const void *)gdn_gen_tiled_kernel, smem, what)) return rc;
     for (u64 u0 = 0; u0 < units; u0 += 65535) {
         const unsigned cnt = (unsigned)(units - u0 < 65535 ? units - u0 : 65535);
         gdn_gen_tiled_kernel<<<dim3((unsigned)nx, cnt, 1), THREADS, smem, st>>>(

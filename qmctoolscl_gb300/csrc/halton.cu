@@ -538,11 +538,9 @@ int run_launch(qmc_halton_plan *p, cudaStream_t st)
 template <u32 PPL>
 int gen_smem_attr(size_t smem)
 {
-    const int v = (int)smem;
-    cudaError_t e = cudaFuncSetAttribute(halton_gen_kernel<PPL, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, v);
-    if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(halton_gen_kernel<PPL, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, v);
-    return qmcgb::cuda_status(e, "cudaFuncSetAttribute");
+    if (int rc = qmcgb::raise_smem_limit((const void *)halton_gen_kernel<PPL, true>, smem, "halton_gen_kernel smem"))
+        return rc;
+    return qmcgb::raise_smem_limit((const void *)halton_gen_kernel<PPL, false>, smem, "halton_gen_kernel smem");
 }
 
 }  // namespace

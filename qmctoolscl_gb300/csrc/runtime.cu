@@ -3,6 +3,10 @@
 #include <stdio.h>
 #include <string.h>
 
+#include <map>
+#include <mutex>
+#include <utility>
+
 #include "common.cuh"
 
 namespace qmcgb {
@@ -25,6 +29,22 @@ int cuda_status(cudaError_t e, const char *what)
 }
 
 int launch_status(const char *what) { return cuda_status(cudaGetLastError(), what); }
+
+int raise_smem_limit(const void *func, size_t bytes, const char *what)
+{
+    if (bytes <= 48 * 1024) return QMC_OK;
+    static std::mutex mu;
+    static std::map<std::pair<int, const void *>, size_t> high;
+    int dev = 0;
+    if (int rc = cuda_status(cudaGetDevice(&dev), what)) return rc;
+    std::lock_guard<std::mutex> lock(mu);
+    size_t &cur = high[{dev, func}];
+    if (bytes <= cur) return QMC_OK;
+    if (int rc = cuda_status(cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes), what))
+        return rc;
+    cur = bytes;
+    return QMC_OK;
+}
 
 // One word per loaded library and device; kernels OR error codes into it.
 __device__ unsigned int g_device_error;

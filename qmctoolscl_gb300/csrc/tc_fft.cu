@@ -72,10 +72,7 @@ extern "C" int qmc_tc_mma_probe(const void *A, const void *B, float *D, uint32_t
     u32 tcols = 32;
     while (tcols < N) tcols <<= 1;
     const size_t smem = (size_t)(128 + N) * K * 2;
-    if (smem > 48 * 1024) {
-        cudaError_t e = cudaFuncSetAttribute(tc_probe_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess) return qmcgb::cuda_status(e, "tc probe smem");
-    }
+    if (int rc = qmcgb::raise_smem_limit((const void *)tc_probe_kernel, smem, "tc probe smem")) return rc;
     tc_probe_kernel<<<1, 128, smem, QMC_STREAM(s)>>>((const __nv_bfloat16 *)A, (const __nv_bfloat16 *)B, D, N, K,
                                                      tcols, err);
     return qmcgb::launch_status("tc_probe_kernel");
@@ -554,18 +551,16 @@ int run_tc(int kind, u64 d1, u64 d2, u64 n_half, double *xr, double *xi, cudaStr
         A.scale = (pi == np - 1) ? scale : 1.0f;
         const u64 tiles = (p.k0 == 0) ? (A.total + FT_TILE - 1) / FT_TILE : A.total / (A.Q * (u64)A.ct);
         const unsigned grid = qmcgb::grid_for(tiles, 1, (unsigned)qmcgb::sm_count() * 3);  // 3 CTAs per SM fit
-        cudaError_t e;
         if (kind == TC_FFT) {
-            e = cudaFuncSetAttribute(tc_pass_kernel<TC_FFT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-            if (e == cudaSuccess) tc_pass_kernel<TC_FFT><<<grid, FT_THREADS, smem, s>>>(A, err);
+            if (int rc = qmcgb::raise_smem_limit((const void *)tc_pass_kernel<TC_FFT>, smem, what)) return rc;
+            tc_pass_kernel<TC_FFT><<<grid, FT_THREADS, smem, s>>>(A, err);
         } else if (kind == TC_IFFT) {
-            e = cudaFuncSetAttribute(tc_pass_kernel<TC_IFFT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-            if (e == cudaSuccess) tc_pass_kernel<TC_IFFT><<<grid, FT_THREADS, smem, s>>>(A, err);
+            if (int rc = qmcgb::raise_smem_limit((const void *)tc_pass_kernel<TC_IFFT>, smem, what)) return rc;
+            tc_pass_kernel<TC_IFFT><<<grid, FT_THREADS, smem, s>>>(A, err);
         } else {
-            e = cudaFuncSetAttribute(tc_pass_kernel<TC_WHT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-            if (e == cudaSuccess) tc_pass_kernel<TC_WHT><<<grid, FT_THREADS, smem, s>>>(A, err);
+            if (int rc = qmcgb::raise_smem_limit((const void *)tc_pass_kernel<TC_WHT>, smem, what)) return rc;
+            tc_pass_kernel<TC_WHT><<<grid, FT_THREADS, smem, s>>>(A, err);
         }
-        if (e != cudaSuccess) return qmcgb::cuda_status(e, what);
         if (int rc = qmcgb::launch_status(what)) return rc;
     }
     return QMC_OK;

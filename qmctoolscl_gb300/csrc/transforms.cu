@@ -194,18 +194,16 @@ int run_transform(int kind, u64 d1, u64 d2, u64 n_half, double *twr, double *twi
         const size_t smem = (size_t)elems * sizeof(double) * (kind == FT_FWHT ? 1 : 2);
         const u64 tiles = nvec * (n >> p.k1) * ((1ull << p.k0) / p.ct);
         const unsigned grid = qmcgb::grid_for(tiles, 1, (unsigned)qmcgb::sm_count() * 8);
-        cudaError_t e = cudaSuccess;
         if (kind == FT_FFT) {
-            e = cudaFuncSetAttribute(ft_pass_kernel<FT_FFT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-            if (e == cudaSuccess) ft_pass_kernel<FT_FFT><<<grid, FT_THREADS, smem, s>>>(a);
+            if (int rc = qmcgb::raise_smem_limit((const void *)ft_pass_kernel<FT_FFT>, smem, what)) return rc;
+            ft_pass_kernel<FT_FFT><<<grid, FT_THREADS, smem, s>>>(a);
         } else if (kind == FT_IFFT) {
-            e = cudaFuncSetAttribute(ft_pass_kernel<FT_IFFT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-            if (e == cudaSuccess) ft_pass_kernel<FT_IFFT><<<grid, FT_THREADS, smem, s>>>(a);
+            if (int rc = qmcgb::raise_smem_limit((const void *)ft_pass_kernel<FT_IFFT>, smem, what)) return rc;
+            ft_pass_kernel<FT_IFFT><<<grid, FT_THREADS, smem, s>>>(a);
         } else {
-            e = cudaFuncSetAttribute(ft_pass_kernel<FT_FWHT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-            if (e == cudaSuccess) ft_pass_kernel<FT_FWHT><<<grid, FT_THREADS, smem, s>>>(a);
+            if (int rc = qmcgb::raise_smem_limit((const void *)ft_pass_kernel<FT_FWHT>, smem, what)) return rc;
+            ft_pass_kernel<FT_FWHT><<<grid, FT_THREADS, smem, s>>>(a);
         }
-        if (e != cudaSuccess) return qmcgb::cuda_status(e, what);
         if (int rc = qmcgb::launch_status(what)) return rc;
     }
     return QMC_OK;

@@ -274,3 +274,23 @@ def test_halton_batch_tune_keeps_bits(tmp_path, monkeypatch):
     plan.run()
     assert same_bits(x.cpu().numpy().reshape(r, n, -1), want)
     assert plan.tune(reps=2)[0] == share  # cached
+
+
+def test_halton_plans_of_different_sizes_coexist():
+    """Plans whose output tiles need different shared-memory sizes (above the
+    default 48 KB) are created one after the other, then the larger one runs:
+    creating the smaller must not lower the kernel's limit below it."""
+    import torch
+    rng = np.random.Generator(np.random.SFC64(79))
+    plans, wants, xs = [], [], []
+    for d in (100, 97):
+        r, n = 1, 70
+        dims = make_dims(rng, r, PRIMES[:d], n - 1)
+        wants.append(oracle_chain(r, n, 0, dims))
+        x = torch.empty(r * n * d, dtype=torch.float64, device="cuda")
+        xs.append(x)
+        plans.append(halton.HaltonPlan(r, n, 0, _dev_dims(dims), x))
+    for plan, x, want in zip(plans, xs, wants):
+        plan.prepare()
+        plan.run()
+        assert same_bits(x.cpu().numpy().reshape(1, 70, -1), want)
