@@ -744,7 +744,10 @@ def run_fft(args):
     fp64_vs_numpy = float(np.linalg.norm(got - want) / np.linalg.norm(want))
     worst = max(e["fft_max"] for e in err.values())
     passes = lambda l: 1 if l <= 12 else 2  # noqa: E731
-    alg_tc = sum(32.0 * g["n"] * g["cnt"] * passes(g["L"]) for g in groups)
+    # bytes per complex sample: one pass reads and writes FP64 (re, im), 32 B; two passes
+    # read FP64 and write the FP32 intermediate (24 B), then read it and write FP64 (24 B)
+    per_sample = lambda l: 32.0 if l <= 12 else 48.0  # noqa: E731
+    alg_tc = sum(per_sample(g["L"]) * g["n"] * g["cnt"] for g in groups)
     return {"metric": METRIC, "value": samples / (ms["fft_tc"] / 1e3) / 1e9, "unit": "Gsamples/s", "n_gpus": 1,
             "steps": steps, "warmup": warm, "ms_per_step": ms["fft_tc"], "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "bf16x3 products, fp32 accumulate, fp64 I/O",
@@ -753,8 +756,9 @@ def run_fft(args):
                        "samples": samples, "lengths": counts},
             "roofline": dict(roofline(alg_tc, ms["fft_tc"]), kernel="tc_pass_kernel<FFT> (all passes of a step)",
                              traffic=alg_tc * TC_FFT_TRAFFIC_RATIO,
-                             note="32 B per complex sample per pass (FP64 read+write); traffic = algorithmic bytes x "
-                                  "the DRAM/algorithmic ratio of the ncu capture in profiles/tc_pass_kernel_fft_n2p20.md"),
+                             note="32 B per complex sample for one pass (FP64 read+write), 48 B for two (FP64 in, "
+                                  "FP32 intermediate, FP64 out); traffic = algorithmic bytes x the DRAM/algorithmic "
+                                  "ratio of the ncu capture in profiles/tc_pass_kernel_fft_n2p20.md"),
             "fp64": {"fft_ms": ms["fft_fp64"], "fwht_ms": ms["fwht_fp64"],
                      "fft_gsamples_per_s": samples / (ms["fft_fp64"] / 1e3) / 1e9,
                      "fp64_vs_numpy_rel_l2": fp64_vs_numpy},

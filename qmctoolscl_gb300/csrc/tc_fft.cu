@@ -92,7 +92,10 @@ extern "C" int qmc_tc_mma_probe(const void *A, const void *B, float *D, uint32_t
 // [k0, k1) on tiles of 4096 values: pass 1 bits [0, min(L,12)) on contiguous
 // blocks (several short vectors per tile), pass 2 bits [12, L) on tiles of
 // Q = 2^(L-12) rows by 4096/Q consecutive columns.  The FFT runs pass 1
-// first, the inverse pass 2 first.
+// first, the inverse pass 2 first.  Between the passes of a complex
+// transform the data stay FP32: element f's (re, im) pair is written into the
+// eight bytes of xr[f], which only the tile holding f reads or writes, and the
+// last pass writes FP64 xr and xi again.
 //
 // Radix-16 step.  The reference's radix-2 stages k..k+3 on bit-reversed
 // input, fused, act on groups of 16 values at positions base + p*2^k
@@ -158,6 +161,7 @@ struct TcPassArgs {
     u32 Q;           // tile rows
     double *xr, *xi;
     float scale;     // applied on write-back when != 1
+    u32 in32, out32; // the pass reads / writes the FP32 intermediate instead of the FP64 arrays
 };
 
 __device__ __forceinline__ u32 brev4(u32 p) { return __brev(p) >> 28; }
@@ -270,12 +274,12 @@ __global__ void __launch_bounds__(FT_THREADS, 3) tc_pass_kernel(TcPassArgs a, un
     u32 phase = 0;
     bool ok = true;
 
-    const u64 n = 1ull << a.L;
     const u32 Q = a.Q, ct = a.ct;
-    const u64 cchunks = (a.k0 == 0) ? 1 : ((1ull << a.k0) / ct);
-    const u64 hchunks = (a.k0 == 0) ? 1 : (n >> a.k1);
-    const u64 tiles_per_vec = cchunks * hchunks;
-    const u64 ntiles = (a.k0 == 0) ? (a.total + FT_TILE - 1) / FT_TILE : (a.total / n) * tiles_per_vec;
+    // ct, the column and row chunk counts and n are powers of two: index math by shifts
+    const u32 ctl = 31 - __clz(ct), ctm = ct - 1;
+    const u32 cchl = (a.k0 == 0) ? 0 : a.k0 - ctl;       // log2 column chunks: 2^k0 / ct
+    const u32 tpvl = (a.k0 == 0) ? 0 : cchl + (a.L - a.k1);  // log2 tiles per vector
+    const u64 ntiles = (a.k0 == 0) ? (a.total + FT_TILE - 1) / FT_TILE : (a.total >> a.L) << tpvl;
     const float tw_sign = (KIND == TC_FFT) ? -1.0f : 1.0f;
 
     for (u64 tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
@@ -283,20 +287,40 @@ __global__ void __launch_bounds__(FT_THREADS, 3) tc_pass_kernel(TcPassArgs a, un
         if (a.k0 == 0) {
             base = tile * FT_TILE;
         } else {
-            const u64 v = tile / tiles_per_vec, rem = tile % tiles_per_vec;
-            base = v * n + (rem / cchunks) * (1ull << a.k1) + (rem % cchunks) * ct;
+            const u64 v = tile >> tpvl, rem = tile & ((1ull << tpvl) - 1);
+            base = (v << a.L) + ((rem >> cchl) << a.k1) + ((rem & ((1ull << cchl) - 1)) << ctl);
         }
         // load (zeros beyond the data): pairs of adjacent elements as 16-byte loads, all of a
         // thread's raw bits in flight before the conversions (whose rare out-of-line fallback
         // would otherwise serialise the loads).  Q * ct is even and ct is 1 (pass 1) or even,
         // so a pair never straddles two rows; a.total is a multiple of n >= 2.
-        {
+        if (KIND != TC_WHT && a.in32) {
+            // the FP32 intermediate of the previous pass: element f's (re, im) in the 8 bytes of xr[f]
+            constexpr u32 PAIRS = FT_TILE / (2 * FT_THREADS);  // 8
+            float4 b[PAIRS];
+#pragma unroll
+            for (u32 i = 0; i < PAIRS; i++) {
+                const u32 e = 2 * (threadIdx.x + i * FT_THREADS);
+                const u64 f = base + ((u64)(e >> ctl) << a.k0) + (e & ctm);
+                b[i] = (e < Q * ct && f < a.total) ? *(const float4 *)(a.xr + f) : make_float4(0.f, 0.f, 0.f, 0.f);
+            }
+#pragma unroll
+            for (u32 i = 0; i < PAIRS; i++) {
+                const u32 e = 2 * (threadIdx.x + i * FT_THREADS);
+                if (e < Q * ct) {
+                    sr[slot(e)] = b[i].x;
+                    si[slot(e)] = b[i].y;
+                    sr[slot(e + 1)] = b[i].z;
+                    si[slot(e + 1)] = b[i].w;
+                }
+            }
+        } else {
             constexpr u32 PAIRS = FT_TILE / (2 * FT_THREADS);  // 8
             ulonglong2 br[PAIRS], bi[PAIRS];
 #pragma unroll
             for (u32 i = 0; i < PAIRS; i++) {
                 const u32 e = 2 * (threadIdx.x + i * FT_THREADS);
-                const u64 f = base + ((u64)(e / ct) << a.k0) + (e % ct);
+                const u64 f = base + ((u64)(e >> ctl) << a.k0) + (e & ctm);
                 const bool in = e < Q * ct && f < a.total;
                 br[i] = in ? *(const ulonglong2 *)(a.xr + f) : make_ulonglong2(0, 0);
                 bi[i] = (in && KIND != TC_WHT) ? *(const ulonglong2 *)(a.xi + f) : make_ulonglong2(0, 0);
@@ -332,7 +356,7 @@ __global__ void __launch_bounds__(FT_THREADS, 3) tc_pass_kernel(TcPassArgs a, un
             if (w == 1) {
                 // FP32 radix-2 butterflies on bit k (as the reference's stage)
                 for (u32 b = threadIdx.x; b < Q * ct / 2; b += FT_THREADS) {
-                    const u32 cc = b % ct, pq = b / ct;
+                    const u32 cc = b & ctm, pq = b >> ctl;
                     const u32 q1 = ((pq >> lo) << (lo + 1)) | (pq & ((1u << lo) - 1));
                     const u32 e1 = slot(q1 * ct + cc), e2 = slot(q1 * ct + cc + (1u << lo) * ct);
                     if (KIND == TC_WHT) {
@@ -365,7 +389,7 @@ __global__ void __launch_bounds__(FT_THREADS, 3) tc_pass_kernel(TcPassArgs a, un
                 // component).  Members are split two at a time with packed BF16x2 conversions.
                 {
                     const u32 gi = 128 * mt + (threadIdx.x & 127), half = threadIdx.x >> 7;
-                    const u32 cc = gi % ct, qq = gi / ct;
+                    const u32 cc = gi & ctm, qq = gi >> ctl;
                     const u32 qlo = qq & ((1u << lo) - 1), qhi = qq >> lo;
                     const u32 row = threadIdx.x & 127;
                     const u32 S = (1u << lo) * ct;
@@ -445,7 +469,7 @@ __global__ void __launch_bounds__(FT_THREADS, 3) tc_pass_kernel(TcPassArgs a, un
                 // read back: warps 0-3 the real outputs, warps 4-7 the imaginary ones
                 {
                     const u32 gi = 128 * mt + 32 * (warp & 3) + lane;
-                    const u32 cc = gi % ct, qq = gi / ct;
+                    const u32 cc = gi & ctm, qq = gi >> ctl;
                     const u32 qlo = qq & ((1u << lo) - 1), qhi = qq >> lo;
                     const u32 S = (1u << lo) * ct;
                     const u32 e0 = (qlo | (qhi << (lo + 4))) * ct + cc;
@@ -472,7 +496,7 @@ __global__ void __launch_bounds__(FT_THREADS, 3) tc_pass_kernel(TcPassArgs a, un
                 if (KIND == TC_IFFT) {
                     // post-twiddle w^-br(q) of the inverse step
                     const u32 gi = 128 * mt + (threadIdx.x & 127), half = threadIdx.x >> 7;
-                    const u32 cc = gi % ct, qq = gi / ct;
+                    const u32 cc = gi & ctm, qq = gi >> ctl;
                     const u32 qlo = qq & ((1u << lo) - 1), qhi = qq >> lo;
                     const u32 S = (1u << lo) * ct;
                     const u32 e0 = (qlo | (qhi << (lo + 4))) * ct + cc + half * 8 * S;
@@ -496,8 +520,12 @@ __global__ void __launch_bounds__(FT_THREADS, 3) tc_pass_kernel(TcPassArgs a, un
         if (!ok) break;
         // store, pairs of adjacent elements as 16-byte stores
         for (u32 e = 2 * threadIdx.x; e < Q * ct; e += 2 * FT_THREADS) {
-            const u64 f = base + ((u64)(e / ct) << a.k0) + (e % ct);
-            if (f < a.total) {
+            const u64 f = base + ((u64)(e >> ctl) << a.k0) + (e & ctm);
+            if (KIND != TC_WHT && a.out32) {
+                // FP32 intermediate for the next pass, in the bytes of this tile's own xr elements
+                if (f < a.total)
+                    *(float4 *)(a.xr + f) = make_float4(sr[slot(e)], si[slot(e)], sr[slot(e + 1)], si[slot(e + 1)]);
+            } else if (f < a.total) {
                 *(double2 *)(a.xr + f) = make_double2(to_f64(sr[slot(e)] * a.scale), to_f64(sr[slot(e + 1)] * a.scale));
                 if (KIND != TC_WHT)
                     *(double2 *)(a.xi + f) =
@@ -549,6 +577,11 @@ int run_tc(int kind, u64 d1, u64 d2, u64 n_half, double *xr, double *xi, cudaStr
         A.xr = xr;
         A.xi = xi;
         A.scale = (pi == np - 1) ? scale : 1.0f;
+        // between passes the complex transform keeps FP32 (re, im) pairs in xr's bytes: a
+        // quarter less traffic than FP64 arrays and no conversions; the values are the FP32
+        // ones the FP64 round trip would restore exactly
+        A.in32 = (kind != TC_WHT && pi > 0) ? 1u : 0u;
+        A.out32 = (kind != TC_WHT && pi < np - 1) ? 1u : 0u;
         const u64 tiles = (p.k0 == 0) ? (A.total + FT_TILE - 1) / FT_TILE : A.total / (A.Q * (u64)A.ct);
         const unsigned grid = qmcgb::grid_for(tiles, 1, (unsigned)qmcgb::sm_count() * 3);  // 3 CTAs per SM fit
         if (kind == TC_FFT) {

@@ -36,7 +36,7 @@ def _bitrev(m):
 
 
 @pytest.mark.parametrize("m,d1,d2", [(1, 1, 1), (4, 2, 3), (5, 1, 1), (8, 3, 5), (10, 2, 2), (11, 1, 3), (12, 2, 1),
-                                     (13, 1, 2), (16, 1, 1), (17, 2, 1), (20, 1, 1)])
+                                     (13, 1, 2), (16, 1, 1), (17, 2, 1), (20, 1, 1), (22, 1, 1), (24, 1, 1)])
 def test_tc_fft_and_inverse_against_numpy(m, d1, d2):
     from qmctoolscl_gb300 import tc_fft
     rng = np.random.Generator(np.random.SFC64(m))
@@ -52,7 +52,7 @@ def test_tc_fft_and_inverse_against_numpy(m, d1, d2):
     assert err2 < 1e-6, err2
 
 
-@pytest.mark.parametrize("m", [1, 4, 7, 12, 14, 19])
+@pytest.mark.parametrize("m", [1, 4, 7, 12, 14, 19, 22])
 def test_tc_fwht_against_fp64(m):
     from qmctoolscl_gb300 import tc_fft
     import qmctoolscl_gb300 as q
