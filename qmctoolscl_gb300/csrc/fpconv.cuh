@@ -24,34 +24,35 @@ typedef unsigned int u32;
 // FP32 bits of RN(x) for the FP64 bits b; false outside zero and the normal FP32 range
 FPC_HD bool f64_to_f32_bits(u64 b, u32 &out)
 {
-    const u32 hi = (u32)(b >> 32), lo = (u32)b;
+    const u32 hi = (u32)(b >> 32);
     const u32 sign = hi & 0x80000000u;
-    if ((b << 1) == 0) {  // +-0
-        out = sign;
-        return true;
+    // FP32 biased exponent e - 896 must lie in [1, 254]: e in [897, 1150]
+    if ((hi & 0x7FFFFFFFu) - (897u << 20) >= (254u << 20)) {
+        if ((b << 1) == 0) {  // +-0
+            out = sign;
+            return true;
+        }
+        return false;
     }
-    const u32 e = (hi >> 20) & 0x7FFu;
-    // FP32 biased exponent e - 896 must lie in [1, 254]
-    if (e - 897u > 253u) return false;
-    const u32 m = ((hi & 0xFFFFFu) << 3) | (lo >> 29);  // the top 23 fraction bits
-    const u32 rem = lo & 0x1FFFFFFFu;                   // the 29 dropped bits
-    u32 r = ((e - 896u) << 23) | m;
-    r += (u32)((rem > 0x10000000u) | ((rem == 0x10000000u) & (m & 1u)));  // a carry bumps the exponent
-    out = sign | r;
+    // round to nearest even at bit 29: add half a unit less one, plus the kept last bit; the
+    // rounded significand's carry runs into the exponent field (up to inf past the largest float)
+    const u64 a = (b & 0x7FFFFFFFFFFFFFFFull) + 0x0FFFFFFFull + ((b >> 29) & 1u);
+    // bits 29.. of a are (e << 23) | fraction; rebias mod 2^32 (the result is below 2^31)
+    out = ((u32)(a >> 29) - (896u << 23)) + sign;
     return true;
 }
 
 // FP64 bits of the FP32 value with bits u (exact); false for subnormals, inf and nan
 FPC_HD bool f32_to_f64_bits(u32 u, u64 &out)
 {
-    const u32 sign = u & 0x80000000u;
-    if ((u << 1) == 0) {
-        out = (u64)sign << 32;
-        return true;
+    if ((u << 1) - 0x01000000u >= 0xFE000000u) {  // biased exponent 0 or 255
+        if ((u << 1) == 0) {
+            out = (u64)(u & 0x80000000u) << 32;
+            return true;
+        }
+        return false;
     }
-    const u32 E = (u >> 23) & 0xFFu;
-    if (E - 1u > 253u) return false;
-    const u32 hi = sign | ((E + 896u) << 20) | ((u & 0x7FFFFFu) >> 3);
+    const u32 hi = (u & 0x80000000u) + ((u & 0x7FFFFFFFu) >> 3) + (896u << 20);
     out = ((u64)hi << 32) | (u64)(u << 29);
     return true;
 }

@@ -208,9 +208,9 @@ __device__ __forceinline__ float step_matrix(u32 kk, u32 n)
 // splits into the quarter J >> 30, the table index (J >> 20) mod 1024, and,
 // when bits > 12, a remainder below 2 pi / 4096 whose sine and cosine are
 // two-term series (the next terms are below 2^-40).
-__device__ __forceinline__ void twiddle(const float2 *tab, u32 t, u32 bits, float sign, float &wr, float &wi)
+// twiddle_turn takes the angle J / 2^32 of a turn directly (J = t << (32 - bits)).
+__device__ __forceinline__ void twiddle_turn(const float2 *tab, u32 J, u32 bits, float sign, float &wr, float &wi)
 {
-    const u32 J = t << (32 - bits);
     const float2 e = tab[(J >> 20) & 1023u];  // (cos, -sin) of 2 pi r / 4096
     float c = e.x, sn = e.y;
     const u32 quarter = J >> 30;              // times (-i)^quarter
@@ -233,6 +233,11 @@ __device__ __forceinline__ void twiddle(const float2 *tab, u32 t, u32 bits, floa
     }
     wr = c;
     wi = sign < 0.0f ? sn : -sn;
+}
+
+__device__ __forceinline__ void twiddle(const float2 *tab, u32 t, u32 bits, float sign, float &wr, float &wi)
+{
+    twiddle_turn(tab, t << (32 - bits), bits, sign, wr, wi);
 }
 
 template <int KIND>
@@ -394,8 +399,11 @@ __global__ void __launch_bounds__(FT_THREADS, 3) tc_pass_kernel(TcPassArgs a, un
                     const u32 row = threadIdx.x & 127;
                     const u32 S = (1u << lo) * ct;
                     const u32 e0 = (qlo | (qhi << (lo + 4))) * ct + cc + half * 8 * S;
-                    // the group's offset below bit k, the same for all its members
+                    // the group's offset below bit k, the same for all its members; member
+                    // half*8 + p (p < 8) has br = 2*brev3(p) + half, so its twiddle angle as a
+                    // fraction of a turn is J = cg*half + 2*cg*brev3(p) with cg = c << (28 - k)
                     const u32 cgrp = ((u32)base + (qlo << a.k0) + cc) & ((1u << k) - 1);
+                    const u32 cg = cgrp << (28 - k), cgh = half ? cg : 0u;
                     u32 pr[3][4], pim[3][4];  // [split][pair of members]: two BF16 per word
 #pragma unroll
                     for (u32 pp = 0; pp < 8; pp += 2) {
@@ -407,8 +415,7 @@ __global__ void __launch_bounds__(FT_THREADS, 3) tc_pass_kernel(TcPassArgs a, un
                             xi2[h] = (KIND == TC_WHT) ? 0.0f : si[e];
                             if (KIND == TC_FFT && k > 0) {  // pre-twiddle w^br(p) (w = 1 on the first step)
                                 float wr, wi;
-                                twiddle(tab, (cgrp * brev4(half * 8 + pp + h)) & ((1u << (k + 4)) - 1), k + 4, -1.0f,
-                                        wr, wi);
+                                twiddle_turn(tab, cgh + 2u * cg * (brev4(pp + h) >> 1), k + 4, -1.0f, wr, wi);
                                 const float tr = xr2[h] * wr - xi2[h] * wi;
                                 xi2[h] = xr2[h] * wi + xi2[h] * wr;
                                 xr2[h] = tr;
@@ -501,12 +508,13 @@ __global__ void __launch_bounds__(FT_THREADS, 3) tc_pass_kernel(TcPassArgs a, un
                     const u32 S = (1u << lo) * ct;
                     const u32 e0 = (qlo | (qhi << (lo + 4))) * ct + cc + half * 8 * S;
                     const u32 cgrp = ((u32)base + (qlo << a.k0) + cc) & ((1u << k) - 1);
+                    const u32 cg = cgrp << (28 - k), cgh = half ? cg : 0u;
                     if (k > 0) {
 #pragma unroll
                         for (u32 pp = 0; pp < 8; pp++) {
                             const u32 e = slot(e0 + pp * S);
                             float wr, wi;
-                            twiddle(tab, (cgrp * brev4(half * 8 + pp)) & ((1u << (k + 4)) - 1), k + 4, 1.0f, wr, wi);
+                            twiddle_turn(tab, cgh + 2u * cg * (brev4(pp) >> 1), k + 4, 1.0f, wr, wi);
                             const float xr_ = sr[e], xi_ = si[e];
                             sr[e] = xr_ * wr - xi_ * wi;
                             si[e] = xr_ * wi + xi_ * wr;
