@@ -370,13 +370,17 @@ __device__ __forceinline__ void dim_value(const HDim &D, const u32 *Cj, const u6
                     y[q][u] = done[q] ? 0ull : Yj[(t + u) * D.b + dim_mod(D, acc)];
                 }
             }
+            if (ADD == ADD_INT) {
 #pragma unroll
-            for (u32 u = 0; u < HT_GROUP; u++) {
+                for (u32 u = 0; u < HT_GROUP; u++) {
 #pragma unroll
-                for (u32 q = 0; q < PPL; q++) {
-                    if (ADD == ADD_INT)
-                        add_term_int(vi[q], y[q][u]);
-                    else
+                    for (u32 q = 0; q < PPL; q++) add_term_int(vi[q], y[q][u]);
+                }
+            } else {
+#pragma unroll
+                for (u32 u = 0; u < HT_GROUP; u++) {
+#pragma unroll
+                    for (u32 q = 0; q < PPL; q++)
                         vd[q] = __dadd_rn(vd[q], as_double(y[q][u]));  // gdn_integer_to_float.c:37
                 }
             }
@@ -405,8 +409,10 @@ __device__ __forceinline__ void dim_value_k(const HDim &D, const u32 *Cj, const 
 // request and all its d dimensions; tiles of all requests form one list.  The
 // tile of doubles is staged in shared memory ([32 * PPL][d]) and stored as
 // contiguous rows.  With one request (ONE) its descriptor is a kernel
-// parameter (the constant bank, no registers held for it).
-template <u32 PPL, bool ONE>
+// parameter (the constant bank, no registers held for it).  Without MIXED
+// every dimension adds on the FP64 unit and the integer adds are not compiled
+// in (fewer registers and instructions for the common split).
+template <u32 PPL, bool ONE, bool MIXED>
 __global__ void __launch_bounds__(HT_THREADS, 3) halton_gen_kernel(HPlanDev P, HReq R1)
 {
     extern __shared__ __align__(16) unsigned char sm[];
@@ -435,7 +441,7 @@ __global__ void __launch_bounds__(HT_THREADS, 3) halton_gen_kernel(HPlanDev P, H
             const u32 j = order[oi];
             const HDim D = dims[j];
             u64 vb[PPL];
-            if (D.add == ADD_INT)
+            if (MIXED && D.add == ADD_INT)
                 dim_value_k<ADD_INT, PPL>(D, Cl + D.c_off, Yl + D.y_off, Tl + D.s_off, base, itrue, active, lane, vb);
             else
                 dim_value_k<ADD_FP64, PPL>(D, Cl + D.c_off, Yl + D.y_off, Tl + D.s_off, base, itrue, active, lane, vb);
@@ -459,9 +465,11 @@ u64 ceil_digits(u64 n_last, u64 b)
 
 // The share of the terms (by count) whose adds go to the FP64 unit; the
 // other dimensions add in integer arithmetic.  Dimensions are taken in order
-// of decreasing tmax for the FP64 side.
-void assign_adds(std::vector<HDim> &hd, double share)
+// of decreasing tmax for the FP64 side.  Returns whether any dimension adds
+// in integer arithmetic.
+bool assign_adds(std::vector<HDim> &hd, double share)
 {
+    bool mixed = false;
     u64 total = 0;
     for (const HDim &h : hd) total += h.tmax;
     std::vector<u32> idx(hd.size());
@@ -472,7 +480,9 @@ void assign_adds(std::vector<HDim> &hd, double share)
         const bool fp = (double)acc + hd[j].tmax / 2.0 < share * (double)total;
         hd[j].add = fp ? ADD_FP64 : ADD_INT;
         if (fp) acc += hd[j].tmax;
+        mixed = mixed || !fp;
     }
+    return mixed;
 }
 
 }  // namespace
@@ -486,6 +496,7 @@ struct qmc_halton_plan {
     void *d_order = nullptr, *d_wstart = nullptr, *d_prep = nullptr;
     size_t smem = 0;
     u32 ppl = 1;
+    bool mixed = false;  // some dimensions add in integer arithmetic
     bool prepared = false;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
@@ -520,27 +531,33 @@ int run_launch(qmc_halton_plan *p, cudaStream_t st)
 {
     const unsigned grid = qmcgb::grid_for(p->P.ntiles, 1, (unsigned)qmcgb::sm_count() * 8);
     const HReq &R1 = p->hreq[0];
-    const bool one = p->hreq.size() == 1;
+    const bool one = p->hreq.size() == 1, mixed = p->mixed;
+#define HT_LAUNCH(PPL_, ONE_, MIXED_) halton_gen_kernel<PPL_, ONE_, MIXED_><<<grid, HT_THREADS, p->smem, st>>>(p->P, R1)
     if (p->ppl == 2) {
-        if (one)
-            halton_gen_kernel<2, true><<<grid, HT_THREADS, p->smem, st>>>(p->P, R1);
-        else
-            halton_gen_kernel<2, false><<<grid, HT_THREADS, p->smem, st>>>(p->P, R1);
+        if (one) {
+            if (mixed) HT_LAUNCH(2, true, true); else HT_LAUNCH(2, true, false);
+        } else {
+            if (mixed) HT_LAUNCH(2, false, true); else HT_LAUNCH(2, false, false);
+        }
     } else {
-        if (one)
-            halton_gen_kernel<1, true><<<grid, HT_THREADS, p->smem, st>>>(p->P, R1);
-        else
-            halton_gen_kernel<1, false><<<grid, HT_THREADS, p->smem, st>>>(p->P, R1);
+        if (one) {
+            if (mixed) HT_LAUNCH(1, true, true); else HT_LAUNCH(1, true, false);
+        } else {
+            if (mixed) HT_LAUNCH(1, false, true); else HT_LAUNCH(1, false, false);
+        }
     }
+#undef HT_LAUNCH
     return qmcgb::launch_status("halton_gen_kernel");
 }
 
 template <u32 PPL>
 int gen_smem_attr(size_t smem)
 {
-    if (int rc = qmcgb::raise_smem_limit((const void *)halton_gen_kernel<PPL, true>, smem, "halton_gen_kernel smem"))
-        return rc;
-    return qmcgb::raise_smem_limit((const void *)halton_gen_kernel<PPL, false>, smem, "halton_gen_kernel smem");
+    const void *fs[] = {(const void *)halton_gen_kernel<PPL, true, true>, (const void *)halton_gen_kernel<PPL, false, true>,
+                        (const void *)halton_gen_kernel<PPL, true, false>, (const void *)halton_gen_kernel<PPL, false, false>};
+    for (const void *f : fs)
+        if (int rc = qmcgb::raise_smem_limit(f, smem, "halton_gen_kernel smem")) return rc;
+    return QMC_OK;
 }
 
 }  // namespace
@@ -674,7 +691,7 @@ int qmc_halton_batch_create(const qmc_halton_request *reqs, int nreq, qmc_halton
         wstart.push_back(pos);
         p->hreq.push_back(R);
     }
-    assign_adds(p->hd, 1.0);
+    p->mixed = assign_adds(p->hd, 1.0);
     const u64 ndims = p->hd.size();
     p->P.nreq = (u64)nreq;
     p->P.total_c = c_base;
@@ -773,10 +790,11 @@ int qmc_halton_plan_graph_launch(qmc_halton_plan *p, qmc_stream_t s)
 int qmc_halton_plan_set_fp64_share(qmc_halton_plan *p, double share)
 {
     QMC_REQUIRE(p && share >= 0.0 && share <= 1.0, "null plan or share outside [0, 1]");
-    assign_adds(p->hd, share);
-    // the previous run may still read the descriptors
+    p->mixed = assign_adds(p->hd, share);
+    // the previous run may still read the descriptors; a captured graph holds the kernel variant
     if (int rc = qmcgb::cuda_status(cudaDeviceSynchronize(), "synchronise before rewriting the descriptors"))
         return rc;
+    drop_graph(p);
     return qmcgb::cuda_status(cudaMemcpy(p->d_dims, p->hd.data(), p->hd.size() * sizeof(HDim), cudaMemcpyHostToDevice),
                               "copy");
 }

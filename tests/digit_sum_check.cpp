@@ -62,6 +62,8 @@ int main(int argc, char **argv)
         if (c % 79 == 0) vb = 0;
         if (c % 5 == 0) yb = vb - ((u64)(1 + next() % 60) << 52);  // same significand, lower binade
         if (c % 3 == 0) yb &= ~((1ull << (next() % 53)) - 1);         // trailing zeros: exact halves
+        if (c % 7 == 0) yb = ((u64)(1023 - 1 - next() % 60) << 52) | (next() & dsum::FRAC);  // y above v too
+        if (c % 11 == 0) yb = ((vb >> 52) << 52) | (next() & dsum::FRAC);                 // same binade
         const u64 got = dsum::pack(emu_add(dsum::unpack(vb), yb, &fast)), want = hw_add(vb, yb);
         if (got != want) {
             printf("add mismatch v=%016llx y=%016llx got=%016llx want=%016llx\n", vb, yb, got, want);
