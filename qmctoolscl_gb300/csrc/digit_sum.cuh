@@ -69,4 +69,25 @@ DS_HD bool add_fast(Sum &v, u64 y)
     return true;
 }
 
+// Bits of RN(r * (double)m) for r the bits of a positive normal double and
+// 0 < m < 2^11, in integer arithmetic: the 64-bit product of the significand
+// and m, normalised, rounded to 53 bits (nearest, ties to even).  The
+// result stays normal and finite for r in [2^-1000, 2^1000).
+DS_HD u64 mul_small(u64 r, u32 m)
+{
+    const u64 P = ((r & FRAC) | HIDDEN) * (u64)m;  // below 2^64, at least 2^52
+    u32 lz;
+#ifdef __CUDA_ARCH__
+    lz = (u32)__clzll((long long)P);
+#else
+    lz = (u32)__builtin_clzll(P);
+#endif
+    const u64 Pn = P << lz;                   // leading one at bit 63
+    const u64 mant = Pn >> 11, rem = Pn & 0x7FFull;
+    const u64 up = (u64)((rem > 0x400ull) | ((rem == 0x400ull) & (mant & 1ull)));
+    // value = mant * 2^(E - 1075) with E = Er + 11 - lz; the hidden bit of mant adds one to the
+    // exponent field, and a round-up to 2^53 carries into it
+    return ((r >> 52) + 10u - lz) * HIDDEN + mant + up;
+}
+
 }  // namespace dsum

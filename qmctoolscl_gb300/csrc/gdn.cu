@@ -30,6 +30,7 @@
 // S is r*d*tmax_new*tmax, perms r*d*tmax_new*bmax.  Per-point kernels walk
 // (row, dimension, digit) as one flat run so stores are contiguous.
 #include "common.cuh"
+#include "digit_sum.cuh"
 
 namespace {
 
@@ -600,23 +601,16 @@ __device__ __noinline__ u64 digit_step_hw(u64 v, double rc, u64 dg)
     return as_bits(__dadd_rn(as_double(v), __dmul_rn(rc, __ull2double_rn(dg))));
 }
 
-// (double)dg for dg < 2^53 (exact), built in integer arithmetic
-__device__ __forceinline__ double small_u64_to_double(u64 dg)
-{
-    if (dg == 0) return 0.0;
-    const u32 lz = (u32)__clzll((long long)dg);
-    return as_double(((u64)(1086 - lz) << 52) + ((dg << lz) >> 11) - (1ull << 52));
-}
-
-// one term of the sum: v = RN(v + RN(recip * digit)), the FP64 operations of
-// gdn_integer_to_float.c:36-37 (the integer emulation of dmul_small_bits /
-// dadd_pos_bits costs about a hundred ALU instructions per digit, and in this
-// kernel the ALU pipe, not the FP64 pipe, is the bottleneck)
+// one term of the sum: v = RN(v + RN(recip * digit)), gdn_integer_to_float.c:36-37; the
+// product in integer arithmetic for digits below 2^11 (dsum::mul_small, exact RN) and the
+// add on the FP64 unit, whose throughput bounds this kernel
 __device__ __forceinline__ u64 digit_term(u64 v, double rc, u64 dg)
 {
     if (dg == 0) return v;  // adds +0: v unchanged
-    if (dg >> 53) return digit_step_hw(v, rc, dg);
-    return as_bits(__dadd_rn(as_double(v), __dmul_rn(rc, small_u64_to_double(dg))));
+    const u64 rb = as_bits(rc);
+    if (dg < 2048 && rb >= (24ull << 52))  // recip >= 2^-999: the product stays normal
+        return as_bits(__dadd_rn(as_double(v), as_double(dsum::mul_small(rb, (u32)dg))));
+    return digit_step_hw(v, rc, dg);
 }
 
 // v = sum_t recip_t * digit_t with the reference's rounding sequence; the
@@ -651,21 +645,106 @@ __device__ __forceinline__ double digits_to_double(const double *rc, const u64 *
     return as_double(v);
 }
 
-constexpr u32 I2F_DIMS = 32;   // dimensions per CTA
-constexpr u32 I2F_TMAX = 64;   // recip table depth held in shared memory
+// RN(recip * (double)dg) for the digits beyond the term table, out of line
+__device__ __noinline__ double term_hw(double rc, u64 dg) { return __dmul_rn(rc, __ull2double_rn(dg)); }
 
+// term t of a digit: the table entry RN(recip_t * dg) for dg < b (T[t * b + dg]), else the
+// product itself (recip_t = T[t * b + 1])
+__device__ __forceinline__ double tbl_term(const double *T, u32 b, u64 t, u64 dg)
+{
+    const u32 row = (u32)t * b;
+    return dg < b ? T[row + (u32)dg] : term_hw(T[row + 1], dg);
+}
+
+// digits_to_double with the products from the term table: one FP64 operation per digit
+__device__ __forceinline__ double digits_to_double_tbl(const double *T, u32 b, const u64 *dig, u64 tmax)
+{
+    double v = 0.0;
+    if ((tmax & 1) == 0 && ((uintptr_t)dig & 15) == 0) {
+        const ulonglong2 *d2 = (const ulonglong2 *)dig;
+        for (u64 t0 = 0; t0 < tmax; t0 += 8) {
+            ulonglong2 q[4];
+#pragma unroll
+            for (u32 u = 0; u < 4; u++) q[u] = t0 + 2 * u < tmax ? d2[t0 / 2 + u] : make_ulonglong2(0, 0);
+#pragma unroll
+            for (u32 u = 0; u < 4; u++) {
+                if (t0 + 2 * u >= tmax) break;
+                v = __dadd_rn(v, tbl_term(T, b, t0 + 2 * u, q[u].x));  // gdn_integer_to_float.c:37
+                v = __dadd_rn(v, tbl_term(T, b, t0 + 2 * u + 1, q[u].y));
+            }
+        }
+        return v;
+    }
+    for (u64 t0 = 0; t0 < tmax; t0 += 8) {
+        u64 dg8[8];
+#pragma unroll
+        for (u32 u = 0; u < 8; u++) dg8[u] = t0 + u < tmax ? dig[t0 + u] : 0;
+#pragma unroll
+        for (u32 u = 0; u < 8; u++)
+            if (t0 + u < tmax) v = __dadd_rn(v, tbl_term(T, b, t0 + u, dg8[u]));
+    }
+    return v;
+}
+
+constexpr u32 I2F_DIMS = 32;            // dimensions per CTA
+constexpr u32 I2F_TMAX = 64;            // recip table depth held in shared memory
+constexpr u32 I2F_SMEM_WORDS = 2048;    // dynamic shared memory (16 KB, 8 CTAs per SM): term or recip table
+enum I2fMode { I2F_LOOP = 0, I2F_RECIP = 1, I2F_TERMS = 2 };
+
+// Each CTA converts a run of points for up to 32 dimensions.  When the CTA's
+// term tables -- RN(recip_t * dg) for t < tmax, dg < b, per dimension -- fit
+// in 16 KB, the products come from shared memory and only the adds run on the
+// FP64 unit; else a table of recip_t (tmax <= 64), else the reference's loop.
 __global__ void __launch_bounds__(THREADS) gdn_to_float_kernel(u64 r, u64 n, u64 d, u64 r_b, u64 tmax,
                                                                const u64 *bases, const u64 *xdig, double *x,
                                                                u64 rows_per_cta, u32 dim_tiles, u64 l_off)
 {
-    __shared__ double rc[I2F_DIMS][I2F_TMAX];
+    extern __shared__ __align__(16) double i2f_sm[];
+    __shared__ u32 toff[I2F_DIMS + 1], tb[I2F_DIMS], mode;
     const u64 l = l_off + (u64)blockIdx.y / dim_tiles;
     if (l >= r) return;
     const u64 j0 = (u64)(blockIdx.y % dim_tiles) * I2F_DIMS;
     const u32 nd = (u32)min((u64)I2F_DIMS, d - j0);
-    const bool table = tmax <= I2F_TMAX;
-    if (table)
-        for (u32 c = threadIdx.x; c < nd; c += blockDim.x) fill_recips(rc[c], bases[(l % r_b) * d + j0 + c], tmax);
+    const u64 *bl = bases + (l % r_b) * d + j0;
+    if (threadIdx.x == 0) {
+        u64 acc = 0;
+        bool fits = tmax <= I2F_TMAX;
+        for (u32 c = 0; c < nd && fits; c++) {
+            const u64 b = bl[c];
+            fits = b >= 2 && b <= I2F_SMEM_WORDS;
+            toff[c] = (u32)acc;
+            tb[c] = (u32)b;
+            acc += tmax * b;
+            fits = fits && acc <= I2F_SMEM_WORDS;
+        }
+        toff[nd] = (u32)acc;
+        mode = fits ? I2F_TERMS : tmax <= I2F_TMAX ? I2F_RECIP : I2F_LOOP;
+    }
+    __syncthreads();
+    if (mode == I2F_TERMS) {
+        // recip_t into column 1 of each row, then every entry from its row's recip
+        for (u32 c = threadIdx.x; c < nd; c += blockDim.x) {
+            const u32 b = tb[c];
+            const double bd = __ull2double_rn(b);
+            double rcp = __ddiv_rn(1.0, bd);
+            for (u32 t = 0; t < (u32)tmax; t++) {
+                i2f_sm[toff[c] + t * b] = 0.0;
+                i2f_sm[toff[c] + t * b + 1] = rcp;
+                rcp = __ddiv_rn(rcp, bd);
+            }
+        }
+        __syncthreads();
+        for (u32 c = 0; c < nd; c++) {
+            const u32 b = tb[c], cnt = (u32)tmax * b;
+            double *T = i2f_sm + toff[c];
+            for (u32 k = threadIdx.x; k < cnt; k += blockDim.x) {
+                const u32 t = k / b, dg = k - t * b;
+                if (dg >= 2) T[k] = __dmul_rn(T[t * b + 1], (double)dg);
+            }
+        }
+    } else if (mode == I2F_RECIP) {
+        for (u32 c = threadIdx.x; c < nd; c += blockDim.x) fill_recips(i2f_sm + c * I2F_TMAX, bl[c], tmax);
+    }
     __syncthreads();
     const u64 row0 = (u64)blockIdx.x * rows_per_cta;
     if (row0 >= n) return;
@@ -678,10 +757,12 @@ __global__ void __launch_bounds__(THREADS) gdn_to_float_kernel(u64 r, u64 n, u64
         const u64 i = row0 + rr, j = j0 + c;
         const u64 *dg = xdig + l * n * d * tmax + i * d * tmax + j * tmax;
         double v;
-        if (table) {
-            v = digits_to_double(rc[c], dg, tmax);
+        if (mode == I2F_TERMS) {
+            v = digits_to_double_tbl(i2f_sm + toff[c], tb[c], dg, tmax);
+        } else if (mode == I2F_RECIP) {
+            v = digits_to_double(i2f_sm + c * I2F_TMAX, dg, tmax);
         } else {  // deep digit expansions: the reference's loop as written
-            const double bd = __ull2double_rn(bases[(l % r_b) * d + j]);
+            const double bd = __ull2double_rn(bl[c]);
             double rcp = __ddiv_rn(1.0, bd);
             v = 0.0;
             for (u64 t = 0; t < tmax; t++) {
@@ -927,7 +1008,8 @@ int qmc_gdn_integer_to_float(uint64_t r, uint64_t n, uint64_t d, uint64_t r_b, u
     u64 splits;
     const PointGrid pg = point_grid(r, n, d, 1, I2F_DIMS, &splits);
     return launch_points(r, pg.dim_tiles, [&](u64 l0, unsigned cnt) {
-        gdn_to_float_kernel<<<dim3((unsigned)splits, cnt, 1), THREADS, 0, QMC_STREAM(s)>>>(
+        gdn_to_float_kernel<<<dim3((unsigned)splits, cnt, 1), THREADS, I2F_SMEM_WORDS * sizeof(double),
+                              QMC_STREAM(s)>>>(
             r, n, d, r_b, tmax, (const u64 *)bases, (const u64 *)xdig, x, pg.rows_per_cta, pg.dim_tiles, l0);
     }, "gdn_integer_to_float");
 }

@@ -70,6 +70,17 @@ int main(int argc, char **argv)
             return 1;
         }
     }
+    // products RN(recip * m) for m < 2^11 against the host's multiply
+    for (long c = 0; c < cases; c++) {
+        u64 rb = ((u64)(1023 - 700 + next() % 1000) << 52) | (next() & dsum::FRAC);
+        if (c % 3 == 0) rb &= ~((1ull << (next() % 53)) - 1);  // trailing zeros: exact and tie products
+        const u32 m = 1 + (u32)(next() % 2047);
+        volatile double p = dbl(rb) * (double)m;
+        if (dsum::mul_small(rb, m) != bits(p)) {
+            printf("mul mismatch r=%016llx m=%u got=%016llx want=%016llx\n", rb, m, dsum::mul_small(rb, m), bits(p));
+            return 1;
+        }
+    }
     // whole chains: base b, recip_0 = 1/b, recip_{t+1} = recip_t/b, terms RN(recip_t * digit)
     for (long c = 0; c < chains; c++) {
         const u32 b = 2 + (u32)(next() % (c % 3 == 0 ? 30 : 2046));

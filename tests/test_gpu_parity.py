@@ -241,6 +241,30 @@ def test_gdn_integer_to_float_depths(tmax):
     assert same_bits(gpu, orc)
 
 
+@pytest.mark.parametrize("bases,tmax,r_b", [([2], 64, 1), ([3], 41, 1), ([541], 3, 1), ([251], 8, 1),
+                                           ([2, 3, 5, 7], 64, 1), ([2, 3, 5, 7], 13, 2), ([2047], 1, 1),
+                                           ([2, 1021], 1, 1), ([2, 1021], 2, 1), ([2, 1023], 2, 1)])
+def test_gdn_integer_to_float_term_table(bases, tmax, r_b):
+    """Shapes whose per-CTA product tables RN(recip_t * digit) fit in shared memory (the
+    one-FP64-add-per-digit path), odd and even digit counts, bases per randomisation, digits
+    at and beyond the base (products outside the table)."""
+    rng = np.random.Generator(np.random.SFC64(len(bases) * 100 + tmax + r_b))
+    r, n, d = 3, 257, len(bases)
+    B = np.array([bases] * r_b, U)
+    if r_b > 1:
+        B[1:] = B[1:] + 2  # another base per randomisation (2 -> 4, 3 -> 5, ...)
+    xdig = np.empty((r, n, d, tmax), U)
+    for l in range(r):
+        for j in range(d):
+            xdig[l, :, j] = rng.integers(0, B[l % r_b, j], (n, tmax), dtype=U)
+    xdig[0, 0, 0, 0] = B[0, 0]             # the base itself: just outside the table
+    xdig[1, 5, d - 1, tmax - 1] = U(1 << 40)  # far outside
+    xdig[2, 7, 0, :] = B[0 if r_b == 1 else 2 % r_b, 0] - 1  # every digit maximal
+    gpu, orc = both("gdn_integer_to_float", [U(r), U(n), U(d), U(r_b), U(tmax), B, xdig,
+                                             poison((r, n, d), np.float64)], ["x"])["x"]
+    assert same_bits(gpu, orc)
+
+
 def test_gdn_same_base_and_interlace_random():
     rng = np.random.Generator(np.random.SFC64(3))
     r, n, d, mmax, tmax, b = 2, 500, 6, 6, 7, 5
