@@ -209,9 +209,16 @@ __device__ __forceinline__ float step_matrix(u32 kk, u32 n)
 // when bits > 12, a remainder below 2 pi / 4096 whose sine and cosine are
 // two-term series (the next terms are below 2^-40).
 // twiddle_turn takes the angle J / 2^32 of a turn directly (J = t << (32 - bits)).
+//
+// The table is stored swizzled: entry r at tab_slot(r), its low four bits
+// XORed with bits 4-7 and 8-11.  A warp's lookups are often r = s * c for a
+// power-of-two stride s (a step's groups differ in c); with 8-byte entries
+// unswizzled, strides of 16 or more put them all in one bank pair.
+__device__ __forceinline__ u32 tab_slot(u32 r) { return r ^ (((r >> 4) ^ (r >> 8)) & 15u); }
+
 __device__ __forceinline__ void twiddle_turn(const float2 *tab, u32 J, u32 bits, float sign, float &wr, float &wi)
 {
-    const float2 e = tab[(J >> 20) & 1023u];  // (cos, -sin) of 2 pi r / 4096
+    const float2 e = tab[tab_slot((J >> 20) & 1023u)];  // (cos, -sin) of 2 pi r / 4096
     float c = e.x, sn = e.y;
     const u32 quarter = J >> 30;              // times (-i)^quarter
     if (quarter & 1u) {
@@ -266,7 +273,7 @@ __global__ void __launch_bounds__(FT_THREADS, 3) tc_pass_kernel(TcPassArgs a, un
     for (u32 r = threadIdx.x; r < 1024; r += FT_THREADS) {
         float sn, c;
         sincospif((float)r / 2048.0f, &sn, &c);
-        tab[r] = make_float2(c, -sn);
+        tab[tab_slot(r)] = make_float2(c, -sn);
     }
     if (threadIdx.x == 0) tc::mbar_init(&bar, 1);
     tc::fence_before_sync();
