@@ -47,8 +47,8 @@ PROFILE_LOG2N = 16  # --small: the same kernel on 512 MiB of output, for ncu cap
 SEED = 2
 FALLBACK_HBM_GBS = 6800.0
 # DRAM bytes / algorithmic bytes of the two captured tensor-core FFT passes (n = 2^20, 24
-# vectors, 48 B per sample): (402.7 + 154.0 + 201.4 + 341.7) MB / 1208.0 MB
-TC_FFT_TRAFFIC_RATIO = 0.9105
+# vectors, 48 B per sample): (402.7 + 153.9 + 201.6 + 342.1) MB / 1208.0 MB
+TC_FFT_TRAFFIC_RATIO = 0.9109
 
 
 def workload_inputs(seed=SEED):
@@ -969,7 +969,7 @@ def run_halton(args):
     alg = 8.0 * r * n * d
     return {"metric": METRIC, "value": pts / (ms_fused / 1e3), "unit": "points/s", "n_gpus": 1,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_fused, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "u32 digits, f64 (integer-emulated) output",
+            "scaling": "weak", "vs_baseline": None, "dtype": "u32 digits, f64 adds (split FP64 unit / integer by the tuned share)",
             "data": "synthetic (np.random.SFC64(4)): reference generators per dimension",
             "config": {"workload": "randomised Halton, bases = first 100 primes, d=100, n=2^18, r=32, "
                                    "tmax_j=ceil(64/log2 b), LMS + permutation + digital shift + float "
@@ -977,8 +977,8 @@ def run_halton(args):
                        "l2": "6.7 GB output per step >> 129 MB L2, no flush needed"},
             "roofline": dict(roofline(alg, ms_gen), kernel="halton_gen_kernel",
                              traffic=profiled_traffic("halton_gen_kernel_r32_n2p18_d100.md"),
-                             note="generation kernel alone; bound by instruction issue (integer + FP64 adds), "
-                                  "not HBM"),
+                             note="generation kernel alone; bound by the FP64 unit's digit adds (one per digit, "
+                                  "the FP64 pipe about 70 % busy in the ncu capture) and integer issue, not HBM"),
             "generate_only_ms": ms_gen,
             "uneven_batch": {"requests": 64, "points": upoints, "coords": ucoords, "graph_ms": ms_u_graph,
                              "per_request_plans_ms": ms_u_single, "speedup": ms_u_single / ms_u_graph,

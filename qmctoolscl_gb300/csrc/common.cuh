@@ -106,55 +106,6 @@ __device__ __forceinline__ u64 add_mod1_fix64(u64 X, u64 S)
     return T;
 }
 
-// RN(a + b) for finite non-negative normal-or-zero doubles given as bits,
-// with a + b < 2^1023.  Exact emulation of the IEEE add in that domain.
-__device__ __forceinline__ u64 dadd_pos_bits(u64 a, u64 b)
-{
-    if (a < b) { const u64 t = a; a = b; b = t; }  // a >= b as values
-    if (b == 0) return a;
-    const u32 ea = (u32)(a >> 52), eb = (u32)(b >> 52);
-    // mantissas with the leading one, placed at bit 62 (one headroom bit,
-    // ten guard bits below the 53-bit field)
-    const u64 ma = ((a & 0xFFFFFFFFFFFFFull) | (1ull << 52)) << 10;
-    u64 mb = ((b & 0xFFFFFFFFFFFFFull) | (1ull << 52)) << 10;
-    const u32 dlt = ea - eb;
-    if (dlt) {
-        if (dlt >= 64) {
-            mb = 1;  // only a sticky bit survives
-        } else {
-            const u64 lost = mb & ((1ull << dlt) - 1);
-            mb = (mb >> dlt) | (lost != 0);
-        }
-    }
-    u64 s = ma + mb;
-    u32 e = ea;
-    if (s >> 63) {  // carry: renormalise by one, keeping the sticky bit
-        s = (s >> 1) | (s & 1);
-        e += 1;
-    }
-    // s has its leading one at bit 62; keep bits 62..10, round on 9..0
-    u64 m = s >> 10;
-    const u64 rem = s & 0x3FFull;
-    m += (rem > 0x200ull) | ((rem == 0x200ull) & (m & 1ull));
-    return ((u64)(e - 1) << 52) + m;  // m may carry to 2^53: exponent bumps
-}
-
-// RN(r * dig) for a positive normal double r (bits) and an integer
-// 1 <= dig < 2^11: the 53x11-bit product fits in 64 bits.
-__device__ __forceinline__ u64 dmul_small_bits(u64 r, u32 dig)
-{
-    const u64 mr = (r & 0xFFFFFFFFFFFFFull) | (1ull << 52);
-    const u64 p = mr * (u64)dig;  // < 2^64
-    const int lz = __clzll((long long)p);
-    const u64 N = p << lz;
-    u64 m = N >> 11;
-    const u64 rem = N & 0x7FFull;
-    m += (rem > 0x400ull) | ((rem == 0x400ull) & (m & 1ull));
-    // value = p * 2^(er-52) with the leading one of p at bit 63-lz
-    const u32 er = (u32)(r >> 52);
-    return ((u64)(er + 10 - lz) << 52) + m;
-}
-
 // ---------------------------------------------------- small integer math --
 
 // Lemire-Kaser-Kurz direct remainder ("Faster remainder by direct

@@ -19,12 +19,14 @@
 //
 // Digits to float.  The reference sums recip_t*digit_t with recip_0 = 1/b
 // and recip_{t+1} = recip_t/b, every operation rounded separately.  The
-// recip_t depend only on (b, t): each CTA computes them once per dimension
-// into shared memory.  The per-digit multiply and add are the FP64
-// operations themselves (__dmul_rn, __dadd_rn): their integer emulation
-// (dmul_small_bits, dadd_pos_bits) measured about a hundred ALU instructions
-// per digit with the ALU pipe 91% busy, while two FP64 operations per digit
-// leave this kernel bound by HBM reads.
+// recip_t depend only on (b, t): each CTA computes them once per dimension.
+// The adds run on the FP64 unit (__dadd_rn), one per digit, and bound the
+// kernel; the products RN(recip_t * digit) come from a shared-memory table
+// of all (t, digit < b) when the CTA's tables fit in 16 KB, else from an
+// integer 53x11-bit product with its rounding (dsum::mul_small) for digits
+// below 2^11, else from __dmul_rn out of line.  (Emulating the adds in
+// integer arithmetic as well measured about a hundred ALU instructions per
+// digit with the ALU pipe 91% busy.)
 //
 // Layout in HBM: xdig is r*n*d*tmax (digit t fastest), C is r*d*mmax*tmax,
 // S is r*d*tmax_new*tmax, perms r*d*tmax_new*bmax.  Per-point kernels walk
