@@ -260,16 +260,22 @@ int launch_gen(GenArgs a, cudaStream_t s, const char *what)
     const u64 units = a.r * a.col_tiles;
     // enough CTAs to fill the GPU several times; each CTA covers a row run of
     // at least four table lengths so building the table stays a small cost
-    const u64 want = (u64)qmcgb::sm_count() * 8;
-    u64 splits = (want + units - 1) / units;
+    const size_t smem = net::table_words(a.K, a.mmax, ncols) * sizeof(u64);
+    auto kern = dnb2_gen_kernel<GRAY>;
+    if (int rc = qmcgb::raise_smem_limit((const void *)kern, smem, what)) return rc;
+    // four waves of resident CTAs (the table's shared memory limits how many fit per SM): short
+    // row runs balance the SMs; one wave of long runs, or 8 CTAs per SM against 6 resident (a
+    // third of a wave left over), measured slower
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, GEN_THREADS, smem) != cudaSuccess || per_sm < 1)
+        per_sm = 1;
+    const u64 want = (u64)qmcgb::sm_count() * (u64)per_sm * 4;
+    u64 splits = want >= units ? want / units : 1;
     const u64 min_rows = 4ull << a.K;
     const u64 max_splits = (a.n + min_rows - 1) / min_rows;
     if (splits > max_splits) splits = max_splits;
     if (splits < 1) splits = 1;
     a.rows_per_cta = (a.n + splits - 1) / splits;
-    const size_t smem = net::table_words(a.K, a.mmax, ncols) * sizeof(u64);
-    auto kern = dnb2_gen_kernel<GRAY>;
-    if (int rc = qmcgb::raise_smem_limit((const void *)kern, smem, what)) return rc;
     // blockIdx.y enumerates (randomisation, column tile), at most 65535 per launch
     const u64 l_per_launch = 65535 / a.col_tiles;
     for (u64 l0 = 0; l0 < a.r; l0 += l_per_launch) {

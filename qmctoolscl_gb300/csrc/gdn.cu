@@ -842,12 +842,14 @@ __global__ void gdn_undo_interlace_kernel(u64 r, u64 d, u64 mmax, u64 d_alpha, u
 
 unsigned flat_grid(u64 total) { return qmcgb::grid_for(total, 256, (unsigned)qmcgb::sm_count() * 32); }
 
-PointGrid point_grid(u64 r, u64 n, u64 d, u64 per_point, u32 dim_tile, u64 *splits_out)
+// ctas_per_sm: CTAs asked for per SM (several waves of short row runs balance the SMs best for
+// the streaming kernels: measured 32 for permutation and shift, 16 for integer-to-float)
+PointGrid point_grid(u64 r, u64 n, u64 d, u64 per_point, u32 dim_tile, u64 *splits_out, u32 ctas_per_sm = 8)
 {
     PointGrid pg;
     pg.dim_tiles = (u32)((d + dim_tile - 1) / dim_tile);
     const u64 units = r * pg.dim_tiles;
-    const u64 want = (u64)qmcgb::sm_count() * 8;
+    const u64 want = (u64)qmcgb::sm_count() * ctas_per_sm;
     u64 splits = (want + units - 1) / units;
     // at least ~2 elements per thread in a CTA
     const u64 per_row = (d < dim_tile ? d : dim_tile) * (per_point ? per_point : 1);
@@ -974,7 +976,7 @@ int qmc_gdn_digital_permutation(uint64_t r, uint64_t n, uint64_t d, uint64_t r_x
     unsigned *err = qmcgb::device_error_ptr();
     QMC_REQUIRE(err, "device error word unavailable");
     u64 splits;
-    const PointGrid pg = point_grid(r, n, d, tmax_new, DIM_TILE, &splits);
+    const PointGrid pg = point_grid(r, n, d, tmax_new, DIM_TILE, &splits, 32);
     const u32 lin = linear_run(pg, d, tmax, tmax_new, xdig, xdig_new);
     return launch_points(r, pg.dim_tiles, [&](u64 l0, unsigned cnt) {
         gdn_perm_kernel<<<dim3((unsigned)splits, cnt, 1), THREADS, 0, QMC_STREAM(s)>>>(
@@ -993,7 +995,7 @@ int qmc_gdn_digital_shift(uint64_t r, uint64_t n, uint64_t d, uint64_t r_x, uint
     unsigned *err = qmcgb::device_error_ptr();
     QMC_REQUIRE(err, "device error word unavailable");
     u64 splits;
-    const PointGrid pg = point_grid(r, n, d, tmax_new, DIM_TILE, &splits);
+    const PointGrid pg = point_grid(r, n, d, tmax_new, DIM_TILE, &splits, 32);
     const u32 lin = linear_run(pg, d, tmax, tmax_new, xdig, xdig_new);
     return launch_points(r, pg.dim_tiles, [&](u64 l0, unsigned cnt) {
         gdn_shift_kernel<<<dim3((unsigned)splits, cnt, 1), THREADS, 0, QMC_STREAM(s)>>>(
@@ -1008,7 +1010,7 @@ int qmc_gdn_integer_to_float(uint64_t r, uint64_t n, uint64_t d, uint64_t r_b, u
     if (r == 0 || n == 0 || d == 0) return QMC_OK;
     QMC_REQUIRE(r_b > 0 && bases && x && (tmax == 0 || xdig), "bad r_b or null array pointer");
     u64 splits;
-    const PointGrid pg = point_grid(r, n, d, 1, I2F_DIMS, &splits);
+    const PointGrid pg = point_grid(r, n, d, 1, I2F_DIMS, &splits, 16);
     return launch_points(r, pg.dim_tiles, [&](u64 l0, unsigned cnt) {
         gdn_to_float_kernel<<<dim3((unsigned)splits, cnt, 1), THREADS, I2F_SMEM_WORDS * sizeof(double),
                               QMC_STREAM(s)>>>(
