@@ -359,7 +359,20 @@ __global__ void __launch_bounds__(THREADS) gdn_gen_tiled_kernel(u64 r, u64 n, u6
     }
 }
 
-__global__ void __launch_bounds__(THREADS) gdn_shift_kernel(u64 r, u64 n, u64 d, u64 r_x, u64 r_b, u64 tmax,
+// (digit + shift) mod b as gdn_digital_shift.c:38 computes it (the sum wraps in 64 bits); a base
+// of 0 is reported, never divided by
+__device__ __forceinline__ u64 shift_mod(const DimInfo &di, u64 sum, unsigned *err)
+{
+    if (di.b == 0) {
+        atomicOr(err, 2u);
+        return 0;
+    }
+    return (di.small && sum < (1ull << 32)) ? (u64)fd_mod(di.fd, (u32)sum) : sum % di.b;
+}
+
+// at most 64 registers (4 CTAs per SM): its general path alone would take 72 and leave 3 CTAs, too
+// few loads in flight for the streaming paths (0.64-0.82 of the copy peak; 0.74-0.91 capped)
+__global__ void __launch_bounds__(THREADS, 4) gdn_shift_kernel(u64 r, u64 n, u64 d, u64 r_x, u64 r_b, u64 tmax,
                                                             u64 tmax_new, const u64 *bases, const u64 *shifts,
                                                             const u64 *xdig, u64 *xdig_new, PointGrid pg,
                                                             u64 l_off, u32 lin, unsigned *err)
@@ -398,20 +411,9 @@ __global__ void __launch_bounds__(THREADS) gdn_shift_kernel(u64 r, u64 n, u64 d,
                 const u32 q = q0 + u * THREADS;
                 if (q >= npair) continue;
                 const u32 sidx = 2 * q - div32(dv_row, 2 * q) * (u32)per_row;  // even, sidx + 1 < per_row
-                u64 v[2];
-#pragma unroll
-                for (u32 h = 0; h < 2; h++) {
-                    const u32 c = div32(dv_t, sidx + h);
-                    const u64 sum = (h ? xv[u].y : xv[u].x) + shl[sidx + h];  // wraps as in C
-                    const DimInfo &di = dims[c];
-                    if (di.b == 0) {
-                        atomicOr(err, 2u);
-                        v[h] = 0;
-                    } else {
-                        v[h] = (di.small && sum < (1ull << 32)) ? (u64)fd_mod(di.fd, (u32)sum) : sum % di.b;
-                    }
-                }
-                dst[q] = make_ulonglong2(v[0], v[1]);
+                // the sums wrap as in C
+                dst[q] = make_ulonglong2(shift_mod(dims[div32(dv_t, sidx)], xv[u].x + shl[sidx], err),
+                                         shift_mod(dims[div32(dv_t, sidx + 1)], xv[u].y + shl[sidx + 1], err));
             }
         }
         return;
@@ -433,16 +435,7 @@ __global__ void __launch_bounds__(THREADS) gdn_shift_kernel(u64 r, u64 n, u64 d,
                 const u32 f = f0 + u * THREADS;
                 if (f >= (u32)total) continue;
                 const u32 sidx = f - div32(dv_row, f) * (u32)per_row;
-                const u64 sum = xv[u] + shl[sidx];  // wraps as in C
-                const DimInfo &di = dims[div32(dv_t, sidx)];
-                u64 v;
-                if (di.b == 0) {
-                    atomicOr(err, 2u);
-                    v = 0;
-                } else {
-                    v = (di.small && sum < (1ull << 32)) ? (u64)fd_mod(di.fd, (u32)sum) : sum % di.b;
-                }
-                dst[f] = v;
+                dst[f] = shift_mod(dims[div32(dv_t, sidx)], xv[u] + shl[sidx], err);  // the sum wraps as in C
             }
         }
         return;
@@ -467,14 +460,7 @@ __global__ void __launch_bounds__(THREADS) gdn_shift_kernel(u64 r, u64 n, u64 d,
             const u64 i = row0 + ps[u].rr, j = j0 + ps[u].c, t = ps[u].t;
             u64 v;
             if (t < tmax) {
-                const u64 sum = xv[u] + sh[u];  // wraps as in C
-                const DimInfo &di = dims[ps[u].c];
-                if (di.b == 0) {
-                    atomicOr(err, 2u);
-                    v = 0;
-                } else {
-                    v = (di.small && sum < (1ull << 32)) ? (u64)fd_mod(di.fd, (u32)sum) : sum % di.b;
-                }
+                v = shift_mod(dims[ps[u].c], xv[u] + sh[u], err);  // the sum wraps as in C
             } else {
                 v = sh[u];
             }
