@@ -156,6 +156,7 @@ __device__ __forceinline__ RunPos run_pos(u64 f, bool narrow, const Div32 &dv_ro
 // streaming kernels handle RUN_UNROLL elements per thread per iteration, all
 // loads issued before any is used (bytes in flight to cover HBM latency)
 constexpr u32 RUN_UNROLL = 4;
+constexpr u32 RUN_UNROLL_1 = 8;  // single-word runs: twice the loads in flight
 
 __device__ __forceinline__ void point_block(const PointGrid &pg, u64 d, u64 &l, u64 &j0, u32 &nd)
 {
@@ -423,15 +424,15 @@ __global__ void __launch_bounds__(THREADS, 4) gdn_shift_kernel(u64 r, u64 n, u64
         const u64 *src = xdig + (l % r_x) * n * d * tmax + row0 * per_row;
         u64 *dst = xdig_new + l * n * d * tmax + row0 * per_row;
         const u64 *shl = shifts + l * per_row;
-        for (u32 f0 = threadIdx.x; f0 < (u32)total; f0 += RUN_UNROLL * THREADS) {
-            u64 xv[RUN_UNROLL];
+        for (u32 f0 = threadIdx.x; f0 < (u32)total; f0 += RUN_UNROLL_1 * THREADS) {
+            u64 xv[RUN_UNROLL_1];
 #pragma unroll
-            for (u32 u = 0; u < RUN_UNROLL; u++) {
+            for (u32 u = 0; u < RUN_UNROLL_1; u++) {
                 const u32 f = f0 + u * THREADS;
                 if (f < (u32)total) xv[u] = src[f];
             }
 #pragma unroll
-            for (u32 u = 0; u < RUN_UNROLL; u++) {
+            for (u32 u = 0; u < RUN_UNROLL_1; u++) {
                 const u32 f = f0 + u * THREADS;
                 if (f >= (u32)total) continue;
                 const u32 sidx = f - div32(dv_row, f) * (u32)per_row;
@@ -520,22 +521,22 @@ __global__ void __launch_bounds__(THREADS) gdn_perm_kernel(u64 r, u64 n, u64 d, 
         const u64 *src = xdig + (l % r_x) * n * d * tmax + row0 * per_row;
         u64 *dst = xdig_new + l * n * d * tmax + row0 * per_row;
         const u64 prow0 = l * per_row * bmax;
-        for (u32 f0 = threadIdx.x; f0 < (u32)total; f0 += RUN_UNROLL * THREADS) {
-            u64 xv[RUN_UNROLL];
+        for (u32 f0 = threadIdx.x; f0 < (u32)total; f0 += RUN_UNROLL_1 * THREADS) {
+            u64 xv[RUN_UNROLL_1];
 #pragma unroll
-            for (u32 u = 0; u < RUN_UNROLL; u++) {
+            for (u32 u = 0; u < RUN_UNROLL_1; u++) {
                 const u32 f = f0 + u * THREADS;
                 if (f < (u32)total) xv[u] = src[f];
             }
 #pragma unroll
-            for (u32 u = 0; u < RUN_UNROLL; u++) {
+            for (u32 u = 0; u < RUN_UNROLL_1; u++) {
                 const u32 f = f0 + u * THREADS;
                 if (f >= (u32)total) continue;
                 const u32 sidx = f - div32(dv_row, f) * (u32)per_row;
                 xv[u] = read_flat(perms, prow0 + (u64)sidx * bmax + xv[u], p_total, err);
             }
 #pragma unroll
-            for (u32 u = 0; u < RUN_UNROLL; u++) {
+            for (u32 u = 0; u < RUN_UNROLL_1; u++) {
                 const u32 f = f0 + u * THREADS;
                 if (f < (u32)total) dst[f] = xv[u];
             }
