@@ -241,7 +241,8 @@ def test_gdn_integer_to_float_depths(tmax):
     assert same_bits(gpu, orc)
 
 
-@pytest.mark.parametrize("bases,tmax,r_b", [([2], 64, 1), ([3], 41, 1), ([541], 3, 1), ([251], 8, 1),
+@pytest.mark.parametrize("bases,tmax,r_b", [([2], 64, 1), ([2], 53, 1), ([2], 54, 1), ([2], 55, 1), ([2], 7, 1),
+                                           ([2, 3], 60, 2), ([3], 41, 1), ([541], 3, 1), ([251], 8, 1),
                                            ([2, 3, 5, 7], 64, 1), ([2, 3, 5, 7], 13, 2), ([2047], 1, 1),
                                            ([2, 1021], 1, 1), ([2, 1021], 2, 1), ([2, 1023], 2, 1)])
 def test_gdn_integer_to_float_term_table(bases, tmax, r_b):
