@@ -39,10 +39,13 @@
 // the shuffled per-digit values).  Per output digit t: the raw digit mod b (32-bit
 // multiply-high division), the term from the table, and v = RN(v + term) --
 // on the FP64 unit or in integer arithmetic on the unpacked sum
-// (digit_sum.cuh), chosen per dimension so that the FP64 pipe and the integer
-// pipes share the work.  Once every remaining term is below half an ulp of v
-// the lane stops.  The tile of doubles is staged in shared memory and stored
-// as 32 contiguous rows.
+// (digit_sum.cuh), chosen per dimension by a share knob.  On GB300 all-FP64
+// measures fastest (an integer add is about 30 dependent instructions, and a
+// mixed kernel carries both code paths), and an all-FP64 plan launches a
+// variant without the integer path.  Once every remaining term of a group of
+// four digits is below half an ulp of v the lane stops.  The tile of doubles
+// is staged in shared memory and stored as contiguous rows.  The grid holds
+// exactly the CTAs resident at once, striding over the equal-cost tiles.
 #include <algorithm>
 #include <vector>
 
