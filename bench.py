@@ -733,6 +733,41 @@ def run_fft(args):
         wnum = torch.linalg.norm(wrt - wr64, dim=1)
         wden = torch.linalg.norm(wr64, dim=1)
         err[g["L"]] = {"fft_max": float((num / den).max()), "fwht_max": float((wnum / wden).max()), "vectors": g["cnt"]}
+    # fused FFT -> pointwise product -> IFFT (the reference's fast kernel matrix-vector product)
+    # against the two transforms alone (a lower bound for the three steps done separately)
+    for g in groups:
+        lam = rng.standard_normal((2, g["n"]))
+        g["lr"], g["li"] = torch.from_numpy(lam[0]).cuda(), torch.from_numpy(lam[1]).cuda()
+
+    def conv_fused():
+        for g in groups:
+            _ffi.check(lib.qmc_tc_fft_mul_ifft(g["cnt"], 1, g["n"] // 2, g["lr"].data_ptr(), g["li"].data_ptr(), 0, 0,
+                                               1.0, g["xr"].data_ptr(), g["xi"].data_ptr(), h), "tc_fft_mul_ifft")
+
+    def conv_transforms_only():
+        for g in groups:
+            _ffi.check(lib.qmc_tc_fft_bro_1d(g["cnt"], 1, g["n"] // 2, g["xr"].data_ptr(), g["xi"].data_ptr(), h),
+                       "tc_fft")
+            _ffi.check(lib.qmc_tc_ifft_bro_1d(g["cnt"], 1, g["n"] // 2, g["xr"].data_ptr(), g["xi"].data_ptr(), h),
+                       "tc_ifft")
+
+    ms["conv_fused"] = gpu_ms(conv_fused, steps, warm, st)
+    ms["conv_transforms"] = gpu_ms(conv_transforms_only, steps, warm, st)
+    conv_err = {}
+    for g in groups:  # one vector per length against numpy
+        m_ = g["L"]
+        brv = np.zeros(g["n"], dtype=np.int64)
+        idx_ = np.arange(g["n"])
+        for b in range(m_):
+            brv |= ((idx_ >> b) & 1) << (m_ - 1 - b)
+        z = g["xr0"][0].cpu().numpy() + 1j * g["xi0"][0].cpu().numpy()
+        lam_c = g["lr"].cpu().numpy() + 1j * g["li"].cpu().numpy()
+        want = np.fft.ifft(np.fft.fft(z[brv], norm="ortho") * lam_c, norm="ortho")[brv]
+        xr1, xi1 = g["xr0"][:1].clone(), g["xi0"][:1].clone()
+        _ffi.check(lib.qmc_tc_fft_mul_ifft(1, 1, g["n"] // 2, g["lr"].data_ptr(), g["li"].data_ptr(), 0, 0, 1.0,
+                                           xr1.data_ptr(), xi1.data_ptr(), h), "tc_fft_mul_ifft")
+        got = xr1[0].cpu().numpy() + 1j * xi1[0].cpu().numpy()
+        conv_err[g["L"]] = float(np.linalg.norm(got - want) / np.linalg.norm(want))
     # FP64 result against numpy on one vector of the largest length
     g = groups[-1]
     m = g["L"]
@@ -770,6 +805,11 @@ def run_fft(args):
             "tc": {"fft_ms": ms["fft_tc"], "fwht_ms": ms["fwht_tc"], "fft_speedup_vs_fp64": ms["fft_fp64"] / ms["fft_tc"],
                    "fwht_speedup_vs_fp64": ms["fwht_fp64"] / ms["fwht_tc"], "max_rel_l2_error": worst,
                    "error_by_log2n": err},
+            "fft_mul_ifft": {"fused_ms": ms["conv_fused"], "fft_plus_ifft_ms": ms["conv_transforms"],
+                             "speedup_vs_transforms_alone": ms["conv_transforms"] / ms["conv_fused"],
+                             "max_rel_l2_error_vs_numpy": max(conv_err.values()), "error_by_log2n": conv_err,
+                             "note": "qmc_tc_fft_mul_ifft: y <- IFFT(FFT(y) * lam), lam of n values per length, "
+                                     "against qmc_tc_fft_bro_1d + qmc_tc_ifft_bro_1d with no pointwise step"},
             "gpu_launches": steps * sum(passes(g["L"]) for g in groups)}
 
 

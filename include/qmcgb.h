@@ -203,6 +203,22 @@ int qmc_tc_fft_bro_1d(uint64_t d1, uint64_t d2, uint64_t n_half, double *xr, dou
 int qmc_tc_ifft_bro_1d(uint64_t d1, uint64_t d2, uint64_t n_half, double *xr, double *xi, qmc_stream_t s);
 int qmc_tc_fwht_1d(uint64_t d1, uint64_t d2, uint64_t n_half, double *x, qmc_stream_t s);
 
+/* The fast kernel matrix-vector product and solve of the reference's
+ * documentation (docs/index.md:1825-1884: u = ifft(fft(y) * kt), v =
+ * ifft(fft(y) / kt), with fft = fft_bro_1d_radix2 and ifft =
+ * ifft_bro_1d_radix2) in one call, in place on (xr, xi):
+ *     y <- IFFT(FFT(y) * lam) * scale      (divide = 0)
+ *     y <- IFFT(FFT(y) / lam) * scale      (divide != 0)
+ * with the tensor-core transforms above (orthonormal; y in the FFT's input
+ * order, lam in its natural output order).  lam = (lam_r, lam_i) holds n
+ * values applied to every vector (lam_per_element = 0) or d1*d2*n values, one
+ * per element (lam_per_element = 1).  The forward transform's last pass, the
+ * pointwise step and the inverse transform's first pass run as one kernel on
+ * each tile, with FP32 intermediates between passes: about half the HBM
+ * traffic of the three steps done separately. */
+int qmc_tc_fft_mul_ifft(uint64_t d1, uint64_t d2, uint64_t n_half, const double *lam_r, const double *lam_i,
+                        uint64_t lam_per_element, int divide, double scale, double *xr, double *xi, qmc_stream_t s);
+
 /* ---- batched plans: many requests of uneven size, one persistent launch -----
  * No single reference counterpart: a plan runs, for every request, the chain
  * of reference calls written next to each struct, bit for bit, in two

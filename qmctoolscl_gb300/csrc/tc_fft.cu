@@ -7,6 +7,7 @@
 // descriptor encodings every tensor-core kernel here relies on.
 #include "fpconv.cuh"
 #include "tc_sm100.cuh"
+#include <type_traits>
 
 namespace {
 
@@ -129,7 +130,7 @@ constexpr u32 FT_KS = 96;              // K of the operands: 3 splits x 32 reals
 constexpr u32 FT_THREADS = 256;
 constexpr u32 TMEM_COLS = 128;         // three 32-column FP32 accumulators
 constexpr u32 FT_PAD = FT_TILE + FT_TILE / 16;  // shared-memory words per component, padded
-enum TcKind { TC_FFT = 0, TC_IFFT = 1, TC_WHT = 2 };
+enum TcKind { TC_FFT = 0, TC_IFFT = 1, TC_WHT = 2, TC_CONV = 3 };  // CONV: FFT steps, pointwise, IFFT steps
 
 // Shared-memory slot of tile element e: one padding word per 16, so that the
 // 32 groups a warp handles (16 consecutive elements apart in the first step)
@@ -162,6 +163,12 @@ struct TcPassArgs {
     double *xr, *xi;
     float scale;     // applied on write-back when != 1
     u32 in32, out32; // the pass reads / writes the FP32 intermediate instead of the FP64 arrays
+    // TC_CONV: between the forward and the inverse steps, y <- y * lam * lam_scale (or
+    // y / lam * lam_scale with divide); lam is n values shared by all vectors (lam_all = 0) or
+    // one per element (lam_all = 1)
+    const double *lr, *li;
+    u32 lam_all, divide;
+    float lam_scale;
 };
 
 __device__ __forceinline__ u32 brev4(u32 p) { return __brev(p) >> 28; }
@@ -247,6 +254,23 @@ __device__ __forceinline__ void twiddle(const float2 *tab, u32 t, u32 bits, floa
     twiddle_turn(tab, t << (32 - bits), bits, sign, wr, wi);
 }
 
+// The split step matrices of the forward and the inverse FFT in operand-B layout, for the
+// fused pass that runs both kinds of step on one tile (filled by tc_stepB_kernel on the
+// caller's stream before every fused transform: the same values each time)
+constexpr u32 FT_B_WORDS = 32 * FT_KS * 2 / 16;  // 16-byte words per matrix
+__device__ uint4 g_stepB[2][FT_B_WORDS];
+
+__global__ void tc_stepB_kernel()
+{
+    for (u32 e = threadIdx.x; e < 2 * 32 * FT_KS; e += blockDim.x) {
+        const u32 which = e / (32 * FT_KS), r = e % (32 * FT_KS);
+        const u32 n = r / FT_KS, rest = r % FT_KS, z = rest / 32, kk = rest % 32;
+        __nv_bfloat16 m[3];
+        split3(which ? step_matrix<TC_IFFT>(kk, n) : step_matrix<TC_FFT>(kk, n), m[0], m[1], m[2]);
+        *(__nv_bfloat16 *)((unsigned char *)g_stepB[which] + tc::kmajor_offset(n, z * 32 + kk, FT_KS)) = m[z];
+    }
+}
+
 template <int KIND>
 __global__ void __launch_bounds__(FT_THREADS, 3) tc_pass_kernel(TcPassArgs a, unsigned *err)
 {
@@ -267,7 +291,7 @@ __global__ void __launch_bounds__(FT_THREADS, 3) tc_pass_kernel(TcPassArgs a, un
     for (u32 e = threadIdx.x; e < NOUT * 3 * KIN; e += FT_THREADS) {
         const u32 n = e / (3 * KIN), rest = e % (3 * KIN), z = rest / KIN, kk = rest % KIN;
         __nv_bfloat16 m[3];
-        split3(step_matrix<KIND>(kk, n), m[0], m[1], m[2]);
+        split3(step_matrix<KIND == TC_CONV ? (int)TC_FFT : KIND>(kk, n), m[0], m[1], m[2]);
         *(__nv_bfloat16 *)(sB + tc::kmajor_offset(n, z * KIN + kk, 3 * KIN)) = m[z];
     }
     for (u32 r = threadIdx.x; r < 1024; r += FT_THREADS) {
@@ -292,7 +316,6 @@ __global__ void __launch_bounds__(FT_THREADS, 3) tc_pass_kernel(TcPassArgs a, un
     const u32 cchl = (a.k0 == 0) ? 0 : a.k0 - ctl;       // log2 column chunks: 2^k0 / ct
     const u32 tpvl = (a.k0 == 0) ? 0 : cchl + (a.L - a.k1);  // log2 tiles per vector
     const u64 ntiles = (a.k0 == 0) ? (a.total + FT_TILE - 1) / FT_TILE : (a.total >> a.L) << tpvl;
-    const float tw_sign = (KIND == TC_FFT) ? -1.0f : 1.0f;
 
     for (u64 tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
         u64 base;
@@ -351,186 +374,224 @@ __global__ void __launch_bounds__(FT_THREADS, 3) tc_pass_kernel(TcPassArgs a, un
             }
         }
         __syncthreads();
-        // steps over the pass's bits: FFT/WHT low to high, inverse high to low
-        const u32 nb = a.k1 - a.k0;
-        const u32 n16 = nb / 4, nrem = nb % 4;
-        for (u32 st = 0; st < n16 + nrem; st++) {
-            // step st covers bits [lo, lo + w) of the pass (w = 4 or 1)
-            u32 lo, w;
-            if (KIND == TC_IFFT) {  // remainder radix-2 bits first (highest), then radix-16 downward
-                if (st < nrem) { lo = nb - 1 - st; w = 1; }
-                else { lo = (n16 - 1 - (st - nrem)) * 4; w = 4; }
-            } else {
-                if (st < n16) { lo = st * 4; w = 4; }
-                else { lo = n16 * 4 + (st - n16); w = 1; }
-            }
-            const u32 k = a.k0 + lo;  // global bit of the step
-            if (w == 1) {
-                // FP32 radix-2 butterflies on bit k (as the reference's stage)
-                for (u32 b = threadIdx.x; b < Q * ct / 2; b += FT_THREADS) {
-                    const u32 cc = b & ctm, pq = b >> ctl;
-                    const u32 q1 = ((pq >> lo) << (lo + 1)) | (pq & ((1u << lo) - 1));
-                    const u32 e1 = slot(q1 * ct + cc), e2 = slot(q1 * ct + cc + (1u << lo) * ct);
-                    if (KIND == TC_WHT) {
-                        const float x1 = sr[e1], x2 = sr[e2];
-                        sr[e1] = x1 + x2;
-                        sr[e2] = x1 - x2;
-                        continue;
-                    }
-                    const u32 f1 = (u32)base + (q1 << a.k0) + cc;  // only its low k bits are used
-                    float wr, wi;
-                    twiddle(tab, f1 & ((1u << k) - 1), k + 1, tw_sign, wr, wi);
-                    const float ar = sr[e1], ai = si[e1], br = sr[e2], bi = si[e2];
-                    if (KIND == TC_FFT) {
-                        const float yr = br * wr - bi * wi, yi = br * wi + bi * wr;
-                        sr[e1] = ar + yr; si[e1] = ai + yi; sr[e2] = ar - yr; si[e2] = ai - yi;
-                    } else {
-                        const float dr = ar - br, di = ai - bi;
-                        sr[e1] = ar + br; si[e1] = ai + bi;
-                        sr[e2] = dr * wr - di * wi; si[e2] = dr * wi + di * wr;
-                    }
+        // the steps over the pass's bits for step kind SK (FFT, IFFT or WHT): false when a wait ran out
+        auto steps = [&](auto skc) -> bool {
+            constexpr int SK = decltype(skc)::value;
+            // steps over the pass's bits: FFT/WHT low to high, inverse high to low
+            const u32 nb = a.k1 - a.k0;
+            const u32 n16 = nb / 4, nrem = nb % 4;
+            for (u32 st = 0; st < n16 + nrem; st++) {
+                // step st covers bits [lo, lo + w) of the pass (w = 4 or 1)
+                u32 lo, w;
+                if (SK == TC_IFFT) {  // remainder radix-2 bits first (highest), then radix-16 downward
+                    if (st < nrem) { lo = nb - 1 - st; w = 1; }
+                    else { lo = (n16 - 1 - (st - nrem)) * 4; w = 4; }
+                } else {
+                    if (st < n16) { lo = st * 4; w = 4; }
+                    else { lo = n16 * 4 + (st - n16); w = 1; }
                 }
-                __syncthreads();
-                continue;
-            }
-            // radix-16 step through the tensor cores, two M-tiles of 128 groups
-            for (u32 mt = 0; mt < FT_GROUPS / 128 && ok; mt++) {
-                // build A: thread t handles group 128*mt + t%128, members 8*(t/128) .. +7 at
-                // elements e0 + pp*S; the eight members' BF16 terms of one product sit side by
-                // side along K (one 16-byte row of a core matrix): one 16-byte store per (product,
-                // component).  Members are split two at a time with packed BF16x2 conversions.
-                {
-                    const u32 gi = 128 * mt + (threadIdx.x & 127), half = threadIdx.x >> 7;
-                    const u32 cc = gi & ctm, qq = gi >> ctl;
-                    const u32 qlo = qq & ((1u << lo) - 1), qhi = qq >> lo;
-                    const u32 row = threadIdx.x & 127;
-                    const u32 S = (1u << lo) * ct;
-                    const u32 e0 = (qlo | (qhi << (lo + 4))) * ct + cc + half * 8 * S;
-                    // the group's offset below bit k, the same for all its members; member
-                    // half*8 + p (p < 8) has br = 2*brev3(p) + half, so its twiddle angle as a
-                    // fraction of a turn is J = cg*half + 2*cg*brev3(p) with cg = c << (28 - k)
-                    const u32 cgrp = ((u32)base + (qlo << a.k0) + cc) & ((1u << k) - 1);
-                    const u32 cg = cgrp << (28 - k), cgh = half ? cg : 0u;
-                    u32 pr[3][4], pim[3][4];  // [split][pair of members]: two BF16 per word
-#pragma unroll
-                    for (u32 pp = 0; pp < 8; pp += 2) {
-                        float xr2[2], xi2[2];
-#pragma unroll
-                        for (u32 h = 0; h < 2; h++) {
-                            const u32 e = slot(e0 + (pp + h) * S);
-                            xr2[h] = sr[e];
-                            xi2[h] = (KIND == TC_WHT) ? 0.0f : si[e];
-                            if (KIND == TC_FFT && k > 0) {  // pre-twiddle w^br(p) (w = 1 on the first step)
-                                float wr, wi;
-                                twiddle_turn(tab, cgh + 2u * cg * (brev4(pp + h) >> 1), k + 4, -1.0f, wr, wi);
-                                const float tr = xr2[h] * wr - xi2[h] * wi;
-                                xi2[h] = xr2[h] * wi + xi2[h] * wr;
-                                xr2[h] = tr;
-                            }
+                const u32 k = a.k0 + lo;  // global bit of the step
+                if (w == 1) {
+                    // FP32 radix-2 butterflies on bit k (as the reference's stage)
+                    for (u32 b = threadIdx.x; b < Q * ct / 2; b += FT_THREADS) {
+                        const u32 cc = b & ctm, pq = b >> ctl;
+                        const u32 q1 = ((pq >> lo) << (lo + 1)) | (pq & ((1u << lo) - 1));
+                        const u32 e1 = slot(q1 * ct + cc), e2 = slot(q1 * ct + cc + (1u << lo) * ct);
+                        if (SK == TC_WHT) {
+                            const float x1 = sr[e1], x2 = sr[e2];
+                            sr[e1] = x1 + x2;
+                            sr[e2] = x1 - x2;
+                            continue;
                         }
-                        // x = x1 + x2 + x3, each RN to BF16 of what is left
-                        float ar = xr2[0], br = xr2[1], ai = xi2[0], bi = xi2[1];
-#pragma unroll
-                        for (u32 z = 0; z < 3; z++) {
-                            const __nv_bfloat162 hr = __floats2bfloat162_rn(ar, br);
-                            pr[z][pp >> 1] = *(const u32 *)&hr;
-                            ar -= __low2float(hr);
-                            br -= __high2float(hr);
-                            if (KIND != TC_WHT) {
-                                const __nv_bfloat162 hi = __floats2bfloat162_rn(ai, bi);
-                                pim[z][pp >> 1] = *(const u32 *)&hi;
-                                ai -= __low2float(hi);
-                                bi -= __high2float(hi);
-                            }
-                        }
-                    }
-#pragma unroll
-                    for (u32 z = 0; z < 3; z++) {
-                        *(uint4 *)(sA + tc::kmajor_offset(row, z * KIN + half * 8, KTOT)) =
-                            make_uint4(pr[z][0], pr[z][1], pr[z][2], pr[z][3]);
-                        if (KIND != TC_WHT)
-                            *(uint4 *)(sA + tc::kmajor_offset(row, z * KIN + 16 + half * 8, KTOT)) =
-                                make_uint4(pim[z][0], pim[z][1], pim[z][2], pim[z][3]);
-                    }
-                }
-                tc::fence_smem_to_async();
-                tc::fence_before_sync();
-                __syncthreads();
-                tc::fence_after_sync();
-                if (threadIdx.x == 0) {
-                    // the six products x_za * m_zb with za + zb <= 2, each KIN/16 MMAs of K = 16 over
-                    // the matching slices of A and B; accumulators: D0, D1 the two K-slices of
-                    // x1*m1 (one MMA each), D2 the products about 2^-8 smaller; summed in FP32 on
-                    // read-back
-                    const u32 kin16 = KIN / 16;  // MMAs per product: 2 (FFT), 1 (WHT)
-                    u32 issued = 0;
-                    for (u32 j = 0; j < 6; j++) {
-                        const u32 za = prod_a(j), zb = prod_b(j);
-                        for (u32 sl = 0; sl < kin16; sl++) {
-                            const u32 dst = j == 0 ? 32u * sl : 64u;
-                            const u32 acc = j == 0 ? 0u : (issued > kin16 ? 1u : 0u);
-                            tc::mma_bf16(tmem + dst, tc::smem_desc(sA + (za * kin16 + sl) * 256, 128, sbo),
-                                         tc::smem_desc(sB + (zb * kin16 + sl) * 256, 128, sbo), idesc, acc);
-                            issued++;
-                        }
-                    }
-                    tc::mma_commit(&bar);
-                }
-                ok = __syncthreads_and(tc::mbar_wait(&bar, phase, WAIT_LIMIT) ? 1 : 0);
-                phase ^= 1;
-                tc::fence_after_sync();
-                if (!ok) break;
-                // read back: warps 0-3 the real outputs, warps 4-7 the imaginary ones
-                {
-                    const u32 gi = 128 * mt + 32 * (warp & 3) + lane;
-                    const u32 cc = gi & ctm, qq = gi >> ctl;
-                    const u32 qlo = qq & ((1u << lo) - 1), qhi = qq >> lo;
-                    const u32 S = (1u << lo) * ct;
-                    const u32 e0 = (qlo | (qhi << (lo + 4))) * ct + cc;
-                    const u32 col0 = (KIND == TC_WHT) ? 0u : 16u * (warp >> 2);
-                    if (KIND != TC_WHT || warp < 4) {
-                        const u32 lanes = (32 * (warp & 3)) << 16;
-                        u32 v0[16], v1[16], v2[16];
-                        tc::tmem_ld16(tmem + lanes + col0, v0);
-                        if (KIND != TC_WHT) tc::tmem_ld16(tmem + lanes + 32 + col0, v1);
-                        tc::tmem_ld16(tmem + lanes + 64 + col0, v2);
-                        tc::tmem_wait_ld();
-                        float *dst = (KIND == TC_WHT || warp < 4) ? sr : si;
-#pragma unroll
-                        for (u32 m = 0; m < 16; m++) {
-                            float y = __uint_as_float(v0[m]);
-                            if (KIND != TC_WHT) y += __uint_as_float(v1[m]);
-                            y += __uint_as_float(v2[m]);
-                            dst[slot(e0 + m * S)] = y;
-                        }
-                    }
-                }
-                tc::fence_before_sync();
-                __syncthreads();
-                if (KIND == TC_IFFT) {
-                    // post-twiddle w^-br(q) of the inverse step
-                    const u32 gi = 128 * mt + (threadIdx.x & 127), half = threadIdx.x >> 7;
-                    const u32 cc = gi & ctm, qq = gi >> ctl;
-                    const u32 qlo = qq & ((1u << lo) - 1), qhi = qq >> lo;
-                    const u32 S = (1u << lo) * ct;
-                    const u32 e0 = (qlo | (qhi << (lo + 4))) * ct + cc + half * 8 * S;
-                    const u32 cgrp = ((u32)base + (qlo << a.k0) + cc) & ((1u << k) - 1);
-                    const u32 cg = cgrp << (28 - k), cgh = half ? cg : 0u;
-                    if (k > 0) {
-#pragma unroll
-                        for (u32 pp = 0; pp < 8; pp++) {
-                            const u32 e = slot(e0 + pp * S);
-                            float wr, wi;
-                            twiddle_turn(tab, cgh + 2u * cg * (brev4(pp) >> 1), k + 4, 1.0f, wr, wi);
-                            const float xr_ = sr[e], xi_ = si[e];
-                            sr[e] = xr_ * wr - xi_ * wi;
-                            si[e] = xr_ * wi + xi_ * wr;
+                        const u32 f1 = (u32)base + (q1 << a.k0) + cc;  // only its low k bits are used
+                        float wr, wi;
+                        twiddle(tab, f1 & ((1u << k) - 1), k + 1, SK == TC_FFT ? -1.0f : 1.0f, wr, wi);
+                        const float ar = sr[e1], ai = si[e1], br = sr[e2], bi = si[e2];
+                        if (SK == TC_FFT) {
+                            const float yr = br * wr - bi * wi, yi = br * wi + bi * wr;
+                            sr[e1] = ar + yr; si[e1] = ai + yi; sr[e2] = ar - yr; si[e2] = ai - yi;
+                        } else {
+                            const float dr = ar - br, di = ai - bi;
+                            sr[e1] = ar + br; si[e1] = ai + bi;
+                            sr[e2] = dr * wr - di * wi; si[e2] = dr * wi + di * wr;
                         }
                     }
                     __syncthreads();
+                    continue;
                 }
+                // radix-16 step through the tensor cores, two M-tiles of 128 groups
+                for (u32 mt = 0; mt < FT_GROUPS / 128 && ok; mt++) {
+                    // build A: thread t handles group 128*mt + t%128, members 8*(t/128) .. +7 at
+                    // elements e0 + pp*S; the eight members' BF16 terms of one product sit side by
+                    // side along K (one 16-byte row of a core matrix): one 16-byte store per (product,
+                    // component).  Members are split two at a time with packed BF16x2 conversions.
+                    {
+                        const u32 gi = 128 * mt + (threadIdx.x & 127), half = threadIdx.x >> 7;
+                        const u32 cc = gi & ctm, qq = gi >> ctl;
+                        const u32 qlo = qq & ((1u << lo) - 1), qhi = qq >> lo;
+                        const u32 row = threadIdx.x & 127;
+                        const u32 S = (1u << lo) * ct;
+                        const u32 e0 = (qlo | (qhi << (lo + 4))) * ct + cc + half * 8 * S;
+                        // the group's offset below bit k, the same for all its members; member
+                        // half*8 + p (p < 8) has br = 2*brev3(p) + half, so its twiddle angle as a
+                        // fraction of a turn is J = cg*half + 2*cg*brev3(p) with cg = c << (28 - k)
+                        const u32 cgrp = ((u32)base + (qlo << a.k0) + cc) & ((1u << k) - 1);
+                        const u32 cg = cgrp << (28 - k), cgh = half ? cg : 0u;
+                        u32 pr[3][4], pim[3][4];  // [split][pair of members]: two BF16 per word
+#pragma unroll
+                        for (u32 pp = 0; pp < 8; pp += 2) {
+                            float xr2[2], xi2[2];
+#pragma unroll
+                            for (u32 h = 0; h < 2; h++) {
+                                const u32 e = slot(e0 + (pp + h) * S);
+                                xr2[h] = sr[e];
+                                xi2[h] = (SK == TC_WHT) ? 0.0f : si[e];
+                                if (SK == TC_FFT && k > 0) {  // pre-twiddle w^br(p) (w = 1 on the first step)
+                                    float wr, wi;
+                                    twiddle_turn(tab, cgh + 2u * cg * (brev4(pp + h) >> 1), k + 4, -1.0f, wr, wi);
+                                    const float tr = xr2[h] * wr - xi2[h] * wi;
+                                    xi2[h] = xr2[h] * wi + xi2[h] * wr;
+                                    xr2[h] = tr;
+                                }
+                            }
+                            // x = x1 + x2 + x3, each RN to BF16 of what is left
+                            float ar = xr2[0], br = xr2[1], ai = xi2[0], bi = xi2[1];
+#pragma unroll
+                            for (u32 z = 0; z < 3; z++) {
+                                const __nv_bfloat162 hr = __floats2bfloat162_rn(ar, br);
+                                pr[z][pp >> 1] = *(const u32 *)&hr;
+                                ar -= __low2float(hr);
+                                br -= __high2float(hr);
+                                if (SK != TC_WHT) {
+                                    const __nv_bfloat162 hi = __floats2bfloat162_rn(ai, bi);
+                                    pim[z][pp >> 1] = *(const u32 *)&hi;
+                                    ai -= __low2float(hi);
+                                    bi -= __high2float(hi);
+                                }
+                            }
+                        }
+#pragma unroll
+                        for (u32 z = 0; z < 3; z++) {
+                            *(uint4 *)(sA + tc::kmajor_offset(row, z * KIN + half * 8, KTOT)) =
+                                make_uint4(pr[z][0], pr[z][1], pr[z][2], pr[z][3]);
+                            if (SK != TC_WHT)
+                                *(uint4 *)(sA + tc::kmajor_offset(row, z * KIN + 16 + half * 8, KTOT)) =
+                                    make_uint4(pim[z][0], pim[z][1], pim[z][2], pim[z][3]);
+                        }
+                    }
+                    tc::fence_smem_to_async();
+                    tc::fence_before_sync();
+                    __syncthreads();
+                    tc::fence_after_sync();
+                    if (threadIdx.x == 0) {
+                        // the six products x_za * m_zb with za + zb <= 2, each KIN/16 MMAs of K = 16 over
+                        // the matching slices of A and B; accumulators: D0, D1 the two K-slices of
+                        // x1*m1 (one MMA each), D2 the products about 2^-8 smaller; summed in FP32 on
+                        // read-back
+                        const u32 kin16 = KIN / 16;  // MMAs per product: 2 (FFT), 1 (WHT)
+                        u32 issued = 0;
+                        for (u32 j = 0; j < 6; j++) {
+                            const u32 za = prod_a(j), zb = prod_b(j);
+                            for (u32 sl = 0; sl < kin16; sl++) {
+                                const u32 dst = j == 0 ? 32u * sl : 64u;
+                                const u32 acc = j == 0 ? 0u : (issued > kin16 ? 1u : 0u);
+                                tc::mma_bf16(tmem + dst, tc::smem_desc(sA + (za * kin16 + sl) * 256, 128, sbo),
+                                             tc::smem_desc(sB + (zb * kin16 + sl) * 256, 128, sbo), idesc, acc);
+                                issued++;
+                            }
+                        }
+                        tc::mma_commit(&bar);
+                    }
+                    ok = __syncthreads_and(tc::mbar_wait(&bar, phase, WAIT_LIMIT) ? 1 : 0);
+                    phase ^= 1;
+                    tc::fence_after_sync();
+                    if (!ok) break;
+                    // read back: warps 0-3 the real outputs, warps 4-7 the imaginary ones
+                    {
+                        const u32 gi = 128 * mt + 32 * (warp & 3) + lane;
+                        const u32 cc = gi & ctm, qq = gi >> ctl;
+                        const u32 qlo = qq & ((1u << lo) - 1), qhi = qq >> lo;
+                        const u32 S = (1u << lo) * ct;
+                        const u32 e0 = (qlo | (qhi << (lo + 4))) * ct + cc;
+                        const u32 col0 = (SK == TC_WHT) ? 0u : 16u * (warp >> 2);
+                        if (SK != TC_WHT || warp < 4) {
+                            const u32 lanes = (32 * (warp & 3)) << 16;
+                            u32 v0[16], v1[16], v2[16];
+                            tc::tmem_ld16(tmem + lanes + col0, v0);
+                            if (SK != TC_WHT) tc::tmem_ld16(tmem + lanes + 32 + col0, v1);
+                            tc::tmem_ld16(tmem + lanes + 64 + col0, v2);
+                            tc::tmem_wait_ld();
+                            float *dst = (SK == TC_WHT || warp < 4) ? sr : si;
+#pragma unroll
+                            for (u32 m = 0; m < 16; m++) {
+                                float y = __uint_as_float(v0[m]);
+                                if (SK != TC_WHT) y += __uint_as_float(v1[m]);
+                                y += __uint_as_float(v2[m]);
+                                dst[slot(e0 + m * S)] = y;
+                            }
+                        }
+                    }
+                    tc::fence_before_sync();
+                    __syncthreads();
+                    if (SK == TC_IFFT) {
+                        // post-twiddle w^-br(q) of the inverse step
+                        const u32 gi = 128 * mt + (threadIdx.x & 127), half = threadIdx.x >> 7;
+                        const u32 cc = gi & ctm, qq = gi >> ctl;
+                        const u32 qlo = qq & ((1u << lo) - 1), qhi = qq >> lo;
+                        const u32 S = (1u << lo) * ct;
+                        const u32 e0 = (qlo | (qhi << (lo + 4))) * ct + cc + half * 8 * S;
+                        const u32 cgrp = ((u32)base + (qlo << a.k0) + cc) & ((1u << k) - 1);
+                        const u32 cg = cgrp << (28 - k), cgh = half ? cg : 0u;
+                        if (k > 0) {
+#pragma unroll
+                            for (u32 pp = 0; pp < 8; pp++) {
+                                const u32 e = slot(e0 + pp * S);
+                                float wr, wi;
+                                twiddle_turn(tab, cgh + 2u * cg * (brev4(pp) >> 1), k + 4, 1.0f, wr, wi);
+                                const float xr_ = sr[e], xi_ = si[e];
+                                sr[e] = xr_ * wr - xi_ * wi;
+                                si[e] = xr_ * wi + xi_ * wr;
+                            }
+                        }
+                        __syncthreads();
+                    }
+                }
+                if (!ok) return false;
             }
-            if (!ok) break;
+            return true;
+        };
+        if constexpr (KIND == TC_CONV) {
+            ok = steps(std::integral_constant<int, TC_FFT>{});
+            if (ok) {
+                // y <- y * lam * s or y / lam * s at the forward transform's output positions f
+                for (u32 e = threadIdx.x; e < Q * ct; e += FT_THREADS) {
+                    const u64 f = base + ((u64)(e >> ctl) << a.k0) + (e & ctm);
+                    if (f >= a.total) continue;
+                    const u64 li_ = a.lam_all ? f : (f & ((1ull << a.L) - 1));
+                    const float lr = to_f32((u64)__double_as_longlong(a.lr[li_]));
+                    const float lm = to_f32((u64)__double_as_longlong(a.li[li_]));
+                    const u32 sl = slot(e);
+                    const float yr = sr[sl], yi = si[sl];
+                    if (a.divide) {
+                        const float q = __fdiv_rn(a.lam_scale, fmaf(lr, lr, lm * lm));
+                        sr[sl] = (yr * lr + yi * lm) * q;
+                        si[sl] = (yi * lr - yr * lm) * q;
+                    } else {
+                        sr[sl] = (yr * lr - yi * lm) * a.lam_scale;
+                        si[sl] = (yr * lm + yi * lr) * a.lam_scale;
+                    }
+                }
+                // operand B: the inverse step matrix for the inverse steps, then the forward one again
+                for (u32 i = threadIdx.x; i < FT_B_WORDS; i += FT_THREADS) ((uint4 *)sB)[i] = g_stepB[1][i];
+                tc::fence_smem_to_async();
+                __syncthreads();
+                ok = steps(std::integral_constant<int, TC_IFFT>{});
+                for (u32 i = threadIdx.x; i < FT_B_WORDS; i += FT_THREADS) ((uint4 *)sB)[i] = g_stepB[0][i];
+                tc::fence_smem_to_async();
+                __syncthreads();
+            }
+        } else {
+            ok = steps(std::integral_constant<int, KIND>{});
         }
         if (!ok) break;
         // store, pairs of adjacent elements as 16-byte stores
@@ -614,9 +675,86 @@ int run_tc(int kind, u64 d1, u64 d2, u64 n_half, double *xr, double *xi, cudaStr
     return QMC_OK;
 }
 
+// y <- IFFT(FFT(y) * lam) * scale, or with / lam: the forward passes but the last, one fused
+// pass over the highest bits (forward steps, the pointwise operation, inverse steps), the
+// inverse passes but the first; FP32 intermediates throughout, the orthonormal factors 1/n
+// folded into the pointwise scale
+int run_conv(u64 d1, u64 d2, u64 n_half, const double *lr, const double *li, u64 lam_all, int divide, double scale,
+             double *xr, double *xi, cudaStream_t s, const char *what)
+{
+    QMC_REQUIRE_DOMAIN(n_half > 0 && (n_half & (n_half - 1)) == 0 && n_half <= (1ull << 23),
+                       "%s: n = 2*n_half must be a power of two up to 2^24", what);
+    const u64 nvec = d1 * d2, n = 2 * n_half;
+    if (nvec == 0) return QMC_OK;
+    QMC_REQUIRE(xr && xi && lr && li, "%s: null data pointer", what);
+    QMC_REQUIRE(lam_all <= 1, "%s: lam_all is 0 (n values for every vector) or 1 (one per element)", what);
+    QMC_REQUIRE((((uintptr_t)xr | (uintptr_t)xi) & 15) == 0, "%s: data arrays must be 16-byte aligned", what);
+    unsigned *err = qmcgb::device_error_ptr();
+    QMC_REQUIRE(err, "device error word unavailable");
+    u32 L = 0;
+    while ((1ull << L) < n) L++;
+    struct P { u32 k0, k1; } passes[8];
+    int np = 0;
+    passes[np++] = {0, L < 12 ? L : 12};
+    for (u32 k0 = 12; k0 < L; k0 += 8) passes[np++] = {k0, (k0 + 8 < L) ? k0 + 8 : L};
+    const size_t smem = FT_PAD * 8 + 128 * FT_KS * 2 + 32 * FT_KS * 2 + 1024 * 8;
+    tc_stepB_kernel<<<1, FT_THREADS, 0, s>>>();
+    if (int rc = qmcgb::launch_status(what)) return rc;
+    // launch order: forward passes 0 .. np-2, the fused pass np-1, inverse passes np-2 .. 0
+    for (int li_ = 0; li_ < 2 * np - 1; li_++) {
+        const int pi = li_ < np ? li_ : 2 * np - 2 - li_;
+        const int kind = li_ < np - 1 ? TC_FFT : li_ == np - 1 ? TC_CONV : TC_IFFT;
+        const P p = passes[pi];
+        TcPassArgs A{};
+        A.total = nvec * n;
+        A.L = L;
+        A.k0 = p.k0;
+        A.k1 = p.k1;
+        if (p.k0 == 0) {
+            A.Q = FT_TILE;
+            A.ct = 1;
+        } else {
+            A.Q = 1u << (p.k1 - p.k0);
+            A.ct = FT_TILE / A.Q;
+            if ((1ull << p.k0) < A.ct) A.ct = (u32)(1ull << p.k0);
+        }
+        A.xr = xr;
+        A.xi = xi;
+        A.scale = 1.0f;
+        A.in32 = li_ > 0 ? 1u : 0u;
+        A.out32 = li_ < 2 * np - 2 ? 1u : 0u;
+        A.lr = lr;
+        A.li = li;
+        A.lam_all = (u32)lam_all;
+        A.divide = divide ? 1u : 0u;
+        A.lam_scale = (float)(scale / (double)n);
+        const u64 tiles = (p.k0 == 0) ? (A.total + FT_TILE - 1) / FT_TILE : A.total / (A.Q * (u64)A.ct);
+        const unsigned grid = qmcgb::grid_for(tiles, 1, (unsigned)qmcgb::sm_count() * 3);
+        if (kind == TC_FFT) {
+            if (int rc = qmcgb::raise_smem_limit((const void *)tc_pass_kernel<TC_FFT>, smem, what)) return rc;
+            tc_pass_kernel<TC_FFT><<<grid, FT_THREADS, smem, s>>>(A, err);
+        } else if (kind == TC_IFFT) {
+            if (int rc = qmcgb::raise_smem_limit((const void *)tc_pass_kernel<TC_IFFT>, smem, what)) return rc;
+            tc_pass_kernel<TC_IFFT><<<grid, FT_THREADS, smem, s>>>(A, err);
+        } else {
+            if (int rc = qmcgb::raise_smem_limit((const void *)tc_pass_kernel<TC_CONV>, smem, what)) return rc;
+            tc_pass_kernel<TC_CONV><<<grid, FT_THREADS, smem, s>>>(A, err);
+        }
+        if (int rc = qmcgb::launch_status(what)) return rc;
+    }
+    return QMC_OK;
+}
+
 }  // namespace
 
 extern "C" {
+
+int qmc_tc_fft_mul_ifft(uint64_t d1, uint64_t d2, uint64_t n_half, const double *lam_r, const double *lam_i,
+                        uint64_t lam_per_element, int divide, double scale, double *xr, double *xi, qmc_stream_t s)
+{
+    return run_conv(d1, d2, n_half, lam_r, lam_i, lam_per_element, divide, scale, xr, xi, QMC_STREAM(s),
+                    "tc_fft_mul_ifft");
+}
 
 int qmc_tc_fft_bro_1d(uint64_t d1, uint64_t d2, uint64_t n_half, double *xr, double *xi, qmc_stream_t s)
 {

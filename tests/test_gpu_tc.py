@@ -64,3 +64,64 @@ def test_tc_fwht_against_fp64(m):
     tc_fft.fwht_1d_tc(2, 1, n // 2, x)
     err = np.linalg.norm(x - want) / np.linalg.norm(want)
     assert err < 1e-6, err
+
+
+def _fft_bro_np(x, br):
+    """fft_bro_1d_radix2 of docs/index.md:1815: np.fft.fft of the bit-reversed input, orthonormal."""
+    return np.fft.fft(x[..., br], norm="ortho")
+
+
+def _ifft_bro_np(X, br):
+    """ifft_bro_1d_radix2: the inverse of _fft_bro_np (natural input, bit-reversed output)."""
+    return np.fft.ifft(X, norm="ortho")[..., br]
+
+
+@pytest.mark.parametrize("m,d1,d2,per_element,divide", [(1, 1, 1, False, False), (5, 2, 1, False, False),
+                                                        (10, 1, 3, True, False), (12, 2, 2, False, True),
+                                                        (13, 1, 2, False, False), (16, 1, 1, True, True),
+                                                        (20, 1, 1, False, False), (22, 1, 1, False, True)])
+def test_tc_fft_mul_ifft_against_numpy(m, d1, d2, per_element, divide):
+    """y <- IFFT(FFT(y) * lam) * s (or / lam) in one call against numpy: one, two and three
+    passes, lam shared or per element, product and quotient."""
+    from qmctoolscl_gb300 import tc_fft
+    rng = np.random.Generator(np.random.SFC64(300 + m))
+    n = 1 << m
+    br = _bitrev(m)
+    y = rng.standard_normal((d1, d2, n)) + 1j * rng.standard_normal((d1, d2, n))
+    shape = (d1, d2, n) if per_element else (n,)
+    lam = (0.5 + rng.random(shape)) * np.exp(2j * np.pi * rng.random(shape))  # |lam| in [0.5, 1.5)
+    scale = float(np.sqrt(2 * n))
+    Y = _fft_bro_np(y, br)
+    want = _ifft_bro_np(Y / lam if divide else Y * lam, br) * scale
+    xr, xi = np.ascontiguousarray(y.real), np.ascontiguousarray(y.imag)
+    tc_fft.fft_mul_ifft_tc(d1, d2, n // 2, np.ascontiguousarray(lam.real), np.ascontiguousarray(lam.imag), xr, xi,
+                           divide=divide, scale=scale)
+    err = np.linalg.norm((xr + 1j * xi) - want) / np.linalg.norm(want)
+    assert err < 1e-6, err
+
+
+def test_tc_fft_mul_ifft_reference_matvec_and_solve():
+    """The fast kernel matrix-vector product and solve of docs/index.md:1825-1884 (u =
+    ifft(yt*kt)*sqrt(2n), v = ifft(yt/kt)/sqrt(2n), kt = fft(k)) with the kernel's
+    transform kt from the FP64 drop-in fft_bro_1d_radix2, against numpy (TC tolerance)."""
+    import qmctoolscl_gb300 as q
+    from qmctoolscl_gb300 import tc_fft
+    rng = np.random.Generator(np.random.SFC64(7))
+    m = 10
+    n = 1 << m
+    ir = _bitrev(m + 1)
+    y = rng.random(2 * n) + 1j * rng.random(2 * n)
+    k = rng.random(2 * n) + 0j
+    kr, ki = np.ascontiguousarray(k.real), np.ascontiguousarray(k.imag)
+    q.fft_bro_1d_radix2(np.uint64(1), np.uint64(1), np.uint64(n), np.empty(2 * n), np.empty(2 * n), kr, ki)
+    u_np = np.fft.ifft(np.fft.fft(y[ir], norm="ortho") * np.fft.fft(k[ir], norm="ortho"), norm="ortho")[ir] \
+        * np.sqrt(2 * n)
+    v_np = np.fft.ifft(np.fft.fft(y[ir], norm="ortho") / np.fft.fft(k[ir], norm="ortho"), norm="ortho")[ir] \
+        / np.sqrt(2 * n)
+    # the solve divides by kt: its error is the transforms' (about 1e-7) times kt's condition
+    cond = np.abs(kr + 1j * ki).max() / np.abs(kr + 1j * ki).min()
+    for divide, scale, want, tol in ((False, np.sqrt(2 * n), u_np, 1e-6), (True, 1 / np.sqrt(2 * n), v_np, 1e-6 * cond)):
+        xr, xi = np.ascontiguousarray(y.real), np.ascontiguousarray(y.imag)
+        tc_fft.fft_mul_ifft_tc(1, 1, n, kr, ki, xr, xi, divide=divide, scale=scale)
+        err = np.linalg.norm((xr + 1j * xi) - want) / np.linalg.norm(want)
+        assert err < tol, (divide, err, cond)
