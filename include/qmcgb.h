@@ -203,6 +203,18 @@ int qmc_tc_fft_bro_1d(uint64_t d1, uint64_t d2, uint64_t n_half, double *xr, dou
 int qmc_tc_ifft_bro_1d(uint64_t d1, uint64_t d2, uint64_t n_half, double *xr, double *xi, qmc_stream_t s);
 int qmc_tc_fwht_1d(uint64_t d1, uint64_t d2, uint64_t n_half, double *x, qmc_stream_t s);
 
+/* ---- generalized Halton (qrng) ---------------------------------------------
+ * qmctoolscl/c_funcs/halton_qrng.c:3-162, the raw ctypes binding halton_qrng_c
+ * of the reference (pdm_build.py:84-94): n points (indices n0 .. n0+n-1) of d
+ * dimensions of the generalized Halton sequence in the form of the R package
+ * qrng, res d x n (dimension-major), randu_d_32 d x 32 uniforms for the digit
+ * shifts, dvec the prime index of each dimension; bit for bit the reference's
+ * values.  d above 360 or n + n0 above 2^31 - 1 (undefined in the reference)
+ * return QMC_ERR_DOMAIN; a dvec entry outside [0, 360) sets bit 1 of the device
+ * error word and leaves that dimension unwritten. */
+int qmc_halton_qrng(int n, int d, int n0, int generalized, double *res, const double *randu_d_32, const int *dvec,
+                    qmc_stream_t s);
+
 /* The fast kernel matrix-vector product and solve of the reference's
  * documentation (docs/index.md:1825-1884: u = ifft(fft(y) * kt), v =
  * ifft(fft(y) / kt), with fft = fft_bro_1d_radix2 and ifft =

@@ -90,3 +90,29 @@ def call_ref(name, *args):
     """Run the compiled reference C function ``name`` (bs_* set to the extents)."""
     a = list(args)
     ref_lib()[name](*(a[:3] + a[:3] + a[3:]))
+
+
+_QRNG_ARGTYPES = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                  np.ctypeslib.ndpointer(ctypes.c_double, flags="C_CONTIGUOUS"),
+                  np.ctypeslib.ndpointer(ctypes.c_double, flags="C_CONTIGUOUS"),
+                  np.ctypeslib.ndpointer(ctypes.c_int, flags="C_CONTIGUOUS")]
+
+
+def _qrng(path, symbol):
+    fn = getattr(ctypes.CDLL(path), symbol)
+    fn.argtypes = _QRNG_ARGTYPES
+    fn.restype = None
+    return fn
+
+
+def halton_qrng(n, d, n0, generalized, res, randu_d_32, dvec):
+    """The oracle restatement of halton_qrng (qmctoolscl/c_funcs/halton_qrng.c:3-162):
+    res (d x n) filled in place."""
+    if not os.path.exists(ORACLE_SO):
+        build()
+    _qrng(ORACLE_SO, "oracle_halton_qrng")(n, d, n0, generalized, res, randu_d_32, dvec)
+
+
+def halton_qrng_ref(n, d, n0, generalized, res, randu_d_32, dvec):
+    """The reference's own compiled halton_qrng (where oracle/_ref is built)."""
+    _qrng(REF_SO, "halton_qrng")(n, d, n0, generalized, res, randu_d_32, dvec)

@@ -541,3 +541,85 @@ ORACLE_API void oracle_fwht_1d_radix2(u64 d1, u64 d2, u64 n_half, double *x)
         }
     }
 }
+
+/* ------------------------------------------------------------------------ */
+/* qmctoolscl/c_funcs/halton_qrng.c:3-162: the generalized Halton sequence of
+ * Faure and Lemieux in the form of the R package qrng (ghalton): for point i
+ * and dimension j with base b = the dvec[j]-th prime, the 32 base-b digits of
+ * i, each mapped to (f * digit + s_k) mod b with the multiplier f (1, or the
+ * table below when generalized) and the random digit shift
+ * s_k = (int)(b * randu_d_32[j*32+k]), summed by Horner's rule from digit 31
+ * down, every add and divide rounded (halton_qrng.c:133-140).  Output res is
+ * d x n (dimension-major); point 0 (when n0 = 0) is the shift alone
+ * (halton_qrng.c:68-83). */
+
+/* the scrambling multipliers of the generalized sequence, one per prime
+ * (halton_qrng.c:37-60): a published table that the parity needs as it is */
+static const int QRNG_MULT[360] = {
+    1, 1, 3, 3, 4, 9, 7, 5, 9, 18, 18, 8, 13, 31, 9, 19, 36, 33,
+    21, 44, 43, 61, 60, 56, 26, 71, 32, 77, 26, 95, 92, 47, 29, 61, 57, 69,
+    115, 63, 92, 31, 104, 126, 50, 80, 55, 152, 114, 80, 83, 97, 95, 150, 148, 55,
+    80, 192, 71, 76, 82, 109, 105, 173, 58, 143, 56, 177, 203, 239, 196, 143, 278, 227,
+    87, 274, 264, 84, 226, 163, 231, 177, 95, 116, 165, 131, 156, 105, 188, 142, 105, 125,
+    269, 292, 215, 182, 294, 152, 148, 144, 382, 194, 346, 323, 220, 174, 133, 324, 215, 246,
+    159, 337, 254, 423, 484, 239, 440, 362, 464, 376, 398, 174, 149, 418, 306, 282, 434, 196,
+    458, 313, 512, 450, 161, 315, 441, 549, 555, 431, 295, 557, 172, 343, 472, 604, 297, 524,
+    251, 514, 385, 531, 663, 674, 255, 519, 324, 391, 394, 533, 253, 717, 651, 399, 596, 676,
+    425, 261, 404, 691, 604, 274, 627, 777, 269, 217, 599, 447, 581, 640, 666, 595, 669, 686,
+    305, 460, 599, 335, 258, 649, 771, 619, 666, 669, 707, 737, 854, 925, 818, 424, 493, 463,
+    535, 782, 476, 451, 520, 886, 340, 793, 390, 381, 274, 500, 581, 345, 363, 1024, 514, 773,
+    932, 556, 954, 793, 294, 863, 393, 827, 527, 1007, 622, 549, 613, 799, 408, 856, 601, 1072,
+    938, 322, 1142, 873, 629, 1071, 1063, 1205, 596, 973, 984, 875, 918, 1133, 1223, 933, 1110, 1228,
+    1017, 701, 480, 678, 1172, 689, 1138, 1022, 682, 613, 635, 984, 526, 1311, 459, 1348, 477, 716,
+    1075, 682, 1245, 401, 774, 1026, 499, 1314, 743, 693, 1282, 1003, 1181, 1079, 765, 815, 1350, 1144,
+    1449, 718, 805, 1203, 1173, 737, 562, 579, 701, 1104, 1105, 1379, 827, 1256, 759, 540, 1284, 1188,
+    776, 853, 1140, 445, 1265, 802, 932, 632, 1504, 856, 1229, 1619, 774, 1229, 1300, 1563, 1551, 1265,
+    905, 1333, 493, 913, 1397, 1250, 612, 1251, 1765, 1303, 595, 981, 671, 1403, 820, 1404, 1661, 973,
+    1340, 1015, 1649, 855, 1834, 1621, 1704, 893, 1033, 721, 1737, 1507, 1851, 1006, 994, 923, 872, 1860,
+};
+
+static int qrng_prime(int idx)  /* the (idx+1)-th prime, idx < 360 (halton_qrng.c:28-35) */
+{
+    int count = -1, c = 1;
+    while (count < idx) {
+        c++;
+        int is_p = 1;
+        for (int q = 2; q * q <= c; q++)
+            if (c % q == 0) {
+                is_p = 0;
+                break;
+            }
+        count += is_p;
+    }
+    return c;
+}
+
+ORACLE_API void oracle_halton_qrng(int n, int d, int n0, int generalized, double *res, const double *randu_d_32,
+                                   const int *dvec)
+{
+    for (int j = 0; j < d; j++) {
+        const int b = qrng_prime(dvec[j]);
+        const unsigned f = generalized ? (unsigned)QRNG_MULT[dvec[j]] : 1u;
+        unsigned s[32];
+        double u = 0.0;
+        for (int k = 31; k >= 0; k--) {
+            s[k] = (unsigned)(int)(b * randu_d_32[j * 32 + k]);
+            u += s[k];
+            u /= b;
+        }
+        if (n0 == 0) res[(long)j * n] = u;
+        for (int i = n0 == 0 ? 1 : n0; i < n + n0; i++) {
+            unsigned dg[32] = {0}, t = (unsigned)i;
+            for (int k = 0; t > 0 && k < 32; k++) {
+                dg[k] = t % (unsigned)b;
+                t /= (unsigned)b;
+            }
+            double v = 0.0;
+            for (int k = 31; k >= 0; k--) {
+                v += (f * dg[k] + s[k]) % (unsigned)b;
+                v /= b;
+            }
+            res[(long)j * n + (i - n0)] = v;
+        }
+    }
+}

@@ -30,6 +30,7 @@ EXTRA = {
     "qmc_tc_ifft_bro_1d": [U64, U64, U64, PTR, PTR, PTR],
     "qmc_tc_fwht_1d": [U64, U64, U64, PTR, PTR],
     "qmc_tc_fft_mul_ifft": [U64, U64, U64, PTR, PTR, U64, INT, ctypes.c_double, PTR, PTR, PTR],
+    "qmc_halton_qrng": [INT, INT, INT, INT, PTR, PTR, PTR, PTR],
 }
 
 
