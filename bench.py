@@ -1177,8 +1177,66 @@ def run_gdn_plain(args):
             "kernels": res, "gpu_launches": (15 + len(other)) * args.steps}
 
 
+def run_qrng(args):
+    """The generalized Halton sequence of halton_qrng (qmctoolscl/c_funcs/halton_qrng.c:3-162):
+    n = 2^20 points of d = 100 dimensions (the first 100 primes), generalized multipliers,
+    through the C ABI; checked against the oracle on a slice; the oracle over all host threads
+    (one dimension per task) as the CPU baseline."""
+    import torch
+    import oracle
+    from qmctoolscl_gb300 import _ffi
+    lib = _ffi.lib()
+    n, d = 1 << (16 if args.small else 20), 100
+    rng = np.random.Generator(np.random.SFC64(6))
+    randu_np = rng.random(d * 32)
+    dvec_np = np.arange(d, dtype=np.int32)
+    randu, dvec = torch.from_numpy(randu_np).cuda(), torch.from_numpy(dvec_np).cuda()
+    res = torch.empty(d * n, dtype=torch.float64, device="cuda")
+    st = torch.cuda.current_stream()
+    h = st.cuda_stream
+
+    def step():
+        _ffi.check(lib.qmc_halton_qrng(n, d, 0, 1, res.data_ptr(), randu.data_ptr(), dvec.data_ptr(), h), "qrng")
+
+    ms = gpu_ms(step, args.steps, args.warmup, st)
+    _ffi.check(lib.qmc_device_error_check(h), "qrng")
+    # parity on a slice: every dimension, points n0 .. n0+4095 of the same run
+    nn, n0 = 4096, n // 2
+    want = np.empty(d * nn)
+    oracle.halton_qrng(nn, d, n0, 1, want, randu_np, dvec_np)
+    got = res.view(d, n)[:, n0:n0 + nn].cpu().numpy().reshape(-1)
+    assert np.array_equal(got.view(np.uint64), want.view(np.uint64)), "halton_qrng differs from the oracle"
+    # CPU: the oracle on all host threads, one dimension per task, a sample of the points
+    threads = host_threads()
+    ns = 1 << (15 if args.small else 19)  # about 10 CPU-seconds on 16 cores
+
+    def one_dim(j):
+        r_ = np.empty(ns)
+        oracle.halton_qrng(ns, 1, 0, 1, r_, np.ascontiguousarray(randu_np[j * 32:(j + 1) * 32]), dvec_np[j:j + 1])
+
+    t0 = time.perf_counter()
+    with concurrent.futures.ThreadPoolExecutor(threads) as ex:
+        list(ex.map(one_dim, range(d)))
+    t_cpu = time.perf_counter() - t0
+    pts = n
+    return {"metric": METRIC, "value": pts / (ms / 1e3), "unit": "points/s (d=100)", "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64 adds and divides (the reference's Horner steps)",
+            "data": "synthetic (np.random.SFC64(6)) digit-shift uniforms",
+            "config": {"workload": "halton_qrng, generalized, n=2^%d, d=100 (first 100 primes)" % (n.bit_length() - 1),
+                       "n": n, "d": d, "l2": "%.0f MB output per step" % (8 * n * d / 1e6)},
+            "roofline": dict(roofline(8.0 * n * d, ms), kernel="halton_qrng_kernel",
+                             note="bound by the FP64 unit: each digit step is the reference's rounded add and "
+                                  "divide (a divide is several FP64 operations), not by HBM"),
+            "gpu_launches": args.steps,
+            "cpu_baseline": {"value": ns / t_cpu, "unit": "points/s (d=100)", "cores": threads, "kind": "port",
+                             "sample": "2^%d points of all 100 dimensions, one dimension per thread, by the oracle "
+                                       "(C restatement of halton_qrng.c)" % (ns.bit_length() - 1), "seconds": t_cpu,
+                             "cpu_seconds": t_cpu * threads}}
+
+
 WORKLOADS = {"net_plain": run_net_plain, "net_lms": run_net_lms, "fft": run_fft, "halton": run_halton,
-             "plain": run_gdn_plain, "gdn_plain": run_gdn_plain}
+             "plain": run_gdn_plain, "gdn_plain": run_gdn_plain, "qrng": run_qrng}
 
 
 def main():

@@ -11,12 +11,21 @@
 // count m are zero, so the Horner steps over them are the same for every
 // point with m digits.  Each CTA owns one dimension and computes, once, the
 // prefix P[m] after the steps k = 31 .. m (P[0] is the reference's point 0);
-// a point then needs only its own m steps, each the reference's FP64 add and
-// divide.  The digits come from the top down by divisions by b^k (32-bit
+// a point then needs only its own m steps, each the reference's rounded add
+// and divide -- in integer arithmetic (qrng_step.cuh), because on GB300 an
+// FP64 divide is a sequence of several operations on the narrow FP64 pipe.
+// The digits come from the top down by divisions by b^k (32-bit
 // multiply-high, exact).
 #include "common.cuh"
+#include "qrng_step.cuh"
 
 namespace {
+
+// the step with the FP64 operations, out of line, for what qstep::step leaves out
+__device__ __noinline__ u64 qrng_step_hw(u64 v, u32 c, double bd)
+{
+    return (u64)__double_as_longlong(__ddiv_rn(__dadd_rn(__longlong_as_double((long long)v), (double)c), bd));
+}
 
 constexpr int QRNG_DIMS = 360;
 
@@ -71,7 +80,9 @@ __constant__ int c_qrng_mult[QRNG_DIMS] = {
 
 constexpr u32 QRNG_THREADS = 256;
 
-__global__ void __launch_bounds__(QRNG_THREADS) halton_qrng_kernel(int n, int n0, int generalized, double *res,
+// eight CTAs per SM (32 registers): each point's digit steps are one dependent chain, so
+// occupancy beats the few spilled registers (2, 3, 4, 6 CTAs per SM measured slower)
+__global__ void __launch_bounds__(QRNG_THREADS, 8) halton_qrng_kernel(int n, int n0, int generalized, double *res,
                                                                    const double *randu, const int *dvec,
                                                                    unsigned *err)
 {
@@ -115,6 +126,7 @@ __global__ void __launch_bounds__(QRNG_THREADS) halton_qrng_kernel(int n, int n0
     }
     __syncthreads();
     const FastDiv32 fb = fastdiv32_make((u32)b);
+    const qstep::Div qd = qstep::make_div((u32)b);
     const u32 f = (u32)f_s;
     double *out = res + (u64)j * (u64)n;
     for (u64 q = (u64)blockIdx.x * QRNG_THREADS + threadIdx.x; q < (u64)n; q += (u64)gridDim.x * QRNG_THREADS) {
@@ -122,14 +134,16 @@ __global__ void __launch_bounds__(QRNG_THREADS) halton_qrng_kernel(int n, int n0
         int m = 0;  // base-b digit count of t (at most 32)
         while (m < 32 && pwv[m + 1] <= (u64)t && pwv[m + 1] < (1ull << 32)) m++;
         if (t) m++;
-        double v = P[m];
+        u64 v = (u64)__double_as_longlong(P[m]);
         for (int k = m - 1; k >= 0; k--) {
             const u32 top = k ? fd_div(pw[k], t) : t;       // t / b^k
             const u32 dig = top - fd_div(fb, top) * (u32)b;  // its lowest digit: digit k of t
             const u32 c = fd_mod(fb, f * dig + s[k]);       // halton_qrng.c:135
-            v = __ddiv_rn(__dadd_rn(v, (double)c), bd);    // halton_qrng.c:135-136
+            u64 o;                                          // halton_qrng.c:135-136: v = RN(RN(v + c) / b)
+            if (!qstep::step(v, c, qd, o)) o = qrng_step_hw(v, c, bd);
+            v = o;
         }
-        out[q] = v;
+        out[q] = __longlong_as_double((long long)v);
     }
 }
 

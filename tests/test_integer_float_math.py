@@ -6,7 +6,9 @@ the host with g++ and checked against the host's IEEE arithmetic:
   (recip_0 = 1/b, recip_{t+1} = recip_t/b, terms RN(recip_t * digit)) over
   random bases and digits;
 * fpconv.cuh -- FP64 <-> FP32 conversions with round to nearest even
-  (tensor-core transforms).
+  (tensor-core transforms);
+* qrng_step.cuh -- one Horner step of halton_qrng, RN(RN(v + c) / b), over
+  random operands, ties and whole 32-step chains.
 """
 import os
 import shutil
@@ -47,5 +49,17 @@ def test_digit_sum_matches_ieee(digit_sum_checker, seed):
 @pytest.mark.parametrize("seed", [1, 2])
 def test_fp64_fp32_conversions_match_hardware(fpconv_checker, seed):
     out = subprocess.run([fpconv_checker, "5000000", str(seed)], capture_output=True, text=True, timeout=120)
+    assert out.returncode == 0, out.stdout + out.stderr
+    assert out.stdout.startswith("ok")
+
+
+@pytest.fixture(scope="module")
+def qrng_step_checker(tmp_path_factory):
+    return _compile(tmp_path_factory, "qrng_step_check.cpp")
+
+
+@pytest.mark.parametrize("seed", [1, 2])
+def test_qrng_step_matches_ieee(qrng_step_checker, seed):
+    out = subprocess.run([qrng_step_checker, "3000000", str(seed)], capture_output=True, text=True, timeout=120)
     assert out.returncode == 0, out.stdout + out.stderr
     assert out.stdout.startswith("ok")
