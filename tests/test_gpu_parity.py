@@ -359,3 +359,49 @@ def test_device_tensors_in_place_no_copies():
     _tp, tc = q.lat_gen_gray(U(r), U(n), U(d), U(0), gt, xt, wait=False)
     assert tc == -1
     torch.cuda.synchronize()
+
+
+# the extents that bound the output loops (n_half = 0 and a zero alpha-dimension count are
+# undefined in the reference: log2(0), a division by zero)
+_EXTENTS = ("r", "n", "d", "d1", "d2")
+
+
+def _zero_extent_cases():
+    """(case id, extent) for the first golden case of every function and each extent it has."""
+    seen, out = set(), []
+    for cid in _golden.case_ids():
+        case = cases[cid]
+        if case["name"] in seen:
+            continue
+        seen.add(case["name"])
+        for ext in _EXTENTS:
+            if ext in case["scalars"]:
+                out.append((cid, ext))
+    return out
+
+
+@pytest.mark.parametrize("cid,ext", _zero_extent_cases(), ids=lambda v: str(v))
+def test_zero_extent_writes_nothing(cid, ext):
+    """An extent of 0 (the reference's loops do not run): the outputs keep every bit of
+    their previous contents on the GPU as in the oracle, and nothing is reported."""
+    case = cases[cid]
+    names = [a for a, _k in SIGNATURES[case["name"]][0]]
+    args_g, args_o = _golden.build_args(case), _golden.build_args(case)
+    for args in (args_g, args_o):
+        args[names.index(ext)] = U(0)
+    if case["name"] in ("dnb2_interlace", "gdn_interlace") and ext == "d":
+        # the reference would read its (empty) d-dimension input outside the array: reported
+        from qmctoolscl_gb300._ffi import QmcError
+        with pytest.raises(QmcError, match="outside its array"):
+            run_gpu(case["name"], args_g)
+        return
+    before = {o: np.array(args_g[names.index(o)], copy=True) for o in case["outputs"]}
+    run_gpu(case["name"], args_g)
+    oracle.call(case["name"], *args_o)
+    for o in case["outputs"]:
+        got, orc = args_g[names.index(o)], args_o[names.index(o)]
+        if o in _golden.TWIDDLES:  # written at any vector count, to 1e-15 as in the golden cases
+            assert np.allclose(got, orc, rtol=0, atol=1e-15), o
+            continue
+        assert same_bits(got, orc), (o, "differs from the oracle")
+        assert same_bits(got, before[o]), (o, "written at a zero extent")
