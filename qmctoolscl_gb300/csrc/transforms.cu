@@ -8,7 +8,9 @@
 // frequency: stage k pairs at distance 2^s, s = m-k-1, twiddle
 // tw[(i1 mod 2^s) * 2^k] with the opposite sign), fwht_1d_radix2.c:3-53.
 // Every stage of the reference divides by sqrt(2); here the stages are
-// unscaled and the last pass multiplies by 2^(-m/2) once.  The results agree
+// unscaled, run two at a time as radix-4 steps (three complex twiddle
+// products per four values instead of four, half the shared-memory round
+// trips), and the last pass multiplies by 2^(-m/2) once.  The results agree
 // with the reference to FP64 rounding (not bit for bit).
 //
 // Passes.  Stages whose butterflies span the index bits [k0, k1) act on
@@ -82,10 +84,111 @@ __global__ void __launch_bounds__(FT_THREADS) ft_pass_kernel(PassArgs a)
         }
         __syncthreads();
         const u32 nb = tile_elems / 2;
-        for (u32 st = 0; st < a.k1 - a.k0; st++) {
-            // FFT and WHT: bits k0..k1-1 ascending; inverse FFT descending
-            const u32 bit = (KIND == FT_IFFT) ? (a.k1 - 1 - st) : (a.k0 + st);
-            const u32 hb = bit - a.k0;  // bit within q
+        const u32 nbits = a.k1 - a.k0;
+        // stages in pairs (radix-4 steps), a single radix-2 stage for an odd bit count: the FFT
+        // and WHT go up from bit k0 (the odd stage last), the inverse down from k1-1 (the odd
+        // stage last as well, at bit k0)
+        for (u32 done = 0; done < nbits;) {
+            const u32 w = (nbits - done >= 2) ? 2u : 1u;
+            const u32 bit = (KIND == FT_IFFT) ? (a.k1 - done - w) : (a.k0 + done);  // lowest bit of the step
+            const u32 hb = bit - a.k0;
+            done += w;
+            if (w == 2) {
+                const u32 S = (1u << hb) * ct;  // member stride in the tile
+                // at bit 0 every twiddle is 1: the same step without the products (a separate loop,
+                // so the FP64 multiplies are skipped rather than predicated off)
+                if (KIND != FT_FWHT && bit == 0) {
+                    for (u32 b = threadIdx.x; b < tile_elems / 4; b += FT_THREADS) {
+                        const u32 p = b / ct, cc = b % ct;
+                        const u32 e0 = (p << 2) * ct + cc, e1 = e0 + S, e2 = e1 + S, e3 = e2 + S;
+                        const double x0r = sr[e0], x0i = si[e0], x1r = sr[e1], x1i = si[e1];
+                        const double x2r = sr[e2], x2i = si[e2], x3r = sr[e3], x3i = si[e3];
+                        if (KIND == FT_FFT) {
+                            const double ar = x0r + x1r, ai = x0i + x1i, br = x0r - x1r, bi = x0i - x1i;
+                            const double cr = x2r + x3r, ci = x2i + x3i, dr = x2r - x3r, di = x2i - x3i;
+                            sr[e0] = ar + cr;
+                            si[e0] = ai + ci;
+                            sr[e2] = ar - cr;
+                            si[e2] = ai - ci;
+                            sr[e1] = br + di;
+                            si[e1] = bi - dr;
+                            sr[e3] = br - di;
+                            si[e3] = bi + dr;
+                        } else {
+                            const double ar = x0r + x2r, ai = x0i + x2i, cr = x0r - x2r, ci = x0i - x2i;
+                            const double br = x1r + x3r, bi = x1i + x3i, dr = x1r - x3r, di = x1i - x3i;
+                            sr[e0] = ar + br;
+                            si[e0] = ai + bi;
+                            sr[e1] = ar - br;
+                            si[e1] = ai - bi;
+                            sr[e2] = cr - di;
+                            si[e2] = ci + dr;
+                            sr[e3] = cr + di;
+                            si[e3] = ci - dr;
+                        }
+                    }
+                    __syncthreads();
+                    continue;
+                }
+                for (u32 b = threadIdx.x; b < tile_elems / 4; b += FT_THREADS) {
+                    const u32 p = b / ct, cc = b % ct;
+                    const u32 q0 = ((p >> hb) << (hb + 2)) | (p & ((1u << hb) - 1));
+                    const u32 e0 = q0 * ct + cc, e1 = e0 + S, e2 = e1 + S, e3 = e2 + S;
+                    if (KIND == FT_FWHT) {
+                        const double x0 = sr[e0], x1 = sr[e1], x2 = sr[e2], x3 = sr[e3];
+                        const double u0 = x0 + x1, u1 = x0 - x1, u2 = x2 + x3, u3 = x2 - x3;
+                        sr[e0] = u0 + u2;
+                        sr[e2] = u0 - u2;
+                        sr[e1] = u1 + u3;
+                        sr[e3] = u1 - u3;
+                        continue;
+                    }
+                    // the group's offset below bit `bit`; w = tw[c * n / 2^(bit+2)] and its powers
+                    const u64 i0 = (h << a.k1) + ((u64)q0 << a.k0) + c0 + cc;
+                    const u64 c = i0 & ((1ull << bit) - 1);
+                    const u32 sh = a.m - bit - 2;
+                    const double w1r = a.twr[c << sh], w1i = a.twi[c << sh];
+                    const double w2r = a.twr[c << (sh + 1)], w2i = a.twi[c << (sh + 1)];
+                    const double w3r = a.twr[(3 * c) << sh], w3i = a.twi[(3 * c) << sh];
+                    const double x0r = sr[e0], x0i = si[e0], x1r = sr[e1], x1i = si[e1];
+                    const double x2r = sr[e2], x2i = si[e2], x3r = sr[e3], x3i = si[e3];
+                    if (KIND == FT_FFT) {
+                        // two decimation-in-time stages: pre-twiddles w^br(p) (br: 0, 2, 1, 3) and the
+                        // 4-point DFT of the bit-reversed group
+                        const double y1r = fma(x1r, w2r, -x1i * w2i), y1i = fma(x1r, w2i, x1i * w2r);
+                        const double y2r = fma(x2r, w1r, -x2i * w1i), y2i = fma(x2r, w1i, x2i * w1r);
+                        const double y3r = fma(x3r, w3r, -x3i * w3i), y3i = fma(x3r, w3i, x3i * w3r);
+                        const double ar = x0r + y1r, ai = x0i + y1i, br = x0r - y1r, bi = x0i - y1i;
+                        const double cr = y2r + y3r, ci = y2i + y3i, dr = y2r - y3r, di = y2i - y3i;
+                        sr[e0] = ar + cr;
+                        si[e0] = ai + ci;
+                        sr[e2] = ar - cr;
+                        si[e2] = ai - ci;
+                        sr[e1] = br + di;  // (x0 - x1) - i (x2 - x3)
+                        si[e1] = bi - dr;
+                        sr[e3] = br - di;  // (x0 - x1) + i (x2 - x3)
+                        si[e3] = bi + dr;
+                    } else {
+                        // two decimation-in-frequency stages (bits bit+1, then bit): the inverse
+                        // 4-point DFT and post-twiddles v^(0, 2, 1, 3) (v = the + sign twiddle)
+                        const double ar = x0r + x2r, ai = x0i + x2i, cr = x0r - x2r, ci = x0i - x2i;
+                        const double br = x1r + x3r, bi = x1i + x3i, dr = x1r - x3r, di = x1i - x3i;
+                        sr[e0] = ar + br;
+                        si[e0] = ai + bi;
+                        const double z1r = ar - br, z1i = ai - bi;
+                        sr[e1] = fma(z1r, w2r, -z1i * w2i);
+                        si[e1] = fma(z1r, w2i, z1i * w2r);
+                        const double z2r = cr - di, z2i = ci + dr;  // (x0 - x2) + i (x1 - x3)
+                        sr[e2] = fma(z2r, w1r, -z2i * w1i);
+                        si[e2] = fma(z2r, w1i, z2i * w1r);
+                        const double z3r = cr + di, z3i = ci - dr;  // (x0 - x2) - i (x1 - x3)
+                        sr[e3] = fma(z3r, w3r, -z3i * w3i);
+                        si[e3] = fma(z3r, w3i, z3i * w3r);
+                    }
+                }
+                __syncthreads();
+                continue;
+            }
             const u32 half = 1u << hb;
             for (u32 b = threadIdx.x; b < nb; b += FT_THREADS) {
                 const u32 p = b / ct, cc = b % ct;
