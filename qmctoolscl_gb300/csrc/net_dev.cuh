@@ -84,45 +84,62 @@ __device__ __forceinline__ void build_table(u64 *T, u64 *H, const u64 *Cl, u64 m
     }
 }
 
-// Write rows [row_begin, row_end) of the tile.  Each thread owns VEC
-// adjacent columns (16-byte loads and stores for VEC = 2) and walks rows
-// ry, ry + R, ...: R rows per step, so a step of the CTA writes R consecutive
-// row segments, and a thread's high-bit term stays cached while m >> K holds.
-// Threads beyond R*groups idle (ncols need not divide the CTA).  xb_l / x_l
-// point at column j0 of the randomisation's slab (either may be null); d is
-// the row pitch.
-template <bool GRAY, int VEC>
+// Write rows [row_begin, row_end) of the tile.  Each thread owns VEC columns
+// (VEC = 2: one adjacent pair, one 16-byte load and store; VEC = 4: two pairs
+// half a row apart) and
+// walks rows ry, ry + R, ...: R rows per step, so a step of the CTA writes R
+// consecutive row segments, and a thread's high-bit term stays cached while
+// m >> K holds.  Threads beyond R*groups idle (ncols need not divide the CTA).
+// xb_l / x_l point at column j0 of the randomisation's slab (either may be
+// null); d is the row pitch.  The per-row index work (sequence index, Gray
+// code, high-bit key, store offset) is the kernel's ALU cost, so a thread
+// takes four columns where it can and uses 32-bit indices (I = u32) when
+// every index stays below 2^32.
+template <bool GRAY, int VEC, typename I>
 __device__ __forceinline__ void gen_rows_vec(const u64 *T, const u64 *H, u32 K, u32 ncols, u64 n_start, u64 d,
                                              u64 row_begin, u64 row_end, u64 *xb_l, double *x_l, int e_float)
 {
     const u32 groups = ncols / VEC;
     const u32 R = blockDim.x / groups;
     if (threadIdx.x >= R * groups) return;
-    const u32 c0 = (threadIdx.x % groups) * VEC;
+    // VEC = 4: two column pairs half a row apart (2g, 2g+1 and ncols/2 + 2g, +1), so each
+    // 16-byte store instruction of a warp covers a contiguous run of the row
+    const u32 c0 = (threadIdx.x % groups) * (VEC == 4 ? 2u : (u32)VEC);
+    const u32 chalf = VEC == 4 ? ncols / 2 : 2u;  // column offset of the second pair
     const u32 nlo = 1u << K;
-    u64 hi_key = ~0ull, hx[VEC];
+    I hi_key = ~(I)0;
+    u64 hx[VEC];
 #pragma unroll
     for (int v = 0; v < VEC; v++) hx[v] = 0;
-    for (u64 row = row_begin + threadIdx.x / groups; row < row_end; row += R) {
-        const u64 m = seq_index(GRAY, n_start, row);
-        const u64 hi = m >> K;
+    const I ns = (I)n_start;
+    const u64 row0 = row_begin + threadIdx.x / groups;
+    u64 o = row0 * d + c0;
+    const u64 ostep = (u64)R * d;
+    for (I row = (I)row0; row < (I)row_end; row += R, o += ostep) {
+        const I k = ns + row;
+        const I m = GRAY ? (k ^ (k >> 1)) : k;
+        const I hi = m >> K;
         if (hi != hi_key) {  // XOR of the high-bit columns picked by hi: changes every 2^K rows
 #pragma unroll
             for (int v = 0; v < VEC; v++) hx[v] = 0;
-            for (u64 hb = hi; hb; hb &= hb - 1) {
-                const u32 b = __ffsll((long long)hb) - 1;
+            for (I hb = hi; hb; hb &= hb - 1) {
+                const u32 b = (sizeof(I) == 4 ? __ffs((int)(u32)hb) : __ffsll((long long)hb)) - 1;
 #pragma unroll
-                for (int v = 0; v < VEC; v++) hx[v] ^= H[b * ncols + c0 + v];
+                for (int v = 0; v < VEC; v++) hx[v] ^= H[b * ncols + c0 + (v >> 1) * chalf + (v & 1)];
             }
             hi_key = hi;
         }
-        const u32 ti = (u32)(m & (nlo - 1)) * ncols + c0;
-        const u64 o = row * d + c0;
-        if (VEC == 2) {
-            const ulonglong2 t = *(const ulonglong2 *)(T + ti);
-            const u64 v0 = t.x ^ hx[0], v1 = t.y ^ hx[VEC - 1];
-            if (xb_l) __stcs((ulonglong2 *)(xb_l + o), make_ulonglong2(v0, v1));
-            if (x_l) __stcs((double2 *)(x_l + o), make_double2(to_float_bits(v0, e_float), to_float_bits(v1, e_float)));
+        const u32 ti = (u32)(m & (I)(nlo - 1)) * ncols + c0;
+        if (VEC >= 2) {
+#pragma unroll
+            for (int h = 0; h < VEC / 2; h++) {
+                const ulonglong2 t = *(const ulonglong2 *)(T + ti + h * chalf);
+                const u64 v0 = t.x ^ hx[2 * h], v1 = t.y ^ hx[2 * h + 1];
+                if (xb_l) __stcs((ulonglong2 *)(xb_l + o + h * chalf), make_ulonglong2(v0, v1));
+                if (x_l)
+                    __stcs((double2 *)(x_l + o + h * chalf),
+                           make_double2(to_float_bits(v0, e_float), to_float_bits(v1, e_float)));
+            }
         } else {
             const u64 v0 = T[ti] ^ hx[0];
             if (xb_l) __stcs(xb_l + o, v0);
@@ -131,17 +148,30 @@ __device__ __forceinline__ void gen_rows_vec(const u64 *T, const u64 *H, u32 K, 
     }
 }
 
-// VEC = 2 needs an even column count and 16-byte aligned rows (d even and
-// 16-byte aligned bases).
+template <bool GRAY, typename I>
+__device__ __forceinline__ void gen_rows_i(const u64 *T, const u64 *H, u32 K, u32 ncols, u64 n_start, u64 d,
+                                           u64 row_begin, u64 row_end, u64 *xb_l, double *x_l, int e_float)
+{
+    const bool vec2 = (ncols % 2 == 0) && (d % 2 == 0) && !(((uintptr_t)xb_l | (uintptr_t)x_l) & 15);
+    if (vec2 && ncols % 4 == 0 && d % 4 == 0)
+        gen_rows_vec<GRAY, 4, I>(T, H, K, ncols, n_start, d, row_begin, row_end, xb_l, x_l, e_float);
+    else if (vec2)
+        gen_rows_vec<GRAY, 2, I>(T, H, K, ncols, n_start, d, row_begin, row_end, xb_l, x_l, e_float);
+    else
+        gen_rows_vec<GRAY, 1, I>(T, H, K, ncols, n_start, d, row_begin, row_end, xb_l, x_l, e_float);
+}
+
+// VEC = 2 and 4 need an even row pitch and 16-byte aligned rows (d even and 16-byte aligned
+// bases); 32-bit indices when n_start + row_end stays at or below 2^31, so that neither the
+// index nor the row counter (stepped by R <= blockDim.x) can wrap.
 template <bool GRAY>
 __device__ __forceinline__ void gen_rows(const u64 *T, const u64 *H, u32 K, u32 ncols, u64 n_start, u64 d,
                                          u64 row_begin, u64 row_end, u64 *xb_l, double *x_l, int e_float)
 {
-    const bool vec2 = (ncols % 2 == 0) && (d % 2 == 0) && !(((uintptr_t)xb_l | (uintptr_t)x_l) & 15);
-    if (vec2)
-        gen_rows_vec<GRAY, 2>(T, H, K, ncols, n_start, d, row_begin, row_end, xb_l, x_l, e_float);
+    if (n_start + row_end <= (1ull << 31) && n_start + row_end >= n_start)
+        gen_rows_i<GRAY, u32>(T, H, K, ncols, n_start, d, row_begin, row_end, xb_l, x_l, e_float);
     else
-        gen_rows_vec<GRAY, 1>(T, H, K, ncols, n_start, d, row_begin, row_end, xb_l, x_l, e_float);
+        gen_rows_i<GRAY, u64>(T, H, K, ncols, n_start, d, row_begin, row_end, xb_l, x_l, e_float);
 }
 
 }  // namespace
