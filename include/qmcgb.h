@@ -42,7 +42,8 @@ enum qmc_status {
     QMC_ERR_CUDA = -3,   /* a CUDA runtime or launch error */
     QMC_ERR_DEVICE = -4  /* a kernel recorded an error in the device error word (bits: 1 an index the
                             reference would read out of its array, 2 a base below 2, 4 a tensor-core
-                            completion wait that ran out, 8 a fused generalized-net matrix entry >= 2^32) */
+                            completion wait that ran out, 8 a fused generalized-net matrix entry >= 2^32,
+                            16 a nested-uniform scrambling tree deeper than its keys allow) */
 };
 
 /* message of the last failing call on this host thread ("" if none) */
@@ -361,6 +362,34 @@ int qmc_halton_plan_destroy(qmc_halton_plan *plan);
  * overlap on the GPU race, so order them on one stream. */
 #define QMC_NOALLOC_MATRIX_WORDS 131072
 int qmc_net_gen_noalloc(const qmc_net_request *req, qmc_stream_t s);
+
+/* ---- nested uniform (Owen) scrambling of base-2 digital nets ----------------
+ * Replaces the reference's Python routine dnb2_nested_uniform_scramble
+ * (qmctoolscl/rand_funcs.py:162-253), which the reference binds only in
+ * Python (no C function exists for it); bit for bit its output and its
+ * generators' advanced states.  One generator per (replication l, dimension
+ * j), g = l*d + j, each numpy's SFC64 in six words (a, b, c, w, has_uint32,
+ * uinteger) in `states` (r*d*6 words, device, updated in place).  The
+ * reference keeps a tree per generator between calls; here a generator's
+ * history is the keys (xb << (tmax_new - tmax), tmax_new bits) and draws of
+ * every entry seen so far, phantom root entry first:
+ *   h0 = 0: fresh trees (the phantom's tmax_new-bit draw comes first);
+ *   h0 > 0: hist_keys / hist_draws hold r*d*h0 words, generator-major.
+ * keys_out / draws_out (each r*d*(max(h0,1)+n) words, or NULL) receive the
+ * history after the call, the history for the next call on the same trees.
+ * xb (r_x, n, d), xrb (r, n, d) as in the reference (xrb[l] uses xb[l % r_x]).
+ * All arrays are device memory.  `work` is a 256-byte aligned device
+ * workspace of work_bytes: generators run in chunks of as many as fit
+ * (qmc_dnb2_nus_workspace_size gives the bytes for a chunk of `generators`).
+ * Stream-ordered, allocates nothing.  QMC_ERR_DOMAIN for tmax_new > 64 (the
+ * reference asserts t <= 64); QMC_ERR_ARG for more than 2^30 - 1 entries per
+ * generator or a workspace smaller than one generator needs. */
+int qmc_dnb2_nus_workspace_size(uint64_t n, uint64_t h0, uint64_t generators, uint64_t *bytes);
+int qmc_dnb2_nested_uniform_scramble(uint64_t r, uint64_t n, uint64_t d, uint64_t r_x, uint64_t tmax,
+                                     uint64_t tmax_new, uint64_t *states, uint64_t h0, const uint64_t *hist_keys,
+                                     const uint64_t *hist_draws, const uint64_t *xb, uint64_t *xrb,
+                                     uint64_t *keys_out, uint64_t *draws_out, void *work, uint64_t work_bytes,
+                                     qmc_stream_t s);
 
 #ifdef __cplusplus
 }

@@ -116,3 +116,43 @@ def halton_qrng(n, d, n0, generalized, res, randu_d_32, dvec):
 def halton_qrng_ref(n, d, n0, generalized, res, randu_d_32, dvec):
     """The reference's own compiled halton_qrng (where oracle/_ref is built)."""
     _qrng(REF_SO, "halton_qrng")(n, d, n0, generalized, res, randu_d_32, dvec)
+
+
+_U64P = np.ctypeslib.ndpointer(ctypes.c_uint64, flags="C_CONTIGUOUS")
+
+
+def _nus_lib():
+    if not os.path.exists(ORACLE_SO):
+        build()
+    lib = ctypes.CDLL(ORACLE_SO)
+    lib.oracle_nus_forest_new.argtypes = [ctypes.c_uint64]
+    lib.oracle_nus_forest_new.restype = ctypes.c_void_p
+    lib.oracle_nus_forest_free.argtypes = [ctypes.c_void_p]
+    lib.oracle_nus_forest_free.restype = None
+    lib.oracle_dnb2_nested_uniform_scramble.argtypes = [ctypes.c_uint64] * 6 + [_U64P, ctypes.c_void_p, _U64P, _U64P]
+    lib.oracle_dnb2_nested_uniform_scramble.restype = None
+    return lib
+
+
+class NusForest:
+    """The oracle restatement of dnb2_nested_uniform_scramble
+    (qmctoolscl/rand_funcs.py:155-253): r*d scrambling trees kept between
+    calls, as the reference keeps its root nodes.  ``states`` holds six words
+    per generator (a, b, c, w, has_uint32, uinteger of numpy's SFC64) and is
+    advanced in place."""
+
+    def __init__(self, ntrees):
+        self._lib = _nus_lib()
+        self._h = self._lib.oracle_nus_forest_new(ntrees)
+
+    def scramble(self, r, n, d, r_x, tmax, tmax_new, states, xb, xrb):
+        self._lib.oracle_dnb2_nested_uniform_scramble(r, n, d, r_x, tmax, tmax_new, states, self._h,
+                                                      np.ascontiguousarray(xb, dtype=np.uint64), xrb)
+
+    def close(self):
+        if self._h:
+            self._lib.oracle_nus_forest_free(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()

@@ -623,3 +623,181 @@ ORACLE_API void oracle_halton_qrng(int n, int d, int n0, int generalized, double
         }
     }
 }
+
+/* ------------------------------------------------------------------------ */
+/* Nested uniform (Owen) scrambling of base-2 digital nets                   */
+/* ------------------------------------------------------------------------ */
+
+/* numpy's SFC64 bit generator: Chris Doty-Humphrey's published SFC64 step
+ * (state a, b, c and a counter w) and numpy's 32-bit draw, which hands out
+ * the low half of a 64-bit output and keeps the high half for the next
+ * 32-bit draw (has_uint32 / uinteger in the generator's state). */
+typedef struct {
+    u64 a, b, c, w;
+    int has;
+    u64 half;
+} sfc64_t;
+
+static u64 sfc64_next64(sfc64_t *g)
+{
+    u64 out = g->a + g->b + g->w++;
+    g->a = g->b ^ (g->b >> 11);
+    g->b = g->c + (g->c << 3);
+    g->c = ((g->c << 24) | (g->c >> 40)) + out;
+    return out;
+}
+
+static u64 sfc64_next32(sfc64_t *g)
+{
+    if (g->has) {
+        g->has = 0;
+        return g->half;
+    }
+    u64 x = sfc64_next64(g);
+    g->has = 1;
+    g->half = x >> 32;
+    return x & 0xFFFFFFFFull;
+}
+
+/* Generator.integers(0, 2**m) for 0 <= m <= 63 and random_tbit_uint64s(rng,
+ * m, 1) for m <= 64 (qmctoolscl/rand_funcs.py:4-20).  numpy draws from
+ * [0, 2^m) with Lemire's multiply-shift on a 32-bit output when 2^m - 1 fits
+ * 32 bits and on a 64-bit output otherwise; with a power-of-two range the
+ * rejection threshold is zero, so the value is the top m bits of that output
+ * and nothing is drawn for m = 0.  m = 64 (the int64 range of
+ * random_tbit_uint64s) is one raw 64-bit output. */
+static u64 sfc64_bits(sfc64_t *g, unsigned m)
+{
+    if (m == 0) return 0;
+    if (m <= 32) return sfc64_next32(g) >> (32 - m);
+    if (m == 64) return sfc64_next64(g);
+    return sfc64_next64(g) >> (64 - m);
+}
+
+/* One node of the scrambling tree (rand_funcs.py:155-160, NUSNode_dnb2): a
+ * leaf holds the trailing bits xb of the one point seen below it and the
+ * random bits for all of them; an internal node holds one random bit. */
+typedef struct {
+    u64 shift_bits, xb;
+    int64_t child[2];
+    int leaf;
+} nus_node_t;
+
+typedef struct {
+    nus_node_t *node;
+    u64 count, cap;
+    int init;
+} nus_tree_t;
+
+typedef struct {
+    u64 ntrees;
+    nus_tree_t *tree;
+} nus_forest_t;
+
+#include <stdlib.h>
+
+ORACLE_API void *oracle_nus_forest_new(u64 ntrees)
+{
+    nus_forest_t *f = (nus_forest_t *)calloc(1, sizeof(nus_forest_t));
+    f->ntrees = ntrees;
+    f->tree = (nus_tree_t *)calloc(ntrees ? ntrees : 1, sizeof(nus_tree_t));
+    return f;
+}
+
+ORACLE_API void oracle_nus_forest_free(void *h)
+{
+    nus_forest_t *f = (nus_forest_t *)h;
+    if (!f) return;
+    for (u64 k = 0; k < f->ntrees; k++) free(f->tree[k].node);
+    free(f->tree);
+    free(f);
+}
+
+static int64_t nus_new_node(nus_tree_t *t, u64 shift_bits, u64 xb, int leaf)
+{
+    if (t->count == t->cap) {
+        t->cap = t->cap ? 2 * t->cap : 64;
+        t->node = (nus_node_t *)realloc(t->node, t->cap * sizeof(nus_node_t));
+    }
+    nus_node_t *p = &t->node[t->count];
+    p->shift_bits = shift_bits;
+    p->xb = xb;
+    p->child[0] = p->child[1] = -1;
+    p->leaf = leaf;
+    return (int64_t)t->count++;
+}
+
+/* dnb2_nested_uniform_scramble (qmctoolscl/rand_funcs.py:162-253).
+ * states: r*d generator states, 6 words each (a, b, c, w, has_uint32,
+ * uinteger), advanced in place; forest: r*d trees from oracle_nus_forest_new,
+ * kept between calls as the reference keeps its root nodes.  The walk per
+ * point follows rand_funcs.py:200-251: bit t-1 of the point picks the child;
+ * an internal node adds its bit; a missing child becomes a new leaf with t-1
+ * fresh random bits; a leaf holding another point is split, its bits moving
+ * down with its point, until the two points part. */
+ORACLE_API void oracle_dnb2_nested_uniform_scramble(u64 r, u64 n, u64 d, u64 r_x, u64 tmax, u64 tmax_new,
+                                                    u64 *states, void *forest, const u64 *xb, u64 *xrb)
+{
+    nus_forest_t *f = (nus_forest_t *)forest;
+    u64 t_delta = tmax_new - tmax;
+    for (u64 l = 0; l < r; l++) {
+        u64 l_x = l % r_x;
+        for (u64 j = 0; j < d; j++) {
+            u64 *st = states + 6 * (l * d + j);
+            sfc64_t g = {st[0], st[1], st[2], st[3], (int)st[4], st[5]};
+            nus_tree_t *tr = &f->tree[l * d + j];
+            if (!tr->init) { /* rand_funcs.py:191-195 */
+                tr->count = 0;
+                nus_new_node(tr, sfc64_bits(&g, (unsigned)tmax_new), 0, 1);
+                tr->init = 1;
+            }
+            for (u64 i = 0; i < n; i++) {
+                /* numpy's uint64 << gives 0 for a count of 64 (tmax = 0) */
+                u64 xb_new = t_delta >= 64 ? 0 : xb[l_x * n * d + i * d + j] << t_delta;
+                u64 x = xb_new, shift = 0;
+                int64_t nd = 0;
+                for (u64 t = tmax_new; t > 0; t--) {
+                    u64 top = 1ull << (t - 1), mask = top - 1;
+                    int b = (int)((x >> (t - 1)) & 1u);
+                    u64 x_next = x & mask;
+                    nus_node_t *p = &tr->node[nd];
+                    if (!p->leaf) {
+                        if (p->shift_bits) shift += top;
+                        if (p->child[b] < 0) {
+                            u64 bits = sfc64_bits(&g, (unsigned)(t - 1));
+                            int64_t c = nus_new_node(tr, bits, x_next, 1);
+                            tr->node[nd].child[b] = c;
+                            shift += bits;
+                            break;
+                        }
+                        nd = p->child[b];
+                    } else if (p->xb == x) {
+                        shift += p->shift_bits;
+                        break;
+                    } else {
+                        int nb = (int)((p->xb >> (t - 1)) & 1u);
+                        u64 nxb = p->xb & mask, nbits = p->shift_bits & mask;
+                        u64 lead = (p->shift_bits >> (t - 1)) & 1u;
+                        if (lead) shift += top;
+                        int64_t moved = nus_new_node(tr, nbits, nxb, 1);
+                        p = &tr->node[nd]; /* the pool may have moved */
+                        p->child[nb] = moved;
+                        p->leaf = 0;
+                        p->shift_bits = lead;
+                        if (nb != b) {
+                            u64 bits = sfc64_bits(&g, (unsigned)(t - 1));
+                            int64_t c = nus_new_node(tr, bits, x_next, 1);
+                            tr->node[nd].child[b] = c;
+                            shift += bits;
+                            break;
+                        }
+                        nd = moved;
+                    }
+                    x = x_next;
+                }
+                xrb[l * n * d + i * d + j] = xb_new ^ shift;
+            }
+            st[0] = g.a; st[1] = g.b; st[2] = g.c; st[3] = g.w; st[4] = (u64)g.has; st[5] = g.half;
+        }
+    }
+}

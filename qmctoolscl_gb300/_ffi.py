@@ -31,6 +31,8 @@ EXTRA = {
     "qmc_tc_fwht_1d": [U64, U64, U64, PTR, PTR],
     "qmc_tc_fft_mul_ifft": [U64, U64, U64, PTR, PTR, U64, INT, ctypes.c_double, PTR, PTR, PTR],
     "qmc_halton_qrng": [INT, INT, INT, INT, PTR, PTR, PTR, PTR],
+    "qmc_dnb2_nus_workspace_size": [U64, U64, U64, PTR],
+    "qmc_dnb2_nested_uniform_scramble": [U64] * 6 + [PTR, U64, PTR, PTR, PTR, PTR, PTR, PTR, PTR, U64, PTR],
 }
 
 

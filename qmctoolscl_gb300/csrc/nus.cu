@@ -1,0 +1,582 @@
+// nus.cu -- nested uniform (Owen) scrambling of base-2 digital nets,
+// bit for bit the reference's dnb2_nested_uniform_scramble
+// (qmctoolscl/rand_funcs.py:155-253) with numpy's SFC64 generator streams.
+//
+// The reference walks one binary tree per generator (replication l,
+// dimension j), point by point, and draws random bits whenever a point opens
+// a new branch.  Its output is fixed by three facts:
+//   * the root starts as a leaf for a phantom point with key 0 holding
+//     tmax_new random bits, drawn first (rand_funcs.py:191-195);
+//   * point v then draws tmax_new - L_v - 1 bits, where L_v is the longest
+//     common prefix of v's key (xb << (tmax_new - tmax), tmax_new bits) with
+//     any earlier point's key -- nothing when v repeats an earlier key;
+//   * bit k (from the top) of a point's scramble comes from the draw of the
+//     earliest point that shares the point's first k key bits.
+// So per generator (all generators at once, in chunks that fit the caller's
+// workspace):
+//   1. keys in point order, the phantom (or the history of earlier calls)
+//      first: transposed from xb's (r_x, n, d) layout;
+//   2. stable LSD radix sort of (key, point) pairs, 8 bits per pass;
+//   3. a binary radix tree over the sorted pairs (Karras' parallel
+//      construction, keys extended by the point index so that equal keys
+//      split too);
+//   4. bottom up, each internal node's earliest point; the later of its two
+//      children's earliest points first shares a prefix of the node's
+//      length with an earlier point, which gives every L_v;
+//   5. the draws, one thread per generator in point order (the only serial
+//      step: numpy's SFC64 stream and its bounded-integer rule);
+//   6. each node's part of the scramble (its earliest point's draw over the
+//      depths the node spans) and each leaf's OR over its ancestors;
+//   7. xrb = (xb << (tmax_new - tmax)) ^ scramble, transposed back.
+#include "common.cuh"
+
+namespace {
+
+constexpr u32 NONE = 0xFFFFFFFFu;
+constexpr int NUS_THREADS = 256;
+constexpr int NUS_WARPS = NUS_THREADS / 32;
+constexpr u32 WT = 1024;  // entries per warp tile in the radix passes
+constexpr u32 KID_LEAF_L = 1u << 30, KID_LEAF_R = 1u << 31, KID_MASK = KID_LEAF_L - 1;
+constexpr u32 MAX_ENTRIES = 1u << 30;  // points + history per generator
+// Prefix lengths grow strictly from the root down and stay below T + 32 = 96,
+// so no path in the radix tree has more than 97 nodes; the upward loops stop
+// there and record bit 16 of the device error word instead of running on.
+constexpr int MAX_DEPTH = 97;
+
+struct NusDims {
+    u64 n, d, r_x, td, mask, h0, s0;
+    u32 T, N, NP, H0, NT, S;
+    int fresh;
+};
+
+// ---- 1. keys ---------------------------------------------------------------
+
+__global__ void nus_keys_kernel(NusDims m, const u64 *__restrict__ xb, const u64 *__restrict__ hist_keys,
+                                const u64 *__restrict__ hist_draws, u64 *__restrict__ key, u64 *__restrict__ draw,
+                                u64 *__restrict__ keys_out)
+{
+    __shared__ u64 tile[32][33];
+    const u32 v0 = blockIdx.x * 32, g0 = blockIdx.y * 32;
+    for (u32 k = threadIdx.y; k < 32; k += 8) {  // lanes along generators: xb's dimension axis
+        const u32 v = v0 + k, g = g0 + threadIdx.x;
+        u64 kv = 0;
+        if (v < m.N && g < m.S) {
+            const u64 s = m.s0 + g;
+            if (v < m.H0) {
+                kv = m.fresh ? 0 : hist_keys[s * m.h0 + v];
+            } else {
+                const u64 l = s / m.d, j = s - l * m.d, i = v - m.H0;
+                const u64 w = xb[((l % m.r_x) * m.n + i) * m.d + j];
+                kv = (m.td >= 64 ? 0 : w << m.td) & m.mask;
+            }
+        }
+        tile[k][threadIdx.x] = kv;
+    }
+    __syncthreads();
+    for (u32 k = threadIdx.y; k < 32; k += 8) {  // lanes along points
+        const u32 g = g0 + k, v = v0 + threadIdx.x;
+        if (g < m.S && v < m.N) {
+            const u64 kv = tile[threadIdx.x][k];
+            key[(u64)g * m.NP + v] = kv;
+            if (keys_out) keys_out[(m.s0 + g) * m.N + v] = kv;
+            if (!m.fresh && v < m.H0) draw[(u64)g * m.NP + v] = hist_draws[(m.s0 + g) * m.h0 + v];
+        }
+    }
+}
+
+// ---- 2. stable LSD radix sort, 8 bits per pass --------------------------------
+// Each warp owns a tile of WT consecutive entries of one generator.  Pass:
+// per-tile digit counts, a per-generator exclusive scan over (digit, tile),
+// then each warp scatters its tile in order (ranks among equal digits from
+// __match_any_sync), so equal digits keep their order.
+
+__global__ void __launch_bounds__(NUS_THREADS) nus_hist_kernel(NusDims m, const u64 *__restrict__ key, u32 shift,
+                                                               u32 *__restrict__ cnt)
+{
+    __shared__ u32 h[NUS_WARPS][256];
+    for (u32 k = threadIdx.x; k < NUS_WARPS * 256; k += NUS_THREADS) (&h[0][0])[k] = 0;
+    __syncthreads();
+    const u32 w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const u32 tile = blockIdx.x * NUS_WARPS + w, g = blockIdx.y;
+    if (tile >= m.NT) return;
+    const u64 *kp = key + (u64)g * m.NP;
+    const u32 beg = tile * WT, end = min(beg + WT, m.N);
+    for (u32 p = beg + lane; p < end; p += 32) atomicAdd(&h[w][(u32)(kp[p] >> shift) & 255u], 1u);
+    __syncwarp();
+    for (u32 dg = lane; dg < 256; dg += 32) cnt[((u64)g * 256 + dg) * m.NT + tile] = h[w][dg];
+}
+
+__global__ void __launch_bounds__(1024) nus_scan_kernel(NusDims m, u32 *__restrict__ cnt)
+{
+    __shared__ u32 wsum[32];
+    const u64 total = 256ull * m.NT;
+    u32 *c = cnt + (u64)blockIdx.x * total;
+    const u64 per = (total + 1023) / 1024;
+    const u64 beg = min((u64)threadIdx.x * per, total), end = min(beg + per, total);
+    u32 sum = 0;
+    for (u64 k = beg; k < end; k++) sum += c[k];
+    const u32 lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    u32 incl = sum;
+    for (int o = 1; o < 32; o <<= 1) {
+        const u32 y = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+        if (lane >= (u32)o) incl += y;
+    }
+    if (lane == 31) wsum[w] = incl;
+    __syncthreads();
+    if (w == 0) {
+        u32 x = wsum[lane];
+        for (int o = 1; o < 32; o <<= 1) {
+            const u32 y = __shfl_up_sync(0xFFFFFFFFu, x, o);
+            if (lane >= (u32)o) x += y;
+        }
+        wsum[lane] = x;
+    }
+    __syncthreads();
+    u32 run = incl - sum + (w ? wsum[w - 1] : 0u);
+    for (u64 k = beg; k < end; k++) {
+        const u32 t = c[k];
+        c[k] = run;
+        run += t;
+    }
+}
+
+__global__ void __launch_bounds__(NUS_THREADS) nus_scatter_kernel(NusDims m, const u64 *__restrict__ kin,
+                                                                  const u32 *__restrict__ vin, u32 shift,
+                                                                  const u32 *__restrict__ cnt, u64 *__restrict__ kout,
+                                                                  u32 *__restrict__ vout)
+{
+    __shared__ u32 base[NUS_WARPS][256];
+    const u32 w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const u32 tile = blockIdx.x * NUS_WARPS + w, g = blockIdx.y;
+    if (tile >= m.NT) return;  // whole warps leave; nothing below synchronises the block
+    for (u32 dg = lane; dg < 256; dg += 32) base[w][dg] = cnt[((u64)g * 256 + dg) * m.NT + tile];
+    __syncwarp();
+    const u64 off = (u64)g * m.NP;
+    const u32 beg = tile * WT, end = min(beg + WT, m.N);
+    for (u32 p0 = beg; p0 < end; p0 += 32) {
+        const u32 p = p0 + lane;
+        const bool ok = p < end;
+        const u64 k = ok ? kin[off + p] : 0;
+        const u32 v = ok ? (vin ? vin[off + p] : p) : 0;
+        const u32 dg = ok ? ((u32)(k >> shift) & 255u) : 256u + lane;  // idle lanes match nobody
+        const u32 peers = __match_any_sync(0xFFFFFFFFu, dg);
+        const u32 rank = __popc(peers & ((1u << lane) - 1u));
+        const u32 pos = ok ? base[w][dg] + rank : 0;
+        __syncwarp();
+        if (ok && rank == 0) base[w][dg] += __popc(peers);
+        __syncwarp();
+        if (ok) {
+            kout[off + pos] = k;
+            vout[off + pos] = v;
+        }
+    }
+}
+
+// ---- 3. binary radix tree (Karras, HPG 2012) ------------------------------------
+// Common prefix length of the extended keys (key, point) at sorted positions
+// i and j; -1 outside [0, N).
+
+__device__ __forceinline__ int nus_delta(const u64 *k, const u32 *v, long long i, long long j, u32 N, u32 T)
+{
+    if (j < 0 || j >= (long long)N) return -1;
+    const u64 x = k[i] ^ k[j];
+    if (x) return __clzll((long long)x) - (64 - (int)T);
+    return (int)T + __clz((int)(v[i] ^ v[j]));
+}
+
+__global__ void __launch_bounds__(NUS_THREADS) nus_tree_kernel(NusDims m, const u64 *__restrict__ key,
+                                                               const u32 *__restrict__ val, u32 *__restrict__ kid,
+                                                               unsigned char *__restrict__ dlt,
+                                                               u32 *__restrict__ pleaf, u32 *__restrict__ pint)
+{
+    const u32 i = blockIdx.x * NUS_THREADS + threadIdx.x, g = blockIdx.y;
+    if (i + 1 >= m.N) return;
+    const u64 off = (u64)g * m.NP;
+    const u64 *k = key + off;
+    const u32 *v = val + off;
+    const u32 N = m.N, T = m.T;
+    const long long li = i;
+    const int dir = nus_delta(k, v, li, li + 1, N, T) > nus_delta(k, v, li, li - 1, N, T) ? 1 : -1;
+    const int dmin = nus_delta(k, v, li, li - dir, N, T);
+    long long lmax = 2;
+    while (nus_delta(k, v, li, li + lmax * dir, N, T) > dmin) lmax <<= 1;
+    long long len = 0;
+    for (long long t = lmax >> 1; t >= 1; t >>= 1)
+        if (nus_delta(k, v, li, li + (len + t) * dir, N, T) > dmin) len += t;
+    const long long j = li + len * dir;
+    const int dnode = nus_delta(k, v, li, j, N, T);
+    long long s = 0;
+    for (long long div = 2;; div <<= 1) {
+        const long long t = (len + div - 1) / div;
+        if (nus_delta(k, v, li, li + (s + t) * dir, N, T) > dnode) s += t;
+        if (t <= 1) break;
+    }
+    const long long gamma = li + s * dir + (dir < 0 ? -1 : 0);
+    const bool lleaf = (li < j ? li : j) == gamma, rleaf = (li < j ? j : li) == gamma + 1;
+    kid[off + i] = (u32)gamma | (lleaf ? KID_LEAF_L : 0u) | (rleaf ? KID_LEAF_R : 0u);
+    dlt[off + i] = (unsigned char)dnode;
+    if (lleaf) pleaf[off + gamma] = i; else pint[off + gamma] = i;
+    if (rleaf) pleaf[off + gamma + 1] = i; else pint[off + gamma + 1] = i;
+    if (i == 0) pint[off] = NONE;
+}
+
+// ---- 4. earliest point per node, bottom up; L per point --------------------------
+// The second thread to reach a node (counted in flag) combines its two
+// children; the first stops.  Stores are fenced before the count, loads of
+// other threads' results bypass L1.
+
+__global__ void __launch_bounds__(NUS_THREADS) nus_min_kernel(NusDims m, const u32 *__restrict__ val,
+                                                              const u32 *__restrict__ kid,
+                                                              const unsigned char *__restrict__ dlt,
+                                                              const u32 *__restrict__ pleaf,
+                                                              const u32 *__restrict__ pint, u32 *flag, u32 *minv,
+                                                              unsigned char *__restrict__ Lv, unsigned int *err)
+{
+    const u32 p = blockIdx.x * NUS_THREADS + threadIdx.x, g = blockIdx.y;
+    if (p >= m.N) return;
+    const u64 off = (u64)g * m.NP;
+    u32 u = pleaf[off + p];
+    for (int hop = 0; u != NONE; hop++) {
+        if (hop >= MAX_DEPTH) {
+            atomicOr(err, 16u);
+            return;
+        }
+        __threadfence();
+        if (atomicAdd(&flag[off + u], 1u) == 0) return;
+        const u32 kd = kid[off + u], gm = kd & KID_MASK;
+        const u32 a = (kd & KID_LEAF_L) ? val[off + gm] : __ldcg(&minv[off + gm]);
+        const u32 b = (kd & KID_LEAF_R) ? val[off + gm + 1] : __ldcg(&minv[off + gm + 1]);
+        minv[off + u] = min(a, b);
+        const u32 dl = dlt[off + u];
+        Lv[off + max(a, b)] = (unsigned char)(dl >= m.T ? m.T : dl);
+        u = pint[off + u];
+    }
+}
+
+// ---- 5. the draws: numpy's SFC64 stream, one thread per generator ---------------
+
+struct Sfc64 {
+    u64 a, b, c, w, half;
+    u32 has;
+
+    __device__ __forceinline__ u64 next64()
+    {
+        const u64 out = a + b + w++;
+        a = b ^ (b >> 11);
+        b = c + (c << 3);
+        c = ((c << 24) | (c >> 40)) + out;
+        return out;
+    }
+    __device__ __forceinline__ u64 next32()
+    {
+        if (has) {
+            has = 0;
+            return half;
+        }
+        const u64 x = next64();
+        has = 1;
+        half = x >> 32;
+        return x & 0xFFFFFFFFull;
+    }
+    // Generator.integers(0, 2**bits) (bits <= 63) and random_tbit_uint64s(rng,
+    // bits, 1) (bits <= 64): with a power-of-two range numpy's Lemire rule
+    // never rejects, so the value is the top bits of one 32-bit output (range
+    // up to 2^32) or one 64-bit output; no draw for bits = 0
+    __device__ __forceinline__ u64 bits(u32 nb)
+    {
+        if (nb == 0) return 0;
+        if (nb <= 32) return next32() >> (32 - nb);
+        const u64 x = next64();
+        return nb == 64 ? x : x >> (64 - nb);
+    }
+};
+
+// L_v comes in 16 at a time (one 16-byte load per group, rows start 16-byte
+// aligned), three groups ahead of the draws, so the loop waits only on the
+// generator's own dependency chain.
+constexpr int DRAW_AHEAD = 4;
+
+__global__ void __launch_bounds__(32) nus_draw_kernel(NusDims m, u64 *__restrict__ states,
+                                                      const unsigned char *__restrict__ Lv, u64 *__restrict__ draw)
+{
+    const u32 g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= m.S) return;
+    u64 *st = states + (m.s0 + g) * 6;
+    Sfc64 r{st[0], st[1], st[2], st[3], st[5], (u32)(st[4] != 0)};
+    const u64 off = (u64)g * m.NP;
+    const int T = (int)m.T;
+    u64 *D = draw + off;
+    if (m.fresh) D[0] = r.bits((u32)T);
+    const uint4 *L4 = reinterpret_cast<const uint4 *>(Lv + off);
+    const u32 gend = (m.N + 15) >> 4;  // groups covering [0, N); NP keeps the last one in the row
+    u32 gq = m.H0 >> 4;
+    uint4 ring[DRAW_AHEAD];
+#pragma unroll
+    for (int k = 0; k < DRAW_AHEAD; k++) ring[k] = gq + k < gend ? L4[gq + k] : make_uint4(0, 0, 0, 0);
+    for (; gq < gend; gq++) {
+        const uint4 cur = ring[0];
+#pragma unroll
+        for (int k = 0; k < DRAW_AHEAD - 1; k++) ring[k] = ring[k + 1];
+        ring[DRAW_AHEAD - 1] = gq + DRAW_AHEAD < gend ? L4[gq + DRAW_AHEAD] : make_uint4(0, 0, 0, 0);
+        const u32 words[4] = {cur.x, cur.y, cur.z, cur.w};
+        const u32 v0 = gq << 4;
+#pragma unroll
+        for (int e = 0; e < 16; e++) {
+            const u32 v = v0 + e;
+            if (v >= m.H0 && v < m.N) {
+                const int L = (int)((words[e >> 2] >> (8 * (e & 3))) & 255u);
+                D[v] = r.bits(L >= T - 1 ? 0u : (u32)(T - 1 - L));
+            }
+        }
+    }
+    st[0] = r.a;
+    st[1] = r.b;
+    st[2] = r.c;
+    st[3] = r.w;
+    st[4] = r.has;
+    st[5] = r.half;  // numpy keeps the last buffered half here, used or not
+}
+
+// ---- 6. scramble bits: each node's band, each leaf's ancestors -----------------
+// A node spans the depths (parent's prefix length, own prefix length]; its
+// bits there come from its earliest point's draw.  Depth k is bit T-1-k.
+
+__device__ __forceinline__ u64 band_mask(int kmin, int kmax, int T)
+{
+    if (kmax > T - 1) kmax = T - 1;
+    if (kmin > kmax) return 0;
+    const u32 lo = (u32)(T - 1 - kmax), hi = (u32)(T - 1 - kmin);
+    const u64 upto_hi = hi >= 63 ? ~0ull : ((2ull << hi) - 1ull);
+    return upto_hi & ~((1ull << lo) - 1ull);
+}
+
+__global__ void __launch_bounds__(NUS_THREADS) nus_contrib_kernel(NusDims m, const unsigned char *__restrict__ dlt,
+                                                                  const u32 *__restrict__ pint,
+                                                                  const u32 *__restrict__ minv,
+                                                                  const u64 *__restrict__ draw,
+                                                                  u64 *__restrict__ contrib)
+{
+    const u32 u = blockIdx.x * NUS_THREADS + threadIdx.x, g = blockIdx.y;
+    if (u + 1 >= m.N) return;
+    const u64 off = (u64)g * m.NP;
+    const u32 P = pint[off + u];
+    const int dP = P == NONE ? -1 : (int)dlt[off + P];
+    const u64 mask = band_mask(dP + 1, (int)dlt[off + u], (int)m.T);
+    contrib[off + u] = mask ? (draw[off + minv[off + u]] & mask) : 0;
+}
+
+__global__ void __launch_bounds__(NUS_THREADS) nus_walk_kernel(NusDims m, const u32 *__restrict__ val,
+                                                               const unsigned char *__restrict__ dlt,
+                                                               const u32 *__restrict__ pleaf,
+                                                               const u32 *__restrict__ pint,
+                                                               const u64 *__restrict__ contrib,
+                                                               const u64 *__restrict__ draw, u64 *__restrict__ shv,
+                                                               unsigned int *err)
+{
+    const u32 p = blockIdx.x * NUS_THREADS + threadIdx.x, g = blockIdx.y;
+    if (p >= m.N) return;
+    const u64 off = (u64)g * m.NP;
+    const u32 v = val[off + p];
+    if (v < m.H0) return;  // the phantom and earlier calls' points are not output
+    const u32 P = pleaf[off + p];
+    const int dP = P == NONE ? -1 : (int)dlt[off + P];
+    u64 sh = draw[off + v] & band_mask(dP + 1, (int)m.T - 1, (int)m.T);
+    int hop = 0;
+    for (u32 u = P; u != NONE; u = pint[off + u]) {
+        if (++hop > MAX_DEPTH) {
+            atomicOr(err, 16u);
+            break;
+        }
+        sh |= contrib[off + u];
+    }
+    shv[off + v] = sh;
+}
+
+// ---- 7. output, transposed back to (r, n, d) --------------------------------------
+
+__global__ void nus_out_kernel(NusDims m, const u64 *__restrict__ xb, const u64 *__restrict__ shv,
+                               u64 *__restrict__ xrb)
+{
+    __shared__ u64 tile[32][33];
+    const u32 i0 = blockIdx.x * 32, g0 = blockIdx.y * 32;
+    for (u32 k = threadIdx.y; k < 32; k += 8) {  // lanes along points
+        const u32 g = g0 + k, i = i0 + threadIdx.x;
+        tile[k][threadIdx.x] = (g < m.S && i < m.n) ? shv[(u64)g * m.NP + m.H0 + i] : 0;
+    }
+    __syncthreads();
+    for (u32 k = threadIdx.y; k < 32; k += 8) {  // lanes along generators
+        const u32 g = g0 + threadIdx.x, i = i0 + k;
+        if (g < m.S && i < m.n) {
+            const u64 s = m.s0 + g, l = s / m.d, j = s - l * m.d;
+            const u64 w = xb[((l % m.r_x) * m.n + i) * m.d + j];
+            xrb[(l * m.n + i) * m.d + j] = (m.td >= 64 ? 0 : w << m.td) ^ tile[threadIdx.x][k];
+        }
+    }
+}
+
+// ---- workspace -------------------------------------------------------------------
+
+inline u64 al256(u64 b) { return (b + 255) & ~255ull; }
+
+struct NusWork {
+    u64 *keyA, *keyB, *draw, *shv;
+    u32 *valA, *valB, *cnt, *pleaf, *pint, *kid, *flag;
+    unsigned char *dlt, *Lv;
+    u64 bytes;
+};
+
+// sub-arrays for `count` generators of N entries (stride NP), 256-byte aligned
+NusWork nus_layout(char *base, u64 count, u64 NP, u64 NT)
+{
+    NusWork w{};
+    u64 off = 0;
+    auto take = [&](u64 bytes) {
+        char *p = base ? base + off : nullptr;
+        off += al256(bytes);
+        return p;
+    };
+    const u64 e = count * NP;
+    w.keyA = (u64 *)take(e * 8);
+    w.keyB = (u64 *)take(e * 8);
+    w.draw = (u64 *)take(e * 8);
+    w.shv = (u64 *)take(e * 8);
+    w.valA = (u32 *)take(e * 4);
+    w.valB = (u32 *)take(e * 4);
+    w.pleaf = (u32 *)take(e * 4);
+    w.pint = (u32 *)take(e * 4);
+    w.kid = (u32 *)take(e * 4);
+    w.flag = (u32 *)take(e * 4);
+    w.cnt = (u32 *)take(count * 256 * NT * 4);
+    w.dlt = (unsigned char *)take(e);
+    w.Lv = (unsigned char *)take(e);
+    w.bytes = off;
+    return w;
+}
+
+u64 entries_of(u64 n, u64 h0) { return (h0 ? h0 : 1) + n; }
+u64 padded(u64 N) { return (N + 15) & ~15ull; }
+u64 tiles_of(u64 N) { return (N + WT - 1) / WT; }
+
+}  // namespace
+
+extern "C" {
+
+int qmc_dnb2_nus_workspace_size(uint64_t n, uint64_t h0, uint64_t generators, uint64_t *bytes)
+{
+    QMC_REQUIRE(bytes, "dnb2_nus_workspace_size: null output pointer");
+    const u64 N = entries_of(n, h0);
+    QMC_REQUIRE(N < MAX_ENTRIES, "dnb2_nested_uniform_scramble: %llu points and earlier entries per generator "
+                "(at most 2^30 - 1)", (unsigned long long)N);
+    *bytes = nus_layout(nullptr, generators ? generators : 1, padded(N), tiles_of(N)).bytes;
+    return QMC_OK;
+}
+
+int qmc_dnb2_nested_uniform_scramble(uint64_t r, uint64_t n, uint64_t d, uint64_t r_x, uint64_t tmax,
+                                     uint64_t tmax_new, uint64_t *states, uint64_t h0, const uint64_t *hist_keys,
+                                     const uint64_t *hist_draws, const uint64_t *xb, uint64_t *xrb,
+                                     uint64_t *keys_out, uint64_t *draws_out, void *work, uint64_t work_bytes,
+                                     qmc_stream_t s)
+{
+    if (r == 0 || d == 0) return QMC_OK;
+    QMC_REQUIRE_DOMAIN(tmax_new <= 64, "dnb2_nested_uniform_scramble: tmax_new = %llu (t must be between 0 and 64)",
+                       (unsigned long long)tmax_new);
+    QMC_REQUIRE(r_x >= 1, "dnb2_nested_uniform_scramble: r_x = 0");
+    QMC_REQUIRE(states && work, "dnb2_nested_uniform_scramble: null states or workspace");
+    QMC_REQUIRE(n == 0 || (xb && xrb), "dnb2_nested_uniform_scramble: null xb or xrb");
+    QMC_REQUIRE(h0 == 0 || (hist_keys && hist_draws), "dnb2_nested_uniform_scramble: null history arrays");
+    QMC_REQUIRE(((uintptr_t)work & 255) == 0, "dnb2_nested_uniform_scramble: workspace not 256-byte aligned");
+    const u64 N = entries_of(n, h0);
+    QMC_REQUIRE(N < MAX_ENTRIES, "dnb2_nested_uniform_scramble: %llu points and earlier entries per generator "
+                "(at most 2^30 - 1)", (unsigned long long)N);
+    const u64 NP = padded(N), NT = tiles_of(N), G = r * d;
+    const u64 per = nus_layout(nullptr, 1, NP, NT).bytes;
+    QMC_REQUIRE(work_bytes >= per, "dnb2_nested_uniform_scramble: workspace of %llu bytes, one generator needs %llu",
+                (unsigned long long)work_bytes, (unsigned long long)per);
+    u64 count = work_bytes / per;
+    if (count > G) count = G;
+    if (count > 65535) count = 65535;
+    while (count > 1 && nus_layout(nullptr, count, NP, NT).bytes > work_bytes) count--;
+    NusWork w = nus_layout((char *)work, count, NP, NT);
+    cudaStream_t st = QMC_STREAM(s);
+    const u64 *xb_ = (const u64 *)xb, *hk_ = (const u64 *)hist_keys, *hd_ = (const u64 *)hist_draws;
+    u64 *xrb_ = (u64 *)xrb, *ko_ = (u64 *)keys_out, *do_ = (u64 *)draws_out, *st_ = (u64 *)states;
+
+    NusDims m{};
+    m.n = n;
+    m.d = d;
+    m.r_x = r_x;
+    m.td = tmax_new - tmax;  // wraps when tmax > tmax_new: numpy shifts by >= 64 give 0
+    m.T = (u32)tmax_new;
+    m.mask = tmax_new >= 64 ? ~0ull : ((1ull << tmax_new) - 1);
+    m.h0 = h0;
+    m.fresh = h0 == 0;
+    m.N = (u32)N;
+    m.NP = (u32)NP;
+    m.H0 = (u32)(h0 ? h0 : 1);
+    m.NT = (u32)NT;
+    const u32 passes = m.T ? (m.T + 7) / 8 : 1;
+    unsigned int *err = qmcgb::device_error_ptr();
+    QMC_REQUIRE(err, "device error word unavailable");
+
+    for (u64 s0 = 0; s0 < G; s0 += count) {
+        m.s0 = s0;
+        m.S = (u32)(G - s0 < count ? G - s0 : count);
+        const u64 e = (u64)m.S * NP;
+        nus_keys_kernel<<<dim3((unsigned)((N + 31) / 32), (m.S + 31) / 32), dim3(32, 8), 0, st>>>(
+            m, xb_, hk_, hd_, w.keyA, w.draw, ko_);
+        int rc = qmcgb::launch_status("dnb2_nus keys");
+        if (rc) return rc;
+        const u32 *vfin = nullptr;
+        const u64 *kfin = nullptr;
+        u64 *kfree = nullptr;
+        u32 *vfree = nullptr;
+        if (n > 0) {
+            const u64 *kin = w.keyA;
+            const u32 *vin = nullptr;
+            for (u32 p = 0; p < passes; p++) {
+                u64 *kout = (p & 1) ? w.keyA : w.keyB;
+                u32 *vout = (p & 1) ? w.valA : w.valB;
+                const dim3 tg((unsigned)((NT + NUS_WARPS - 1) / NUS_WARPS), m.S);
+                nus_hist_kernel<<<tg, NUS_THREADS, 0, st>>>(m, kin, 8 * p, w.cnt);
+                nus_scan_kernel<<<m.S, 1024, 0, st>>>(m, w.cnt);
+                nus_scatter_kernel<<<tg, NUS_THREADS, 0, st>>>(m, kin, vin, 8 * p, w.cnt, kout, vout);
+                rc = qmcgb::launch_status("dnb2_nus sort");
+                if (rc) return rc;
+                kin = kout;
+                vin = vout;
+            }
+            kfin = kin;
+            vfin = vin;
+            kfree = (passes & 1) ? w.keyA : w.keyB;
+            vfree = (passes & 1) ? w.valA : w.valB;
+            const dim3 ng((unsigned)((N + NUS_THREADS - 1) / NUS_THREADS), m.S);
+            nus_tree_kernel<<<ng, NUS_THREADS, 0, st>>>(m, kfin, vfin, w.kid, w.dlt, w.pleaf, w.pint);
+            rc = qmcgb::cuda_status(cudaMemsetAsync(w.flag, 0, e * 4, st), "dnb2_nus flags");
+            if (rc) return rc;
+            nus_min_kernel<<<ng, NUS_THREADS, 0, st>>>(m, vfin, w.kid, w.dlt, w.pleaf, w.pint, w.flag, vfree, w.Lv, err);
+            rc = qmcgb::launch_status("dnb2_nus tree");
+            if (rc) return rc;
+        }
+        nus_draw_kernel<<<(m.S + 31) / 32, 32, 0, st>>>(m, st_, w.Lv, w.draw);
+        rc = qmcgb::launch_status("dnb2_nus draws");
+        if (rc) return rc;
+        if (draws_out) {
+            rc = qmcgb::cuda_status(cudaMemcpy2DAsync(do_ + s0 * N, N * 8, w.draw, NP * 8, N * 8, m.S,
+                                                      cudaMemcpyDeviceToDevice, st),
+                                    "dnb2_nus draws out");
+            if (rc) return rc;
+        }
+        if (n > 0) {
+            const dim3 ng((unsigned)((N + NUS_THREADS - 1) / NUS_THREADS), m.S);
+            u64 *contrib = kfree;
+            nus_contrib_kernel<<<ng, NUS_THREADS, 0, st>>>(m, w.dlt, w.pint, vfree, w.draw, contrib);
+            nus_walk_kernel<<<ng, NUS_THREADS, 0, st>>>(m, vfin, w.dlt, w.pleaf, w.pint, contrib, w.draw, w.shv, err);
+            nus_out_kernel<<<dim3((unsigned)((n + 31) / 32), (m.S + 31) / 32), dim3(32, 8), 0, st>>>(m, xb_, w.shv, xrb_);
+            rc = qmcgb::launch_status("dnb2_nus scramble");
+            if (rc) return rc;
+        }
+    }
+    return QMC_OK;
+}
+
+}  // extern "C"
