@@ -1235,8 +1235,129 @@ def run_qrng(args):
                              "cpu_seconds": t_cpu * threads}}
 
 
+def run_nus(args):
+    """Nested uniform (Owen) scrambling of base-2 net points, bit for bit the reference's
+    dnb2_nested_uniform_scramble (qmctoolscl/rand_funcs.py:162-253) with numpy SFC64
+    generators: r=64 replications x d=32 dimensions (2048 generators, fresh trees every step),
+    n=2^20 natural-order net points (m=20, 64-bit keys: tmax = tmax_new = 64), through the C ABI
+    with inputs and generator states resident on the GPU; e2e through the Python drop-in with
+    numpy arrays and numpy Generators.  Checked against the oracle on the first 4096 points of
+    five generators; the oracle over all host threads as the CPU baseline."""
+    import torch
+    import oracle
+    import qmctoolscl_gb300 as q
+    from qmctoolscl_gb300 import _ffi, nus
+    lib = _ffi.lib()
+    r, m, d = (16, 16, 32) if args.small else (64, 20, 32)
+    n, G = 1 << m, r * d
+    rng = np.random.Generator(np.random.SFC64(7))
+    C = np.zeros((1, d, m), dtype=np.uint64)
+    for j in range(d):
+        M = np.triu(rng.integers(0, 2, (m, m)), 1) + np.eye(m, dtype=np.int64)
+        for k in range(m):
+            C[0, j, k] = sum(int(M[t, k]) << (63 - t) for t in range(m))
+    dC = torch.from_numpy(C.reshape(-1).view(np.int64)).cuda()
+    xb = torch.empty(n * d, dtype=torch.int64, device="cuda")
+    q.dnb2_gen_natural(1, n, d, 0, m, dC, xb)
+    xrb = torch.empty(G * n, dtype=torch.int64, device="cuda")  # r x n x d
+    seeds = np.random.SeedSequence(7).spawn(G)
+    states0 = np.stack([nus.sfc64_state_words(np.random.Generator(np.random.SFC64(sd))) for sd in seeds])
+    st0 = torch.from_numpy(states0.reshape(-1).view(np.int64)).cuda()
+    stw = torch.empty_like(st0)
+    free, _tot = torch.cuda.mem_get_info()
+    per = nus.workspace_bytes(n, 0, 1)
+    count = max(1, min(G, min(free // 3, 64 << 30) // per))
+    wbytes = nus.workspace_bytes(n, 0, count)
+    work = torch.empty(wbytes, dtype=torch.uint8, device="cuda")
+    st = torch.cuda.current_stream()
+    h = st.cuda_stream
+
+    def step():
+        stw.copy_(st0)
+        _ffi.check(lib.qmc_dnb2_nested_uniform_scramble(r, n, d, 1, 64, 64, stw.data_ptr(), 0, None, None,
+                                                        xb.data_ptr(), xrb.data_ptr(), None, None, work.data_ptr(),
+                                                        wbytes, h), "nus")
+
+    ms = gpu_ms(step, args.steps, args.warmup, st)
+    _ffi.check(lib.qmc_device_error_check(h), "nus")
+    # parity: the first 4096 points of five generators (a point's result depends only on
+    # the points before it), against the oracle from the same initial states
+    xb_np = xb.cpu().numpy().view(np.uint64).reshape(1, n, d)
+    out = xrb.view(r, n, d)
+    nn = 4096
+    for (l, j) in ((0, 0), (0, 1), (1, 7), (r - 1, d - 1), (r // 2, d // 2)):
+        w = states0[l * d + j].copy()
+        want = np.zeros((1, nn, 1), dtype=np.uint64)
+        f = oracle.NusForest(1)
+        f.scramble(1, nn, 1, 1, 64, 64, w, np.ascontiguousarray(xb_np[:, :nn, j:j + 1]), want)
+        f.close()
+        got = out[l, :nn, j].cpu().numpy().view(np.uint64)
+        assert np.array_equal(got, want.reshape(-1)), "nested uniform scramble differs from the oracle"
+    N = n + 1
+    passes = 8
+    top = min(passes, ((N - 1).bit_length() + 4 + 7) // 8)
+    chunks = -(-G // count)
+    launches = chunks * (1 + 3 * top + 1 + 2 + 1 + 3)
+    del work
+    torch.cuda.empty_cache()
+    # e2e: the drop-in with numpy arrays (xb 1 x n x d in, xrb r x n x d out) and fresh
+    # numpy Generators / root nodes per call
+    xrb_np = np.empty((r, n, d), dtype=np.uint64)
+    e2e_steps = max(1, min(args.steps, 3))
+    times = []
+    for it in range(e2e_steps + 1):
+        gens = np.array([np.random.Generator(np.random.SFC64(sd)) for sd in seeds], dtype=object).reshape(r, d)
+        roots = np.array([q.NUSNode_dnb2() for _ in range(G)]).reshape(r, d)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        q.dnb2_nested_uniform_scramble(r, n, d, 1, 64, 64, gens, roots, xb_np, xrb_np)
+        times.append(time.perf_counter() - t0)
+        del gens, roots
+    t_e2e = float(np.mean(times[1:]))
+    assert np.array_equal(xrb_np[:2, :nn].reshape(-1), out[:2, :nn].cpu().numpy().view(np.uint64).reshape(-1))
+    del xrb_np
+    # CPU: the oracle over all host threads, whole generators (all n points) of replications 0-1
+    threads = host_threads()
+    gs = min(G, 4 * d) if not args.small else min(G, 16 * d)  # about 10 CPU-seconds
+
+    def one_gen(k):
+        l, j = divmod(k, d)
+        w = states0[k].copy()
+        o = np.zeros((1, n, 1), dtype=np.uint64)
+        f = oracle.NusForest(1)
+        f.scramble(1, n, 1, 1, 64, 64, w, np.ascontiguousarray(xb_np[:, :, j:j + 1]), o)
+        f.close()
+
+    t0 = time.perf_counter()
+    with concurrent.futures.ThreadPoolExecutor(threads) as ex:
+        list(ex.map(one_gen, range(gs)))
+    t_cpu = time.perf_counter() - t0
+    pts = G * n
+    return {"metric": METRIC, "value": pts / (ms / 1e3), "unit": "points/s", "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "u64 (keys, GF(2) bits) and the SFC64 stream",
+            "data": "synthetic: natural-order net points of random upper-unit-triangular matrices "
+                    "(np.random.SFC64(7)); generators SFC64(SeedSequence(7).spawn(r*d))",
+            "config": {"workload": "dnb2_nested_uniform_scramble, r=%d, n=2^%d, d=%d, tmax=tmax_new=64, "
+                                   "fresh trees" % (r, m, d), "r": r, "n": n, "d": d,
+                       "generators_per_chunk": int(count), "chunks": int(chunks),
+                       "l2": "%.1f GB output per step" % (8.0 * pts / 1e9)},
+            "roofline": dict(roofline(8.0 * (n * d + pts), ms), kernel="the whole pipeline",
+                             note="not an HBM-bound path: per generator one serial pass of the SFC64 stream "
+                                  "(numpy's draw order) plus a radix sort, a radix tree and a tree walk per point; "
+                                  "achieved counts only the point I/O (xb in, xrb out)"),
+            "e2e": {"value": pts / t_e2e, "unit": "points/s", "seconds_per_call": t_e2e,
+                    "h2d_bytes_per_step": int(8 * n * d + 48 * G), "d2h_bytes_per_step": int(8 * pts + 56 * G),
+                    "path": "qmctoolscl_gb300.dnb2_nested_uniform_scramble with numpy arrays and Generators"},
+            "gpu_launches": args.steps * launches,
+            "cpu_baseline": {"value": gs * n / t_cpu, "unit": "points/s", "cores": threads, "kind": "port",
+                             "sample": "%d whole generators (2^%d points each), one per thread, by the oracle "
+                                       "(C restatement of the reference's tree walk)" % (gs, m),
+                             "seconds": t_cpu}}
+
+
 WORKLOADS = {"net_plain": run_net_plain, "net_lms": run_net_lms, "fft": run_fft, "halton": run_halton,
-             "plain": run_gdn_plain, "gdn_plain": run_gdn_plain, "qrng": run_qrng}
+             "plain": run_gdn_plain, "gdn_plain": run_gdn_plain, "qrng": run_qrng, "nus": run_nus}
 
 
 def main():

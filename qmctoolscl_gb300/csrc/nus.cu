@@ -172,6 +172,54 @@ __global__ void __launch_bounds__(NUS_THREADS) nus_scatter_kernel(NusDims m, con
     }
 }
 
+// Keys that agree in the sorted top bits form runs (in point order); runs of
+// at most RUN_MAX entries are finished here by an insertion sort on the full
+// key, one thread per run.  A longer run sets *longrun and the chunk is sorted
+// again on every digit.  Threads compare only the top bits of neighbouring
+// runs, which the in-place sorts do not change.
+constexpr u32 RUN_MAX = 32;
+
+__global__ void __launch_bounds__(NUS_THREADS) nus_fixup_kernel(NusDims m, u32 lowbits, u64 *key, u32 *val,
+                                                                u32 *longrun)
+{
+    const u32 p = blockIdx.x * NUS_THREADS + threadIdx.x, g = blockIdx.y;
+    if (p >= m.N) return;
+    const u64 off = (u64)g * m.NP;
+    u64 *k = key + off;
+    u32 *v = val + off;
+    const u64 hi = k[p] >> lowbits;
+    if (p > 0 && (k[p - 1] >> lowbits) == hi) return;        // not the first of its run
+    if (p + 1 >= m.N || (k[p + 1] >> lowbits) != hi) return;  // a run of one
+    u32 e = p + 2;
+    while (e < m.N && e - p <= RUN_MAX && (k[e] >> lowbits) == hi) e++;
+    if (e - p > RUN_MAX) {
+        atomicOr(longrun, 1u);
+        return;
+    }
+    for (u32 a = p + 1; a < e; a++) {
+        const u64 x = k[a];
+        const u32 y = v[a];
+        u32 b = a;
+        while (b > p && k[b - 1] > x) {
+            k[b] = k[b - 1];
+            v[b] = v[b - 1];
+            b--;
+        }
+        k[b] = x;
+        v[b] = y;
+    }
+}
+
+// back to point order (for the full sort after a long run)
+__global__ void __launch_bounds__(NUS_THREADS) nus_unsort_kernel(NusDims m, const u64 *__restrict__ key,
+                                                                 const u32 *__restrict__ val, u64 *__restrict__ out)
+{
+    const u32 p = blockIdx.x * NUS_THREADS + threadIdx.x, g = blockIdx.y;
+    if (p >= m.N) return;
+    const u64 off = (u64)g * m.NP;
+    out[off + val[off + p]] = key[off + p];
+}
+
 // ---- 3. binary radix tree (Karras, HPG 2012) ------------------------------------
 // Common prefix length of the extended keys (key, point) at sorted positions
 // i and j; -1 outside [0, N).
@@ -187,7 +235,8 @@ __device__ __forceinline__ int nus_delta(const u64 *k, const u32 *v, long long i
 __global__ void __launch_bounds__(NUS_THREADS) nus_tree_kernel(NusDims m, const u64 *__restrict__ key,
                                                                const u32 *__restrict__ val, u32 *__restrict__ kid,
                                                                unsigned char *__restrict__ dlt,
-                                                               u32 *__restrict__ pleaf, u32 *__restrict__ pint)
+                                                               u32 *__restrict__ pleaf, u32 *__restrict__ pint,
+                                                               u32 *__restrict__ minv, unsigned char *__restrict__ Lv)
 {
     const u32 i = blockIdx.x * NUS_THREADS + threadIdx.x, g = blockIdx.y;
     if (i + 1 >= m.N) return;
@@ -218,11 +267,17 @@ __global__ void __launch_bounds__(NUS_THREADS) nus_tree_kernel(NusDims m, const 
     if (lleaf) pleaf[off + gamma] = i; else pint[off + gamma] = i;
     if (rleaf) pleaf[off + gamma + 1] = i; else pint[off + gamma + 1] = i;
     if (i == 0) pint[off] = NONE;
+    if (lleaf && rleaf) {  // both children are points: this node is finished here (see nus_min_kernel)
+        const u32 a = v[gamma], b = v[gamma + 1];
+        minv[off + i] = min(a, b);
+        Lv[off + max(a, b)] = (unsigned char)(dnode >= (int)T ? T : (u32)dnode);
+    }
 }
 
 // ---- 4. earliest point per node, bottom up; L per point --------------------------
 // The second thread to reach a node (counted in flag) combines its two
-// children; the first stops.  Stores are fenced before the count, loads of
+// children; the first stops.  Nodes with two point children were finished by
+// the tree kernel; the walk starts at their parents, from their left points.  Stores are fenced before the count, loads of
 // other threads' results bypass L1.
 
 __global__ void __launch_bounds__(NUS_THREADS) nus_min_kernel(NusDims m, const u32 *__restrict__ val,
@@ -236,6 +291,13 @@ __global__ void __launch_bounds__(NUS_THREADS) nus_min_kernel(NusDims m, const u
     if (p >= m.N) return;
     const u64 off = (u64)g * m.NP;
     u32 u = pleaf[off + p];
+    {
+        const u32 kd = kid[off + u];
+        if ((kd & KID_LEAF_L) && (kd & KID_LEAF_R)) {  // finished by the tree kernel: its left point goes on
+            if (p != (kd & KID_MASK)) return;
+            u = pint[off + u];
+        }
+    }
     for (int hop = 0; u != NONE; hop++) {
         if (hop >= MAX_DEPTH) {
             atomicOr(err, 16u);
@@ -291,9 +353,34 @@ struct Sfc64 {
     }
 };
 
-// L_v comes in 16 at a time (one 16-byte load per group, rows start 16-byte
-// aligned), three groups ahead of the draws, so the loop waits only on the
-// generator's own dependency chain.
+// One thread per generator.  L_v comes in 16 at a time (one 16-byte load per
+// group, rows start 16-byte aligned), three groups ahead of the draws.  A
+// group whose 16 draws are all 64-bit draws (33..63 bits) or all 32-bit
+// draws (1..32 bits), the usual case, runs unrolled without a branch per
+// draw; any other group (the first and last, repeated keys, mixed widths)
+// takes the general path.
+
+// the top nb bits (33 <= nb <= 63) of a 64-bit output: a right shift by 64 - nb < 32
+__device__ __forceinline__ u64 top_bits64(u64 x, u32 nb)
+{
+    const u32 sh = 64u - nb, lo = (u32)x, hi = (u32)(x >> 32);
+    return ((u64)(hi >> sh) << 32) | __funnelshift_r(lo, hi, sh);
+}
+
+__device__ __forceinline__ u32 byte_of(const u32 (&w)[4], int e) { return (w[e >> 2] >> (8 * (e & 3))) & 255u; }
+
+__device__ __forceinline__ u32 max_byte(const uint4 &c)
+{
+    const u32 m4 = __vmaxu4(__vmaxu4(c.x, c.y), __vmaxu4(c.z, c.w));
+    return max(max(m4 & 255u, (m4 >> 8) & 255u), max((m4 >> 16) & 255u, m4 >> 24));
+}
+
+__device__ __forceinline__ u32 min_byte(const uint4 &c)
+{
+    const u32 m4 = __vminu4(__vminu4(c.x, c.y), __vminu4(c.z, c.w));
+    return min(min(m4 & 255u, (m4 >> 8) & 255u), min((m4 >> 16) & 255u, m4 >> 24));
+}
+
 constexpr int DRAW_AHEAD = 4;
 
 __global__ void __launch_bounds__(32) nus_draw_kernel(NusDims m, u64 *__restrict__ states,
@@ -318,14 +405,45 @@ __global__ void __launch_bounds__(32) nus_draw_kernel(NusDims m, u64 *__restrict
 #pragma unroll
         for (int k = 0; k < DRAW_AHEAD - 1; k++) ring[k] = ring[k + 1];
         ring[DRAW_AHEAD - 1] = gq + DRAW_AHEAD < gend ? L4[gq + DRAW_AHEAD] : make_uint4(0, 0, 0, 0);
-        const u32 words[4] = {cur.x, cur.y, cur.z, cur.w};
+        const u32 w[4] = {cur.x, cur.y, cur.z, cur.w};
         const u32 v0 = gq << 4;
+        const bool inside = v0 >= m.H0 && v0 + 16 <= m.N;
+        const int lmax = (int)max_byte(cur), lmin = (int)min_byte(cur);
+        if (inside && lmax <= T - 34) {  // 16 draws of T-1-L in [33, 63] bits
 #pragma unroll
-        for (int e = 0; e < 16; e++) {
-            const u32 v = v0 + e;
-            if (v >= m.H0 && v < m.N) {
-                const int L = (int)((words[e >> 2] >> (8 * (e & 3))) & 255u);
-                D[v] = r.bits(L >= T - 1 ? 0u : (u32)(T - 1 - L));
+            for (int e = 0; e < 16; e++) D[v0 + e] = top_bits64(r.next64(), (u32)(T - 1) - byte_of(w, e));
+        } else if (inside && lmin >= T - 33 && lmax <= T - 2) {  // 16 draws of 1..32 bits
+            const u32 sh0 = 32u - ((u32)(T - 1) - byte_of(w, 0));
+            int e0 = 0;
+            if (r.has) {  // the buffered half first, then pairs, the last output's high half kept
+                D[v0] = (u32)r.half >> sh0;
+                e0 = 1;
+            }
+#pragma unroll
+            for (int e = 0; e < 16; e += 2) {
+                if (e + e0 + 1 < 16) {
+                    const u64 x = r.next64();
+                    D[v0 + e + e0] = (u32)x >> (32u - ((u32)(T - 1) - byte_of(w, e + e0)));
+                    D[v0 + e + e0 + 1] = (u32)(x >> 32) >> (32u - ((u32)(T - 1) - byte_of(w, e + e0 + 1)));
+                    r.half = x >> 32;
+                }
+            }
+            if (e0) {  // 15 draws after the buffered one: the last takes a low half
+                const u64 x = r.next64();
+                D[v0 + 15] = (u32)x >> (32u - ((u32)(T - 1) - byte_of(w, 15)));
+                r.half = x >> 32;
+                r.has = 1;
+            } else {
+                r.has = 0;
+            }
+        } else {
+#pragma unroll 1
+            for (int e = 0; e < 16; e++) {
+                const u32 v = v0 + e;
+                if (v >= m.H0 && v < m.N) {
+                    const int L = (int)byte_of(w, e);
+                    D[v] = r.bits(L >= T - 1 ? 0u : (u32)(T - 1 - L));
+                }
             }
         }
     }
@@ -420,7 +538,7 @@ inline u64 al256(u64 b) { return (b + 255) & ~255ull; }
 
 struct NusWork {
     u64 *keyA, *keyB, *draw, *shv;
-    u32 *valA, *valB, *cnt, *pleaf, *pint, *kid, *flag;
+    u32 *valA, *valB, *cnt, *pleaf, *pint, *kid, *flag, *ctl;
     unsigned char *dlt, *Lv;
     u64 bytes;
 };
@@ -449,6 +567,7 @@ NusWork nus_layout(char *base, u64 count, u64 NP, u64 NT)
     w.cnt = (u32 *)take(count * 256 * NT * 4);
     w.dlt = (unsigned char *)take(e);
     w.Lv = (unsigned char *)take(e);
+    w.ctl = (u32 *)take(256);
     w.bytes = off;
     return w;
 }
@@ -531,26 +650,59 @@ int qmc_dnb2_nested_uniform_scramble(uint64_t r, uint64_t n, uint64_t d, uint64_
         u64 *kfree = nullptr;
         u32 *vfree = nullptr;
         if (n > 0) {
+            const dim3 tg((unsigned)((NT + NUS_WARPS - 1) / NUS_WARPS), m.S);
+            auto pass = [&](const u64 *kin, const u32 *vin, u32 digit, u64 *kout, u32 *vout) {
+                nus_hist_kernel<<<tg, NUS_THREADS, 0, st>>>(m, kin, 8 * digit, w.cnt);
+                nus_scan_kernel<<<m.S, 1024, 0, st>>>(m, w.cnt);
+                nus_scatter_kernel<<<tg, NUS_THREADS, 0, st>>>(m, kin, vin, 8 * digit, w.cnt, kout, vout);
+                return qmcgb::launch_status("dnb2_nus sort");
+            };
+            // the top digits only: enough for keys that differ in their
+            // first log2(N) + 4 bits, finished by the run fixup
+            const u32 need_bits = (u32)(64 - __builtin_clzll((unsigned long long)(N - 1) | 1ull)) + 4;
+            const u32 top = passes < (need_bits + 7) / 8 ? passes : (need_bits + 7) / 8;
             const u64 *kin = w.keyA;
             const u32 *vin = nullptr;
-            for (u32 p = 0; p < passes; p++) {
-                u64 *kout = (p & 1) ? w.keyA : w.keyB;
-                u32 *vout = (p & 1) ? w.valA : w.valB;
-                const dim3 tg((unsigned)((NT + NUS_WARPS - 1) / NUS_WARPS), m.S);
-                nus_hist_kernel<<<tg, NUS_THREADS, 0, st>>>(m, kin, 8 * p, w.cnt);
-                nus_scan_kernel<<<m.S, 1024, 0, st>>>(m, w.cnt);
-                nus_scatter_kernel<<<tg, NUS_THREADS, 0, st>>>(m, kin, vin, 8 * p, w.cnt, kout, vout);
-                rc = qmcgb::launch_status("dnb2_nus sort");
+            for (u32 q = 0; q < top; q++) {
+                u64 *kout = (q & 1) ? w.keyA : w.keyB;
+                u32 *vout = (q & 1) ? w.valA : w.valB;
+                rc = pass(kin, vin, passes - top + q, kout, vout);
                 if (rc) return rc;
                 kin = kout;
                 vin = vout;
             }
-            kfin = kin;
-            vfin = vin;
-            kfree = (passes & 1) ? w.keyA : w.keyB;
-            vfree = (passes & 1) ? w.valA : w.valB;
+            u64 *kf = (top & 1) ? w.keyB : w.keyA, *ko = (top & 1) ? w.keyA : w.keyB;
+            u32 *vf = (top & 1) ? w.valB : w.valA, *vo = (top & 1) ? w.valA : w.valB;
+            if (top < passes) {
+                const dim3 ng((unsigned)((N + NUS_THREADS - 1) / NUS_THREADS), m.S);
+                rc = qmcgb::cuda_status(cudaMemsetAsync(w.ctl, 0, 4, st), "dnb2_nus run flag");
+                if (rc) return rc;
+                nus_fixup_kernel<<<ng, NUS_THREADS, 0, st>>>(m, 8 * (passes - top), kf, vf, w.ctl);
+                u32 longrun = 0;
+                rc = qmcgb::cuda_status(cudaMemcpyAsync(&longrun, w.ctl, 4, cudaMemcpyDeviceToHost, st),
+                                        "dnb2_nus run flag");
+                if (rc) return rc;
+                rc = qmcgb::cuda_status(cudaStreamSynchronize(st), "dnb2_nus run flag");
+                if (rc) return rc;
+                if (longrun) {  // every digit, from point order, ending in kf / vf
+                    nus_unsort_kernel<<<ng, NUS_THREADS, 0, st>>>(m, kf, vf, w.shv);
+                    const u64 *ki = w.shv;
+                    const u32 *vi = nullptr;
+                    for (u32 q = 0; q < passes; q++) {
+                        const bool to_f = ((passes - 1 - q) & 1) == 0;
+                        rc = pass(ki, vi, q, to_f ? kf : ko, to_f ? vf : vo);
+                        if (rc) return rc;
+                        ki = to_f ? kf : ko;
+                        vi = to_f ? vf : vo;
+                    }
+                }
+            }
+            kfin = kf;
+            vfin = vf;
+            kfree = ko;
+            vfree = vo;
             const dim3 ng((unsigned)((N + NUS_THREADS - 1) / NUS_THREADS), m.S);
-            nus_tree_kernel<<<ng, NUS_THREADS, 0, st>>>(m, kfin, vfin, w.kid, w.dlt, w.pleaf, w.pint);
+            nus_tree_kernel<<<ng, NUS_THREADS, 0, st>>>(m, kfin, vfin, w.kid, w.dlt, w.pleaf, w.pint, vfree, w.Lv);
             rc = qmcgb::cuda_status(cudaMemsetAsync(w.flag, 0, e * 4, st), "dnb2_nus flags");
             if (rc) return rc;
             nus_min_kernel<<<ng, NUS_THREADS, 0, st>>>(m, vfin, w.kid, w.dlt, w.pleaf, w.pint, w.flag, vfree, w.Lv, err);

@@ -135,7 +135,7 @@ Args:
     xrb (np.ndarray of np.uint64): array to store scrambled points of size r*n*d
 
 Keyword arguments (beyond the reference): ``workspace_bytes`` caps the
-device scratch (default: half the free device memory, at most 24 GiB);
+device scratch (default: half the free device memory, at most 48 GiB);
 generators run in chunks that fit it.  ``stream`` selects a
 torch.cuda.Stream."""
     t0_perf = time.perf_counter()
@@ -174,7 +174,7 @@ torch.cuda.Stream."""
     budget = kwargs.get("workspace_bytes")
     if budget is None:
         free, _total = torch.cuda.mem_get_info(dev)
-        budget = min(free // 2, 24 << 30)
+        budget = min(free // 2, 48 << 30)
     count = max(1, min(G, int(budget) // per))
     wbytes = workspace_bytes(n, h0, count)
     with torch.cuda.device(dev), torch.cuda.stream(stream):
