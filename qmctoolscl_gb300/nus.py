@@ -23,9 +23,12 @@ draws (one thread per generator, numpy's SFC64 stream and bounded-integer
 rule), and OR each point's bits from its ancestors' draws.
 
 Generators must be ``numpy.random.Generator(numpy.random.SFC64(...))`` (the
-reference's own family); their states are read before the call and set to
-the advanced states after it, so later draws continue exactly as after the
-reference's call.  Root nodes are ``NUSNode_dnb2`` objects of this module: a
+reference's own family), one per (l, j) pair, as the reference's documented
+use spawns them; their states are read before the call and set to the
+advanced states after it, so later draws continue exactly as after the
+reference's call.  One generator serving several pairs is refused
+(ValueError): the reference would draw its stream across those pairs in
+turn, which the per-pair parallel passes do not reproduce.  Root nodes are ``NUSNode_dnb2`` objects of this module: a
 fresh node starts a tree; a node used by an earlier call keeps that call's
 points and draws, so a later call extends the same scramble as the reference
 does with its own nodes.
@@ -160,6 +163,9 @@ torch.cuda.Stream."""
             raise ValueError("root_nodes were built with another tmax_new")
     else:
         raise ValueError("root_nodes must be all fresh or all built by earlier calls of this function")
+    if len({id(getattr(g, "bit_generator", g)) for g in gens}) != G:
+        raise ValueError("rngs must hold r*d distinct generators: the reference draws a shared generator's "
+                         "stream across the (l, j) pairs it serves, one pair after another")
     dxb, hxb = _u64_array(xb, r_x * n * d, "xb", 9)
     dxrb, hxrb = _u64_array(xrb, r * n * d, "xrb", 10)
     states = np.stack([sfc64_state_words(g) for g in gens]) if G else np.zeros((0, STATE_WORDS), np.uint64)
