@@ -17,17 +17,17 @@
 //   1. keys in point order, the phantom (or the history of earlier calls)
 //      first: transposed from xb's (r_x, n, d) layout;
 //   2. stable LSD radix sort of (key, point) pairs, 8 bits per pass;
-//   3. a binary radix tree over the sorted pairs (Karras' parallel
-//      construction, keys extended by the point index so that equal keys
-//      split too);
-//   4. bottom up, each internal node's earliest point; the later of its two
-//      children's earliest points first shares a prefix of the node's
-//      length with an earlier point, which gives every L_v;
-//   5. the draws, one thread per generator in point order (the only serial
+//   3. bottom up, in one pass, the binary radix tree over the sorted pairs
+//      (Apetrei's agglomerative construction; keys extended by the point
+//      index so that equal keys split too) and each internal node's earliest
+//      point; the later of its two children's earliest points first shares
+//      a prefix of the node's length with an earlier point, which gives
+//      every L_v;
+//   4. the draws, one thread per generator in point order (the only serial
 //      step: numpy's SFC64 stream and its bounded-integer rule);
-//   6. each node's part of the scramble (its earliest point's draw over the
+//   5. each node's part of the scramble (its earliest point's draw over the
 //      depths the node spans) and each leaf's OR over its ancestors;
-//   7. xrb = (xb << (tmax_new - tmax)) ^ scramble, transposed back.
+//   6. xrb = (xb << (tmax_new - tmax)) ^ scramble, transposed back.
 #include "common.cuh"
 
 namespace {
@@ -36,7 +36,6 @@ constexpr u32 NONE = 0xFFFFFFFFu;
 constexpr int NUS_THREADS = 256;
 constexpr int NUS_WARPS = NUS_THREADS / 32;
 constexpr u32 WT = 1024;  // entries per warp tile in the radix passes
-constexpr u32 KID_LEAF_L = 1u << 30, KID_LEAF_R = 1u << 31, KID_MASK = KID_LEAF_L - 1;
 constexpr u32 MAX_ENTRIES = 1u << 30;  // points + history per generator
 // Prefix lengths grow strictly from the root down and stay below T + 32 = 96,
 // so no path in the radix tree has more than 97 nodes; the upward loops stop
@@ -220,10 +219,22 @@ __global__ void __launch_bounds__(NUS_THREADS) nus_unsort_kernel(NusDims m, cons
     out[off + val[off + p]] = key[off + p];
 }
 
-// ---- 3. binary radix tree (Karras, HPG 2012) ------------------------------------
-// Common prefix length of the extended keys (key, point) at sorted positions
-// i and j; -1 outside [0, N).
+// ---- 3-4. binary radix tree, earliest points and L, in one bottom-up pass ----------
+// Apetrei's agglomerative construction (HPG 2014) of the binary radix tree
+// over the sorted extended keys (key, point): lam[i] is the common prefix
+// length of neighbours i and i+1, and internal node s is the split between
+// them (its prefix length is lam[s]).  One thread per leaf climbs: a node
+// covering [l, r] has parent r (it is the parent's left child) when
+// lam[r] > lam[l-1], else parent l-1.  The first child to arrive at a node
+// parks its outer range end and its subtree's earliest point in the node's
+// 64-bit slot with one atomic exchange and stops; the second takes them and
+// goes on with the merged node.  At each node the later of the two earliest
+// points first meets an earlier point at the node's prefix length: its L.
+// Two leaves that are each other's sibling are merged by the left one with
+// no atomic.
 
+// Common prefix length of the extended keys at sorted positions i and j; -1
+// outside [0, N).
 __device__ __forceinline__ int nus_delta(const u64 *k, const u32 *v, long long i, long long j, u32 N, u32 T)
 {
     if (j < 0 || j >= (long long)N) return -1;
@@ -232,90 +243,81 @@ __device__ __forceinline__ int nus_delta(const u64 *k, const u32 *v, long long i
     return (int)T + __clz((int)(v[i] ^ v[j]));
 }
 
-__global__ void __launch_bounds__(NUS_THREADS) nus_tree_kernel(NusDims m, const u64 *__restrict__ key,
-                                                               const u32 *__restrict__ val, u32 *__restrict__ kid,
-                                                               unsigned char *__restrict__ dlt,
-                                                               u32 *__restrict__ pleaf, u32 *__restrict__ pint,
-                                                               u32 *__restrict__ minv, unsigned char *__restrict__ Lv)
+__global__ void __launch_bounds__(NUS_THREADS) nus_lcp_kernel(NusDims m, const u64 *__restrict__ key,
+                                                              const u32 *__restrict__ val,
+                                                              unsigned char *__restrict__ lam)
 {
     const u32 i = blockIdx.x * NUS_THREADS + threadIdx.x, g = blockIdx.y;
     if (i + 1 >= m.N) return;
     const u64 off = (u64)g * m.NP;
-    const u64 *k = key + off;
-    const u32 *v = val + off;
-    const u32 N = m.N, T = m.T;
-    const long long li = i;
-    const int dir = nus_delta(k, v, li, li + 1, N, T) > nus_delta(k, v, li, li - 1, N, T) ? 1 : -1;
-    const int dmin = nus_delta(k, v, li, li - dir, N, T);
-    long long lmax = 2;
-    while (nus_delta(k, v, li, li + lmax * dir, N, T) > dmin) lmax <<= 1;
-    long long len = 0;
-    for (long long t = lmax >> 1; t >= 1; t >>= 1)
-        if (nus_delta(k, v, li, li + (len + t) * dir, N, T) > dmin) len += t;
-    const long long j = li + len * dir;
-    const int dnode = nus_delta(k, v, li, j, N, T);
-    long long s = 0;
-    for (long long div = 2;; div <<= 1) {
-        const long long t = (len + div - 1) / div;
-        if (nus_delta(k, v, li, li + (s + t) * dir, N, T) > dnode) s += t;
-        if (t <= 1) break;
-    }
-    const long long gamma = li + s * dir + (dir < 0 ? -1 : 0);
-    const bool lleaf = (li < j ? li : j) == gamma, rleaf = (li < j ? j : li) == gamma + 1;
-    kid[off + i] = (u32)gamma | (lleaf ? KID_LEAF_L : 0u) | (rleaf ? KID_LEAF_R : 0u);
-    dlt[off + i] = (unsigned char)dnode;
-    if (lleaf) pleaf[off + gamma] = i; else pint[off + gamma] = i;
-    if (rleaf) pleaf[off + gamma + 1] = i; else pint[off + gamma + 1] = i;
-    if (i == 0) pint[off] = NONE;
-    if (lleaf && rleaf) {  // both children are points: this node is finished here (see nus_min_kernel)
-        const u32 a = v[gamma], b = v[gamma + 1];
-        minv[off + i] = min(a, b);
-        Lv[off + max(a, b)] = (unsigned char)(dnode >= (int)T ? T : (u32)dnode);
-    }
+    lam[off + i] = (unsigned char)nus_delta(key + off, val + off, i, (long long)i + 1, m.N, m.T);
 }
 
-// ---- 4. earliest point per node, bottom up; L per point --------------------------
-// The second thread to reach a node (counted in flag) combines its two
-// children; the first stops.  Nodes with two point children were finished by
-// the tree kernel; the walk starts at their parents, from their left points.  Stores are fenced before the count, loads of
-// other threads' results bypass L1.
+constexpr u64 SLOT_EMPTY = ~0ull;  // a parked value has an earliest point below 2^30 in its low word
 
-__global__ void __launch_bounds__(NUS_THREADS) nus_min_kernel(NusDims m, const u32 *__restrict__ val,
-                                                              const u32 *__restrict__ kid,
-                                                              const unsigned char *__restrict__ dlt,
-                                                              const u32 *__restrict__ pleaf,
-                                                              const u32 *__restrict__ pint, u32 *flag, u32 *minv,
-                                                              unsigned char *__restrict__ Lv, unsigned int *err)
+__global__ void __launch_bounds__(NUS_THREADS) nus_build_kernel(NusDims m, const u32 *__restrict__ val,
+                                                                const unsigned char *__restrict__ lam,
+                                                                unsigned long long *slot, u32 *__restrict__ pleaf,
+                                                                u32 *__restrict__ pint, u32 *__restrict__ minv,
+                                                                unsigned char *__restrict__ Lv, unsigned int *err)
 {
     const u32 p = blockIdx.x * NUS_THREADS + threadIdx.x, g = blockIdx.y;
     if (p >= m.N) return;
     const u64 off = (u64)g * m.NP;
-    u32 u = pleaf[off + p];
-    {
-        const u32 kd = kid[off + u];
-        if ((kd & KID_LEAF_L) && (kd & KID_LEAF_R)) {  // finished by the tree kernel: its left point goes on
-            if (p != (kd & KID_MASK)) return;
-            u = pint[off + u];
-        }
+    const long long last = (long long)m.N - 2;  // the last split
+    auto lamv = [&](long long i) -> int { return (i < 0 || i > last) ? -1 : (int)lam[off + i]; };
+    auto settle = [&](u32 node, u32 a, u32 b) {  // node's two earliest points are a and b
+        minv[off + node] = min(a, b);
+        const u32 dl = lam[off + node];
+        Lv[off + max(a, b)] = (unsigned char)(dl >= m.T ? m.T : dl);
+    };
+    // the leaf
+    long long lo = p, hi = p;
+    bool left = lo == 0 || (hi <= last && lamv(hi) > lamv(lo - 1));
+    u32 par = (u32)(left ? hi : lo - 1);
+    pleaf[off + p] = par;
+    u32 mn = val[off + p], node;
+    if (!left && (p - 1 == 0 || lamv((long long)p - 1) > lamv((long long)p - 2))) return;  // merged by leaf p-1
+    if (left && ((long long)p == last || lamv((long long)p + 1) < lamv(p))) {  // sibling leaf p+1
+        const u32 b = val[off + p + 1];
+        settle(p, mn, b);
+        mn = min(mn, b);
+        node = p;
+        hi = (long long)p + 1;
+    } else {
+        const unsigned long long mine = ((unsigned long long)(u32)(left ? lo : hi) << 32) | mn;
+        const unsigned long long prev = atomicExch(&slot[off + par], mine);
+        if (prev == SLOT_EMPTY) return;
+        const u32 other = (u32)(prev >> 32), omn = (u32)prev;
+        if (left) hi = other; else lo = other;
+        settle(par, mn, omn);
+        mn = min(mn, omn);
+        node = par;
     }
-    for (int hop = 0; u != NONE; hop++) {
+    for (int hop = 0;; hop++) {  // the internal node `node` covers [lo, hi]
         if (hop >= MAX_DEPTH) {
             atomicOr(err, 16u);
             return;
         }
-        __threadfence();
-        if (atomicAdd(&flag[off + u], 1u) == 0) return;
-        const u32 kd = kid[off + u], gm = kd & KID_MASK;
-        const u32 a = (kd & KID_LEAF_L) ? val[off + gm] : __ldcg(&minv[off + gm]);
-        const u32 b = (kd & KID_LEAF_R) ? val[off + gm + 1] : __ldcg(&minv[off + gm + 1]);
-        minv[off + u] = min(a, b);
-        const u32 dl = dlt[off + u];
-        Lv[off + max(a, b)] = (unsigned char)(dl >= m.T ? m.T : dl);
-        u = pint[off + u];
+        if (lo == 0 && hi == last + 1) {
+            pint[off + node] = NONE;
+            return;
+        }
+        left = lo == 0 || (hi <= last && lamv(hi) > lamv(lo - 1));
+        par = (u32)(left ? hi : lo - 1);
+        pint[off + node] = par;
+        const unsigned long long mine = ((unsigned long long)(u32)(left ? lo : hi) << 32) | mn;
+        const unsigned long long prev = atomicExch(&slot[off + par], mine);
+        if (prev == SLOT_EMPTY) return;
+        const u32 other = (u32)(prev >> 32), omn = (u32)prev;
+        if (left) hi = other; else lo = other;
+        settle(par, mn, omn);
+        mn = min(mn, omn);
+        node = par;
     }
 }
 
-// ---- 5. the draws: numpy's SFC64 stream, one thread per generator ---------------
+// ---- 4. the draws: numpy's SFC64 stream, one thread per generator ---------------
 
 struct Sfc64 {
     u64 a, b, c, w, half;
@@ -455,7 +457,7 @@ __global__ void __launch_bounds__(32) nus_draw_kernel(NusDims m, u64 *__restrict
     st[5] = r.half;  // numpy keeps the last buffered half here, used or not
 }
 
-// ---- 6. scramble bits: each node's band, each leaf's ancestors -----------------
+// ---- 5. scramble bits: each node's band, each leaf's ancestors -----------------
 // A node spans the depths (parent's prefix length, own prefix length]; its
 // bits there come from its earliest point's draw.  Depth k is bit T-1-k.
 
@@ -510,7 +512,7 @@ __global__ void __launch_bounds__(NUS_THREADS) nus_walk_kernel(NusDims m, const 
     shv[off + v] = sh;
 }
 
-// ---- 7. output, transposed back to (r, n, d) --------------------------------------
+// ---- 6. output, transposed back to (r, n, d) --------------------------------------
 
 __global__ void nus_out_kernel(NusDims m, const u64 *__restrict__ xb, const u64 *__restrict__ shv,
                                u64 *__restrict__ xrb)
@@ -538,7 +540,8 @@ inline u64 al256(u64 b) { return (b + 255) & ~255ull; }
 
 struct NusWork {
     u64 *keyA, *keyB, *draw, *shv;
-    u32 *valA, *valB, *cnt, *pleaf, *pint, *kid, *flag, *ctl;
+    u32 *valA, *valB, *cnt, *pleaf, *pint, *ctl;
+    unsigned long long *slot;
     unsigned char *dlt, *Lv;
     u64 bytes;
 };
@@ -562,8 +565,7 @@ NusWork nus_layout(char *base, u64 count, u64 NP, u64 NT)
     w.valB = (u32 *)take(e * 4);
     w.pleaf = (u32 *)take(e * 4);
     w.pint = (u32 *)take(e * 4);
-    w.kid = (u32 *)take(e * 4);
-    w.flag = (u32 *)take(e * 4);
+    w.slot = (unsigned long long *)take(e * 8);
     w.cnt = (u32 *)take(count * 256 * NT * 4);
     w.dlt = (unsigned char *)take(e);
     w.Lv = (unsigned char *)take(e);
@@ -702,10 +704,10 @@ int qmc_dnb2_nested_uniform_scramble(uint64_t r, uint64_t n, uint64_t d, uint64_
             kfree = ko;
             vfree = vo;
             const dim3 ng((unsigned)((N + NUS_THREADS - 1) / NUS_THREADS), m.S);
-            nus_tree_kernel<<<ng, NUS_THREADS, 0, st>>>(m, kfin, vfin, w.kid, w.dlt, w.pleaf, w.pint, vfree, w.Lv);
-            rc = qmcgb::cuda_status(cudaMemsetAsync(w.flag, 0, e * 4, st), "dnb2_nus flags");
+            nus_lcp_kernel<<<ng, NUS_THREADS, 0, st>>>(m, kfin, vfin, w.dlt);
+            rc = qmcgb::cuda_status(cudaMemsetAsync(w.slot, 0xFF, e * 8, st), "dnb2_nus slots");
             if (rc) return rc;
-            nus_min_kernel<<<ng, NUS_THREADS, 0, st>>>(m, vfin, w.kid, w.dlt, w.pleaf, w.pint, w.flag, vfree, w.Lv, err);
+            nus_build_kernel<<<ng, NUS_THREADS, 0, st>>>(m, vfin, w.dlt, w.slot, w.pleaf, w.pint, vfree, w.Lv, err);
             rc = qmcgb::launch_status("dnb2_nus tree");
             if (rc) return rc;
         }
