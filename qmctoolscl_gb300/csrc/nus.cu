@@ -16,7 +16,9 @@
 // workspace):
 //   1. keys in point order, the phantom (or the history of earlier calls)
 //      first: transposed from xb's (r_x, n, d) layout;
-//   2. stable LSD radix sort of (key, point) pairs, 8 bits per pass;
+//   2. stable LSD radix sort of (key, point) pairs, 8 bits per pass, over
+//      the top log2(N) + 4 bits or so, each run of keys equal there finished
+//      by an insertion sort (all 8-bit digits when a run is long);
 //   3. bottom up, in one pass, the binary radix tree over the sorted pairs
 //      (Apetrei's agglomerative construction; keys extended by the point
 //      index so that equal keys split too) and each internal node's earliest
@@ -470,7 +472,7 @@ __device__ __forceinline__ u64 band_mask(int kmin, int kmax, int T)
     return upto_hi & ~((1ull << lo) - 1ull);
 }
 
-__global__ void __launch_bounds__(NUS_THREADS) nus_contrib_kernel(NusDims m, const unsigned char *__restrict__ dlt,
+__global__ void __launch_bounds__(NUS_THREADS) nus_contrib_kernel(NusDims m, const unsigned char *__restrict__ lam,
                                                                   const u32 *__restrict__ pint,
                                                                   const u32 *__restrict__ minv,
                                                                   const u64 *__restrict__ draw,
@@ -480,13 +482,13 @@ __global__ void __launch_bounds__(NUS_THREADS) nus_contrib_kernel(NusDims m, con
     if (u + 1 >= m.N) return;
     const u64 off = (u64)g * m.NP;
     const u32 P = pint[off + u];
-    const int dP = P == NONE ? -1 : (int)dlt[off + P];
-    const u64 mask = band_mask(dP + 1, (int)dlt[off + u], (int)m.T);
+    const int dP = P == NONE ? -1 : (int)lam[off + P];
+    const u64 mask = band_mask(dP + 1, (int)lam[off + u], (int)m.T);
     contrib[off + u] = mask ? (draw[off + minv[off + u]] & mask) : 0;
 }
 
 __global__ void __launch_bounds__(NUS_THREADS) nus_walk_kernel(NusDims m, const u32 *__restrict__ val,
-                                                               const unsigned char *__restrict__ dlt,
+                                                               const unsigned char *__restrict__ lam,
                                                                const u32 *__restrict__ pleaf,
                                                                const u32 *__restrict__ pint,
                                                                const u64 *__restrict__ contrib,
@@ -499,7 +501,7 @@ __global__ void __launch_bounds__(NUS_THREADS) nus_walk_kernel(NusDims m, const 
     const u32 v = val[off + p];
     if (v < m.H0) return;  // the phantom and earlier calls' points are not output
     const u32 P = pleaf[off + p];
-    const int dP = P == NONE ? -1 : (int)dlt[off + P];
+    const int dP = P == NONE ? -1 : (int)lam[off + P];
     u64 sh = draw[off + v] & band_mask(dP + 1, (int)m.T - 1, (int)m.T);
     int hop = 0;
     for (u32 u = P; u != NONE; u = pint[off + u]) {
@@ -542,7 +544,7 @@ struct NusWork {
     u64 *keyA, *keyB, *draw, *shv;
     u32 *valA, *valB, *cnt, *pleaf, *pint, *ctl;
     unsigned long long *slot;
-    unsigned char *dlt, *Lv;
+    unsigned char *lam, *Lv;
     u64 bytes;
 };
 
@@ -567,7 +569,7 @@ NusWork nus_layout(char *base, u64 count, u64 NP, u64 NT)
     w.pint = (u32 *)take(e * 4);
     w.slot = (unsigned long long *)take(e * 8);
     w.cnt = (u32 *)take(count * 256 * NT * 4);
-    w.dlt = (unsigned char *)take(e);
+    w.lam = (unsigned char *)take(e);
     w.Lv = (unsigned char *)take(e);
     w.ctl = (u32 *)take(256);
     w.bytes = off;
@@ -704,10 +706,10 @@ int qmc_dnb2_nested_uniform_scramble(uint64_t r, uint64_t n, uint64_t d, uint64_
             kfree = ko;
             vfree = vo;
             const dim3 ng((unsigned)((N + NUS_THREADS - 1) / NUS_THREADS), m.S);
-            nus_lcp_kernel<<<ng, NUS_THREADS, 0, st>>>(m, kfin, vfin, w.dlt);
+            nus_lcp_kernel<<<ng, NUS_THREADS, 0, st>>>(m, kfin, vfin, w.lam);
             rc = qmcgb::cuda_status(cudaMemsetAsync(w.slot, 0xFF, e * 8, st), "dnb2_nus slots");
             if (rc) return rc;
-            nus_build_kernel<<<ng, NUS_THREADS, 0, st>>>(m, vfin, w.dlt, w.slot, w.pleaf, w.pint, vfree, w.Lv, err);
+            nus_build_kernel<<<ng, NUS_THREADS, 0, st>>>(m, vfin, w.lam, w.slot, w.pleaf, w.pint, vfree, w.Lv, err);
             rc = qmcgb::launch_status("dnb2_nus tree");
             if (rc) return rc;
         }
@@ -723,8 +725,8 @@ int qmc_dnb2_nested_uniform_scramble(uint64_t r, uint64_t n, uint64_t d, uint64_
         if (n > 0) {
             const dim3 ng((unsigned)((N + NUS_THREADS - 1) / NUS_THREADS), m.S);
             u64 *contrib = kfree;
-            nus_contrib_kernel<<<ng, NUS_THREADS, 0, st>>>(m, w.dlt, w.pint, vfree, w.draw, contrib);
-            nus_walk_kernel<<<ng, NUS_THREADS, 0, st>>>(m, vfin, w.dlt, w.pleaf, w.pint, contrib, w.draw, w.shv, err);
+            nus_contrib_kernel<<<ng, NUS_THREADS, 0, st>>>(m, w.lam, w.pint, vfree, w.draw, contrib);
+            nus_walk_kernel<<<ng, NUS_THREADS, 0, st>>>(m, vfin, w.lam, w.pleaf, w.pint, contrib, w.draw, w.shv, err);
             nus_out_kernel<<<dim3((unsigned)((n + 31) / 32), (m.S + 31) / 32), dim3(32, 8), 0, st>>>(m, xb_, w.shv, xrb_);
             rc = qmcgb::launch_status("dnb2_nus scramble");
             if (rc) return rc;
