@@ -122,6 +122,17 @@ def main():
                       xbs=[net_points(1, 200, 2, 8, rng) << np.uint64(56)]))
     cases.append(dict(r=2, n=16, d=1, r_x=2, tmax=63, tmax_new=64, seed=11, warm=True,
                       xbs=[rnd(2, 16, 1, 63), net_points(2, 16, 1, 4, rng) << np.uint64(59)]))
+    # tmax above tmax_new: the reference's uint64 shift count wraps and numpy shifts to 0
+    cases.append(dict(r=1, n=12, d=2, r_x=1, tmax=20, tmax_new=12, seed=12, warm=True, xbs=[rnd(1, 12, 2, 20)]))
+    # no bits at all (tmax_new = 0): every point repeats the root
+    cases.append(dict(r=2, n=5, d=1, r_x=1, tmax=0, tmax_new=0, seed=13, warm=True,
+                      xbs=[np.zeros((1, 5, 1), np.uint64)]))
+    # r = 3 r_x, 32-bit keys drawn as 32-bit halves, a continuation call
+    cases.append(dict(r=6, n=40, d=2, r_x=2, tmax=32, tmax_new=32, seed=14, warm=True,
+                      xbs=[rnd(2, 40, 2, 32), rnd(2, 40, 2, 32)]))
+    # a longer net: 1024 points of 3 dimensions, 64-bit keys
+    cases.append(dict(r=1, n=1024, d=3, r_x=1, tmax=64, tmax_new=64, seed=15, warm=True,
+                      xbs=[net_points(1, 1024, 3, 10, rng) << np.uint64(54)]))
 
     out = {}
     for c, cs in enumerate(cases):
