@@ -114,6 +114,29 @@ def _u64_array(a, need, name, pos):
     return None, a
 
 
+_ATTRS = {}
+
+
+def _host_writable(arr, allowed):
+    """Address at which the kernels may write the numpy array `arr` directly, or
+    None: the device alias of pinned memory, or the array's own address where
+    the GPU reaches pageable host memory through the host's page tables (GB300
+    next to a Grace CPU).  Otherwise the result goes through a device buffer
+    and a copy."""
+    if not allowed:
+        return None
+    ptr = arr.ctypes.data
+    dev_ptr = _ffi.device_pointer_of_host(ptr)
+    if dev_ptr is not None:
+        return dev_ptr
+    if "a" not in _ATTRS:
+        _ATTRS["a"] = _ffi.device_attributes()
+    a = _ATTRS["a"]
+    if a["pageable_access"] and a["uses_host_page_tables"]:
+        return ptr
+    return None
+
+
 def workspace_bytes(n, h0, generators):
     """Device bytes the kernels need to scramble `generators` generators at once."""
     lib = _ffi.lib()
@@ -140,7 +163,9 @@ Args:
 Keyword arguments (beyond the reference): ``workspace_bytes`` caps the
 device scratch (default: half the free device memory, at most 48 GiB);
 generators run in chunks that fit it.  ``stream`` selects a
-torch.cuda.Stream."""
+torch.cuda.Stream.  ``host_writes`` (default True): a numpy ``xrb`` is
+written by the kernels directly where the GPU can reach it (pinned memory,
+or pageable memory through the host's page tables), else copied back."""
     t0_perf = time.perf_counter()
     t0_process = time.process_time()
     torch = _t()
@@ -189,8 +214,13 @@ torch.cuda.Stream."""
         if dxb is None:
             dxb = torch.from_numpy(hxb.reshape(-1)[:r_x * n * d].view(np.int64)).to(dev) if n else \
                 torch.empty(1, dtype=i64, device=dev)
-        if dxrb is None:
+        xrb_ptr = None
+        if dxrb is None and n:
+            xrb_ptr = _host_writable(hxrb, kwargs.get("host_writes", True))
+        if dxrb is None and xrb_ptr is None:
             dxrb = torch.empty(max(r * n * d, 1), dtype=i64, device=dev)
+        if xrb_ptr is None:
+            xrb_ptr = dxrb.data_ptr()
         if h0:
             hk = torch.stack([node._hist[0] for node in roots]).contiguous()
             hd = torch.stack([node._hist[1] for node in roots]).contiguous()
@@ -201,10 +231,10 @@ torch.cuda.Stream."""
         work = torch.empty(wbytes, dtype=torch.uint8, device=dev)
         rc = lib.qmc_dnb2_nested_uniform_scramble(
             r, n, d, r_x, tmax, tmax_new, dstate.data_ptr(), h0, hk.data_ptr() if h0 else None,
-            hd.data_ptr() if h0 else None, dxb.data_ptr(), dxrb.data_ptr(), keys_out.data_ptr(),
+            hd.data_ptr() if h0 else None, dxb.data_ptr(), xrb_ptr, keys_out.data_ptr(),
             draws_out.data_ptr(), work.data_ptr(), wbytes, stream.cuda_stream)
         _ffi.check(rc, "dnb2_nested_uniform_scramble")
-        if hxrb is not None and n:
+        if hxrb is not None and n and dxrb is not None:
             torch.from_numpy(hxrb.reshape(-1)[:r * n * d].view(np.int64)).copy_(dxrb[:r * n * d])
         new_states = dstate.cpu().numpy().view(np.uint64).reshape(G, STATE_WORDS)
         roots_bits = draws_out[:, 0].cpu().numpy().view(np.uint64)
