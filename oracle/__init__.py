@@ -156,3 +156,40 @@ class NusForest:
 
     def __del__(self):
         self.close()
+
+
+def _gdn_nus_lib():
+    lib = _nus_lib()
+    lib.oracle_gdn_forest_new.argtypes = [ctypes.c_uint64]
+    lib.oracle_gdn_forest_new.restype = ctypes.c_void_p
+    lib.oracle_gdn_forest_free.argtypes = [ctypes.c_void_p]
+    lib.oracle_gdn_forest_free.restype = None
+    lib.oracle_gdn_nested_uniform_scramble.argtypes = [ctypes.c_uint64] * 7 + [_U64P, ctypes.c_void_p, _U64P, _U64P,
+                                                                               _U64P]
+    lib.oracle_gdn_nested_uniform_scramble.restype = ctypes.c_int
+    return lib
+
+
+class GdnNusForest:
+    """The oracle restatement of gdn_nested_uniform_scramble
+    (qmctoolscl/rand_funcs.py:262-356): r*d base-b scrambling trees kept
+    between calls.  ``states`` as for NusForest.  ``scramble`` returns 0, or 1
+    where the reference raises IndexError (a digit at or above its base; a
+    walk that runs out of digits, which happens for tmax_new = tmax)."""
+
+    def __init__(self, ntrees):
+        self._lib = _gdn_nus_lib()
+        self._h = self._lib.oracle_gdn_forest_new(ntrees)
+
+    def scramble(self, r, n, d, r_x, r_b, tmax, tmax_new, states, bases, xdig, xrdig):
+        return self._lib.oracle_gdn_nested_uniform_scramble(
+            r, n, d, r_x, r_b, tmax, tmax_new, states, self._h, np.ascontiguousarray(bases, dtype=np.uint64),
+            np.ascontiguousarray(xdig, dtype=np.uint64), xrdig)
+
+    def close(self):
+        if self._h:
+            self._lib.oracle_gdn_forest_free(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()

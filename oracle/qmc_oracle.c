@@ -801,3 +801,220 @@ ORACLE_API void oracle_dnb2_nested_uniform_scramble(u64 r, u64 n, u64 d, u64 r_x
         }
     }
 }
+
+/* ------------------------------------------------------------------------ */
+/* Nested uniform scrambling of generalized (base-b) digital nets            */
+/* ------------------------------------------------------------------------ */
+
+/* numpy's random_interval(max): a value in [0, max] by masked rejection on
+ * 32-bit draws (64-bit ones above 2^32 - 1), as Generator.shuffle uses it */
+static u64 sfc64_interval(sfc64_t *g, u64 mx)
+{
+    if (mx == 0) return 0;
+    u64 mask = mx;
+    mask |= mask >> 1;
+    mask |= mask >> 2;
+    mask |= mask >> 4;
+    mask |= mask >> 8;
+    mask |= mask >> 16;
+    mask |= mask >> 32;
+    u64 v;
+    if (mx <= 0xFFFFFFFFull) {
+        do v = sfc64_next32(g) & mask; while (v > mx);
+    } else {
+        do v = sfc64_next64(g) & mask; while (v > mx);
+    }
+    return v;
+}
+
+/* random_uint64_permutations(rng, m, b) (rand_funcs.py:22-32): m rows, each
+ * Generator.permutation(b) -- Fisher-Yates from the top of arange(b) */
+static void sfc64_permutations(sfc64_t *g, u64 m, u64 b, u64 *out)
+{
+    for (u64 k = 0; k < m; k++) {
+        u64 *row = out + k * b;
+        for (u64 i = 0; i < b; i++) row[i] = i;
+        for (u64 i = b; i-- > 1;) {
+            u64 j = sfc64_interval(g, i), t = row[i];
+            row[i] = row[j];
+            row[j] = t;
+        }
+    }
+}
+
+/* One node of the base-b tree (rand_funcs.py:255-260, NUSNode_gdn): a leaf
+ * holds the trailing digits of the one point below it and one permutation
+ * per remaining level; an internal node holds one permutation and b
+ * children.  Leaves that split hand their rows and digits down by pointer. */
+typedef struct {
+    u64 *perm, *xdig;
+    int64_t *child;
+    int leaf;
+} gnode_t;
+
+typedef struct {
+    gnode_t *node;
+    u64 count, cap;
+    void **bufs;
+    u64 nbufs, capbufs;
+    int init;
+} gtree_t;
+
+typedef struct {
+    u64 ntrees;
+    gtree_t *tree;
+} gforest_t;
+
+ORACLE_API void *oracle_gdn_forest_new(u64 ntrees)
+{
+    gforest_t *f = (gforest_t *)calloc(1, sizeof(gforest_t));
+    f->ntrees = ntrees;
+    f->tree = (gtree_t *)calloc(ntrees ? ntrees : 1, sizeof(gtree_t));
+    return f;
+}
+
+ORACLE_API void oracle_gdn_forest_free(void *h)
+{
+    gforest_t *f = (gforest_t *)h;
+    if (!f) return;
+    for (u64 k = 0; k < f->ntrees; k++) {
+        gtree_t *t = &f->tree[k];
+        for (u64 i = 0; i < t->nbufs; i++) free(t->bufs[i]);
+        free(t->bufs);
+        free(t->node);
+    }
+    free(f->tree);
+    free(f);
+}
+
+static void *gtree_alloc(gtree_t *t, size_t bytes)
+{
+    if (t->nbufs == t->capbufs) {
+        t->capbufs = t->capbufs ? 2 * t->capbufs : 64;
+        t->bufs = (void **)realloc(t->bufs, t->capbufs * sizeof(void *));
+    }
+    void *p = malloc(bytes ? bytes : 1);
+    t->bufs[t->nbufs++] = p;
+    return p;
+}
+
+static int64_t gtree_leaf(gtree_t *t, u64 *perm, u64 *xdig)
+{
+    if (t->count == t->cap) {
+        t->cap = t->cap ? 2 * t->cap : 64;
+        t->node = (gnode_t *)realloc(t->node, t->cap * sizeof(gnode_t));
+    }
+    gnode_t *p = &t->node[t->count];
+    p->perm = perm;
+    p->xdig = xdig;
+    p->child = NULL;
+    p->leaf = 1;
+    return (int64_t)t->count++;
+}
+
+/* gdn_nested_uniform_scramble (qmctoolscl/rand_funcs.py:262-356).  states:
+ * r*d generator states as for the base-2 scramble; forest: r*d trees from
+ * oracle_gdn_forest_new, kept between calls.  xdig (r_x, n, d, tmax) digits,
+ * xrdig (r, n, d, tmax_new).  Returns 0, or 1 where the reference raises
+ * IndexError: a digit at or above its base, or a walk that runs out of
+ * digits (tmax_new = tmax and a point that repeats an earlier one down to
+ * its last digit). */
+ORACLE_API int oracle_gdn_nested_uniform_scramble(u64 r, u64 n, u64 d, u64 r_x, u64 r_b, u64 tmax, u64 tmax_new,
+                                                  u64 *states, void *forest, const u64 *bases, const u64 *xdig,
+                                                  u64 *xrdig)
+{
+    gforest_t *f = (gforest_t *)forest;
+    u64 *xd = (u64 *)malloc((tmax_new + 1) * sizeof(u64));
+    int bad = 0;
+    for (u64 l = 0; l < r && !bad; l++) {
+        u64 l_b = l % r_b, l_x = l % r_x;
+        for (u64 j = 0; j < d && !bad; j++) {
+            u64 *st = states + 6 * (l * d + j);
+            sfc64_t g = {st[0], st[1], st[2], st[3], (int)st[4], st[5]};
+            gtree_t *tr = &f->tree[l * d + j];
+            u64 b = bases[l_b * d + j];
+            if (!tr->init) { /* rand_funcs.py:318-322 */
+                tr->count = 0;
+                u64 *perm = (u64 *)gtree_alloc(tr, tmax_new * b * sizeof(u64));
+                u64 *z = (u64 *)gtree_alloc(tr, tmax_new * sizeof(u64));
+                for (u64 k = 0; k < tmax_new; k++) z[k] = 0;
+                sfc64_permutations(&g, tmax_new, b, perm);
+                gtree_leaf(tr, perm, z);
+                tr->init = 1;
+            }
+            for (u64 i = 0; i < n && !bad; i++) {
+                const u64 *x = xdig + ((l_x * n + i) * d + j) * tmax;
+                u64 *out = xrdig + ((l * n + i) * d + j) * tmax_new;
+                int64_t nd = 0;
+                for (u64 t = 0; t <= tmax; t++) {
+                    if (t >= tmax_new) { bad = 1; break; } /* _xdig[0] of an empty array */
+                    u64 len = tmax_new - t;
+                    for (u64 k = 0; k < len; k++) xd[k] = (t + k < tmax) ? x[t + k] : 0;
+                    u64 dig = xd[0];
+                    if (dig >= b) { bad = 1; break; }
+                    gnode_t *p = &tr->node[nd];
+                    if (!p->leaf) {
+                        out[t] = p->perm[dig];
+                        if (p->child[dig] < 0) {
+                            u64 m = len - 1;
+                            u64 *perm = (u64 *)gtree_alloc(tr, m * b * sizeof(u64));
+                            u64 *rest = (u64 *)gtree_alloc(tr, m * sizeof(u64));
+                            sfc64_permutations(&g, m, b, perm);
+                            for (u64 k = 0; k < m; k++) rest[k] = xd[1 + k];
+                            for (u64 k = 0; k < m; k++) {
+                                if (rest[k] >= b) { bad = 1; break; }
+                                out[t + 1 + k] = perm[k * b + rest[k]];
+                            }
+                            int64_t c = gtree_leaf(tr, perm, rest);
+                            tr->node[nd].child[dig] = c;
+                            break;
+                        }
+                        nd = p->child[dig];
+                        continue;
+                    }
+                    int same = 1;
+                    for (u64 k = 0; k < len; k++)
+                        if (p->xdig[k] != xd[k]) { same = 0; break; }
+                    if (same) {
+                        for (u64 k = 0; k < len; k++) {
+                            if (xd[k] >= b) { bad = 1; break; }
+                            out[t + k] = p->perm[k * b + xd[k]];
+                        }
+                        break;
+                    }
+                    u64 node_dig = p->xdig[0];
+                    if (node_dig >= b) { bad = 1; break; }
+                    out[t] = p->perm[dig];
+                    u64 *rows = p->perm, *digs = p->xdig;
+                    int64_t *kids = (int64_t *)gtree_alloc(tr, b * sizeof(int64_t));
+                    for (u64 k = 0; k < b; k++) kids[k] = -1;
+                    int64_t moved = gtree_leaf(tr, rows + b, digs + 1);
+                    p = &tr->node[nd]; /* the pool may have moved */
+                    p->leaf = 0;
+                    p->perm = rows; /* its first row: the permutation of this level */
+                    p->xdig = NULL;
+                    p->child = kids;
+                    kids[node_dig] = moved;
+                    if (node_dig == dig) {
+                        nd = moved;
+                        continue;
+                    }
+                    u64 m = len - 1;
+                    u64 *perm = (u64 *)gtree_alloc(tr, m * b * sizeof(u64));
+                    u64 *rest = (u64 *)gtree_alloc(tr, m * sizeof(u64));
+                    sfc64_permutations(&g, m, b, perm);
+                    for (u64 k = 0; k < m; k++) rest[k] = xd[1 + k];
+                    for (u64 k = 0; k < m; k++) {
+                        if (rest[k] >= b) { bad = 1; break; }
+                        out[t + 1 + k] = perm[k * b + rest[k]];
+                    }
+                    kids[dig] = gtree_leaf(tr, perm, rest);
+                    break;
+                }
+            }
+            st[0] = g.a; st[1] = g.b; st[2] = g.c; st[3] = g.w; st[4] = (u64)g.has; st[5] = g.half;
+        }
+    }
+    free(xd);
+    return bad;
+}
