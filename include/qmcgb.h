@@ -391,6 +391,29 @@ int qmc_dnb2_nested_uniform_scramble(uint64_t r, uint64_t n, uint64_t d, uint64_
                                      uint64_t *keys_out, uint64_t *draws_out, void *work, uint64_t work_bytes,
                                      qmc_stream_t s);
 
+/* ---- nested uniform (Owen) scrambling of generalized (base-b) nets ----------
+ * Replaces the reference's Python routine gdn_nested_uniform_scramble
+ * (qmctoolscl/rand_funcs.py:262-356): bit for bit its xrdig and its
+ * generators' advanced states, for fresh trees (one call per set of root
+ * nodes).  Generator g = l*d + j with base bases[(l % r_b)*d + j] (2..65536)
+ * and numpy's SFC64 state in six words (states, r*d*6, updated in place).
+ * xdig (r_x, n, d, tmax) digits, xrdig (r, n, d, tmax_new); needs
+ * 1 <= tmax < tmax_new <= 255 and tmax * ceil(log2 b) <= 128 (the digits are
+ * compared as 128-bit keys).  `perms` holds perm_capacity 16-bit entries for
+ * the drawn permutations of one chunk of generators; when a chunk needs more,
+ * the call returns QMC_ERR_ARG with the entries needed in *perm_needed (the
+ * largest chunk so far) before drawing for that chunk -- states of earlier
+ * chunks are then already advanced, so a caller retries from its own copy.
+ * A digit at or above its base sets bit 1 of the device error word (the
+ * reference raises IndexError).  Device memory throughout; `work` is a
+ * 256-byte aligned workspace of work_bytes (qmc_gdn_nus_workspace_size);
+ * synchronises its stream twice per chunk. */
+int qmc_gdn_nus_workspace_size(uint64_t n, uint64_t generators, uint64_t *bytes);
+int qmc_gdn_nested_uniform_scramble(uint64_t r, uint64_t n, uint64_t d, uint64_t r_x, uint64_t r_b, uint64_t tmax,
+                                    uint64_t tmax_new, uint64_t *states, const uint64_t *bases,
+                                    const uint64_t *xdig, uint64_t *xrdig, uint16_t *perms, uint64_t perm_capacity,
+                                    uint64_t *perm_needed, void *work, uint64_t work_bytes, qmc_stream_t s);
+
 #ifdef __cplusplus
 }
 #endif

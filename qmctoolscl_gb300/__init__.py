@@ -15,7 +15,7 @@ batched uneven requests in one persistent launch, CUDA-graph replay) and
 __version__ = "1.2.1"
 
 from .rand_funcs import *  # noqa: F401,F403
-from .nus import NUSNode_dnb2, dnb2_nested_uniform_scramble  # noqa: F401
+from .nus import NUSNode_dnb2, NUSNode_gdn, dnb2_nested_uniform_scramble, gdn_nested_uniform_scramble  # noqa: F401
 from .api import (  # noqa: F401
     lat_gen_linear,
     lat_gen_natural,

@@ -33,6 +33,8 @@ EXTRA = {
     "qmc_halton_qrng": [INT, INT, INT, INT, PTR, PTR, PTR, PTR],
     "qmc_dnb2_nus_workspace_size": [U64, U64, U64, PTR],
     "qmc_dnb2_nested_uniform_scramble": [U64] * 6 + [PTR, U64, PTR, PTR, PTR, PTR, PTR, PTR, PTR, U64, PTR],
+    "qmc_gdn_nus_workspace_size": [U64, U64, PTR],
+    "qmc_gdn_nested_uniform_scramble": [U64] * 7 + [PTR, PTR, PTR, PTR, PTR, U64, PTR, PTR, U64, PTR],
 }
 
 

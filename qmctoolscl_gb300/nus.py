@@ -246,3 +246,133 @@ or pageable memory through the host's page tables), else copied back."""
         node.shift_bits = np.uint64(roots_bits[k])
         node._hist = (keys_out[k], draws_out[k], tmax_new)
     return time.perf_counter() - t0_perf, time.process_time() - t0_process
+
+
+class NUSNode_gdn(object):
+    """Root of one generator's base-b scrambling tree, with the fields of the
+    reference's node (qmctoolscl/rand_funcs.py:255-260).  A fresh node (perm
+    None) starts a tree.  The GPU form scrambles fresh trees: after a call the
+    node is marked used (perm set) and holds no tree to continue."""
+
+    def __init__(self, perm=None, xdig=None, children=None):
+        self.perm = perm
+        self.xdig = xdig
+        self.children = children
+
+
+def gdn_workspace_bytes(n, generators):
+    """Device bytes the kernels need to scramble `generators` base-b generators at once."""
+    lib = _ffi.lib()
+    out = ctypes.c_uint64(0)
+    _ffi.check(lib.qmc_gdn_nus_workspace_size(n, generators, ctypes.byref(out)), "gdn_nested_uniform_scramble")
+    return out.value
+
+
+def gdn_nested_uniform_scramble(r, n, d, r_x, r_b, tmax, tmax_new, rngs, root_nodes, bases, xdig, xrdig, **kwargs):
+    """Nested uniform scramble of general digital nets
+
+Args:
+    r (np.uint64): replications
+    n (np.uint64): points
+    d (np.uint64): dimensions
+    r_x (np.uint64): replications of xb
+    r_b (np.uint64): replications of bases
+    tmax (np.uint64): maximum number digits in each point representation
+    tmax_new (np.uint64): maximum number digits in each point representation after scrambling
+    rngs (np.ndarray of numpy.random._generator.Generator): random number generators of size r*d
+    root_nodes (np.ndarray of NUSNode_gdn): root nodes of size r*d
+    bases (np.ndarray of np.uint64): array of bases of size r*d
+    xdig (np.ndarray of np.uint64): array of unrandomized points of size r*n*d*tmax
+    xrdig (np.ndarray of np.uint64): array to store scrambled points of size r*n*d*tmax_new
+
+Runs on the GPU for fresh root nodes (one call per set of nodes; a used set
+raises NotImplementedError) with bases 2..65536, tmax < tmax_new <= 255 and
+tmax * ceil(log2 b) <= 128 (ValueError otherwise).  A digit at or above its
+base raises IndexError, as the reference does.  Keyword arguments:
+``workspace_bytes`` caps the device scratch, ``stream`` selects a
+torch.cuda.Stream."""
+    t0_perf = time.perf_counter()
+    t0_process = time.process_time()
+    torch = _t()
+    r, n, d, r_x, r_b, tmax, tmax_new = (int(v) for v in (r, n, d, r_x, r_b, tmax, tmax_new))
+    G = r * d
+    gens = _objects(rngs, r, d, "rngs")
+    roots = _objects(root_nodes, r, d, "root_nodes")
+    for node in roots:
+        assert isinstance(node, NUSNode_gdn)
+    if any(node.perm is not None for node in roots):
+        raise NotImplementedError("gdn_nested_uniform_scramble on the GPU scrambles fresh trees only; these root "
+                                  "nodes were used by an earlier call")
+    if len({id(getattr(g, "bit_generator", g)) for g in gens}) != G:
+        raise ValueError("rngs must hold r*d distinct generators: the reference draws a shared generator's "
+                         "stream across the (l, j) pairs it serves, one pair after another")
+    bases_np = np.ascontiguousarray(np.asarray(bases, dtype=np.uint64)).reshape(-1)
+    if bases_np.size < r_b * d:
+        raise ValueError("bases has %d elements, the call needs r_b*d = %d" % (bases_np.size, r_b * d))
+    bases_np = bases_np[:r_b * d]
+    if G and (bases_np.min() < 2 or bases_np.max() > 65536):
+        raise ValueError("bases must lie in 2..65536 for the GPU form")
+    if not (1 <= tmax < tmax_new <= 255):
+        raise ValueError("the GPU form needs 1 <= tmax < tmax_new <= 255 (tmax=%d, tmax_new=%d)" % (tmax, tmax_new))
+    if G and tmax * int(np.ceil(np.log2(float(bases_np.max())))) > 128:
+        raise ValueError("tmax * ceil(log2 b) must not exceed 128 bits for the GPU form")
+    dxd, hxd = _u64_array(xdig, r_x * n * d * tmax, "xdig", 11)
+    dxr, hxr = _u64_array(xrdig, r * n * d * tmax_new, "xrdig", 12)
+    states = np.stack([sfc64_state_words(g) for g in gens]) if G else np.zeros((0, STATE_WORDS), np.uint64)
+    lib = _ffi.lib()
+    if G == 0:
+        return time.perf_counter() - t0_perf, time.process_time() - t0_process
+    dev = dxd.device if dxd is not None else (dxr.device if dxr is not None else
+                                              torch.device("cuda", torch.cuda.current_device()))
+    stream = kwargs.get("stream") or torch.cuda.current_stream(dev)
+    per = gdn_workspace_bytes(n, 1)
+    budget = kwargs.get("workspace_bytes")
+    if budget is None:
+        free, _total = torch.cuda.mem_get_info(dev)
+        budget = min(free // 4, 32 << 30)
+    # a first guess at the permutation entries per generator: every level below
+    # the digits that n points share, for every point (exact sizes come back
+    # from the call when the guess is short)
+    bmax = int(bases_np.max())
+    share = int(np.floor(np.log(max(n, 1)) / np.log(max(int(bases_np.min()), 2))))
+    perm_per = (n + 1) * bmax * max(1, tmax_new - max(share - 1, 0))
+    count = max(1, min(G, int(budget) // (per + 2 * perm_per)))
+    wbytes = gdn_workspace_bytes(n, count)
+    capacity = count * perm_per
+    with torch.cuda.device(dev), torch.cuda.stream(stream):
+        i64 = torch.int64
+        dbases = torch.from_numpy(bases_np.view(np.int64)).to(dev)
+        if dxd is None:
+            dxd = torch.from_numpy(hxd.reshape(-1)[:r_x * n * d * tmax].view(np.int64)).to(dev) if n else \
+                torch.empty(1, dtype=i64, device=dev)
+        if dxr is None:
+            dxr = torch.empty(max(r * n * d * tmax_new, 1), dtype=i64, device=dev)
+        work = torch.empty(wbytes, dtype=torch.uint8, device=dev)
+        needed = ctypes.c_uint64(0)
+        for _attempt in range(3):
+            dstate = torch.from_numpy(states.reshape(-1).view(np.int64)).to(dev)
+            perms = torch.empty(max(capacity, 1), dtype=torch.int16, device=dev)
+            rc = lib.qmc_gdn_nested_uniform_scramble(
+                r, n, d, r_x, r_b, tmax, tmax_new, dstate.data_ptr(), dbases.data_ptr(), dxd.data_ptr(),
+                dxr.data_ptr(), perms.data_ptr(), capacity, ctypes.byref(needed), work.data_ptr(), wbytes,
+                stream.cuda_stream)
+            if rc == _ffi.QMC_ERR_ARG and needed.value > capacity:
+                del perms
+                capacity = int(needed.value * 1.25) + 1
+                continue
+            _ffi.check(rc, "gdn_nested_uniform_scramble")
+            break
+        else:
+            raise _ffi.QmcError("gdn_nested_uniform_scramble: permutation buffer sizing did not settle")
+        rc = lib.qmc_device_error_check(stream.cuda_stream)
+        if rc == _ffi.QMC_ERR_DEVICE:
+            raise IndexError("gdn_nested_uniform_scramble: a digit at or above its base")
+        _ffi.check(rc, "gdn_nested_uniform_scramble")
+        if hxr is not None and n:
+            torch.from_numpy(hxr.reshape(-1)[:r * n * d * tmax_new].view(np.int64)).copy_(dxr[:r * n * d * tmax_new])
+        new_states = dstate.cpu().numpy().view(np.uint64).reshape(G, STATE_WORDS)
+        del work, perms
+    for k in range(G):
+        set_sfc64_state(gens[k], new_states[k])
+        roots[k].perm = np.zeros(0, dtype=np.uint64)  # used: the GPU form keeps no tree
+    return time.perf_counter() - t0_perf, time.process_time() - t0_process
