@@ -1356,8 +1356,97 @@ def run_nus(args):
                              "seconds": t_cpu}}
 
 
+def run_gdn_nus(args):
+    """Nested uniform (Owen) scrambling of generalized nets, bit for bit the reference's
+    gdn_nested_uniform_scramble (qmctoolscl/rand_funcs.py:262-356) with numpy SFC64 generators:
+    Halton points in the first 8 primes (natural order, identity matrices), r=16, n=2^16,
+    tmax=16, tmax_new=20, fresh trees, through the drop-in with device arrays; e2e with numpy
+    arrays.  Checked against the oracle on the first 512 points of three generators; the
+    oracle over all host threads as the CPU baseline."""
+    import torch
+    import oracle
+    import qmctoolscl_gb300 as q
+    from qmctoolscl_gb300 import nus
+    r, m = (4, 12) if args.small else (16, 16)
+    n, d, tmax, tmax_new = 1 << m, 8, 16, 20
+    G = r * d
+    bases_np = np.array([[2, 3, 5, 7, 11, 13, 17, 19]], dtype=np.uint64)
+    C = torch.from_numpy(np.tile(np.eye(tmax, dtype=np.uint64)[None, None], (1, d, 1, 1)).reshape(-1).view(np.int64)).cuda()
+    dbases = torch.from_numpy(bases_np.reshape(-1).view(np.int64)).cuda()
+    xdig = torch.empty(n * d * tmax, dtype=torch.int64, device="cuda")
+    q.gdn_gen_natural(1, n, d, 1, tmax, tmax, 0, dbases, C, xdig)
+    xr = torch.empty(G * n * tmax_new, dtype=torch.int64, device="cuda")
+    seeds = np.random.SeedSequence(8).spawn(G)
+    st = torch.cuda.current_stream()
+
+    def call(xin, xout):
+        gens = np.array([np.random.Generator(np.random.SFC64(sd)) for sd in seeds], dtype=object).reshape(r, d)
+        roots = np.array([q.NUSNode_gdn() for _ in range(G)]).reshape(r, d)
+        q.gdn_nested_uniform_scramble(r, n, d, 1, 1, tmax, tmax_new, gens, roots, bases_np, xin, xout)
+
+    ms = gpu_ms(lambda: call(xdig, xr), args.steps, args.warmup, st)
+    xd_np = xdig.cpu().numpy().view(np.uint64).reshape(1, n, d, tmax)
+    out = xr.view(r, n, d, tmax_new)
+    nn = 512
+    for (l, j) in ((0, 0), (1, 3), (r - 1, d - 1)):
+        w = nus.sfc64_state_words(np.random.Generator(np.random.SFC64(seeds[l * d + j])))
+        want = np.zeros((1, nn, 1, tmax_new), dtype=np.uint64)
+        f = oracle.GdnNusForest(1)
+        assert f.scramble(1, nn, 1, 1, 1, tmax, tmax_new, w, bases_np[:, j:j + 1].copy(),
+                          np.ascontiguousarray(xd_np[:, :nn, j:j + 1]), want) == 0
+        f.close()
+        got = out[l, :nn, j].cpu().numpy().view(np.uint64)
+        assert np.array_equal(got, want.reshape(nn, tmax_new)), "base-b nested uniform scramble differs from the oracle"
+    # e2e: numpy arrays in and out
+    xr_np = np.empty((r, n, d, tmax_new), dtype=np.uint64)
+    call(xd_np, xr_np)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    call(xd_np, xr_np)
+    t_e2e = time.perf_counter() - t0
+    # CPU: the oracle, whole generators of replication 0 (all 8 bases), one per thread
+    threads = host_threads()
+
+    def one_gen(k):
+        j = k % d
+        w = nus.sfc64_state_words(np.random.Generator(np.random.SFC64(seeds[k])))
+        o = np.zeros((1, n, 1, tmax_new), dtype=np.uint64)
+        f = oracle.GdnNusForest(1)
+        f.scramble(1, n, 1, 1, 1, tmax, tmax_new, w, bases_np[:, j:j + 1].copy(),
+                   np.ascontiguousarray(xd_np[:, :, j:j + 1]), o)
+        f.close()
+
+    gs = min(G, 2 * d)
+    t0 = time.perf_counter()
+    with concurrent.futures.ThreadPoolExecutor(threads) as ex:
+        list(ex.map(one_gen, range(gs)))
+    t_cpu = time.perf_counter() - t0
+    pts = G * n
+    return {"metric": METRIC, "value": pts / (ms / 1e3), "unit": "points/s (d=8, 20 digits each)", "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "u64 digits, 128-bit keys, the SFC64 stream",
+            "data": "synthetic: natural-order Halton digits in bases 2..19; generators "
+                    "SFC64(SeedSequence(8).spawn(r*d))",
+            "config": {"workload": "gdn_nested_uniform_scramble, r=%d, n=2^%d, d=8 (first 8 primes), tmax=16, "
+                                   "tmax_new=20, fresh trees" % (r, m), "r": r, "n": n, "d": d},
+            "roofline": dict(roofline(8.0 * (n * d * tmax + pts * tmax_new), ms), kernel="the whole pipeline",
+                             note="bound by the serial permutation draws: per generator numpy's Fisher-Yates "
+                                  "(b-1 masked draws per level) for every level below each point's branch, "
+                                  "one thread per generator; achieved counts only the digit I/O"),
+            "e2e": {"value": pts / t_e2e, "unit": "points/s", "seconds_per_call": t_e2e,
+                    "h2d_bytes_per_step": int(8 * n * d * tmax + 48 * G),
+                    "d2h_bytes_per_step": int(8 * pts * tmax_new + 48 * G),
+                    "path": "qmctoolscl_gb300.gdn_nested_uniform_scramble with numpy arrays and Generators"},
+            "gpu_launches": args.steps * (8 + 3 * min(8, (n.bit_length() + 4 + 7) // 8)),  # one chunk
+            "cpu_baseline": {"value": gs * n / t_cpu, "unit": "points/s", "cores": threads, "kind": "port",
+                             "sample": "%d whole generators (2^%d points each, bases 2..19), one per thread, by the "
+                                       "oracle (C restatement of the reference's tree walk)" % (gs, m),
+                             "seconds": t_cpu}}
+
+
 WORKLOADS = {"net_plain": run_net_plain, "net_lms": run_net_lms, "fft": run_fft, "halton": run_halton,
-             "plain": run_gdn_plain, "gdn_plain": run_gdn_plain, "qrng": run_qrng, "nus": run_nus}
+             "plain": run_gdn_plain, "gdn_plain": run_gdn_plain, "qrng": run_qrng, "nus": run_nus,
+             "gdn_nus": run_gdn_nus}
 
 
 def main():
