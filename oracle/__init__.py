@@ -8,7 +8,7 @@ Two CPU implementations live here:
 
 * ``liboracle.so`` -- qmc_oracle.c, our C restatement of the reference C
   backend (each function cites the reference file:line it follows).  Built by
-  ``make -C oracle``; it builds on any host with gcc, including the GPU machine.
+  ``make -C oracle``; it builds on any host with gcc (x86-64 or aarch64).
 * ``_ref/c_lib.so`` -- the reference's own C sources compiled where they lie
   (``make -C oracle ref``); only available where the reference checkout is.
   Used to pin the restatement and to make the golden fixtures.
