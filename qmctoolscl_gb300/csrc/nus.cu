@@ -70,6 +70,9 @@ __global__ void nus_keys_kernel(NusDims m, const u64 *__restrict__ xb, const u64
 }
 
 
+// ---- 2-3. the radix sort and the bottom-up tree pass: nus_dev.cuh -------------------
+
+// ---- 4. the draws, one thread per generator --------------------------------------
 // One thread per generator.  L_v comes in 16 at a time (one 16-byte load per
 // group, rows start 16-byte aligned), three groups ahead of the draws.  A
 // group whose 16 draws are all 64-bit draws (33..63 bits) or all 32-bit
