@@ -68,3 +68,26 @@ def test_shared_generator_is_refused():
     with pytest.raises(ValueError):
         q.dnb2_nested_uniform_scramble(2, 4, 1, 1, 8, 16, np.array([g, h], dtype=object).reshape(2, 1), roots, xb,
                                        xrb)
+
+
+def test_c_entry_points_check_arguments_before_any_launch():
+    """the C ABI rejects out-of-domain calls with a status and a message, on
+    the host, before touching any pointer (addresses here are never used)"""
+    from qmctoolscl_gb300 import _ffi
+    lib = _ffi.lib()
+    fake = 0x100000  # 256-byte aligned, never dereferenced by a rejected call
+    rc = lib.qmc_dnb2_nested_uniform_scramble(1, 4, 1, 1, 8, 65, fake, 0, None, None, fake, fake, None, None, fake,
+                                              1 << 30, None)
+    assert rc == _ffi.QMC_ERR_DOMAIN and b"between 0 and 64" in lib.qmc_last_error()
+    rc = lib.qmc_dnb2_nested_uniform_scramble(1, 4, 1, 1, 8, 16, fake, 0, None, None, fake, fake, None, None, fake,
+                                              64, None)  # workspace far too small
+    assert rc == _ffi.QMC_ERR_ARG and b"workspace" in lib.qmc_last_error()
+    needed = ctypes.c_uint64(7)
+    rc = lib.qmc_gdn_nested_uniform_scramble(1, 4, 1, 1, 1, 3, 3, fake, fake, fake, fake, fake, 1 << 20,
+                                             ctypes.byref(needed), fake, 1 << 30, None)
+    assert rc == _ffi.QMC_ERR_ARG and b"tmax < tmax_new" in lib.qmc_last_error() and needed.value == 0
+    rc = lib.qmc_gdn_nested_uniform_scramble(1, 4, 1, 1, 1, 3, 5, None, fake, fake, fake, fake, 1 << 20,
+                                             ctypes.byref(needed), fake, 1 << 30, None)
+    assert rc == _ffi.QMC_ERR_ARG
+    assert lib.qmc_gdn_nested_uniform_scramble(0, 4, 1, 1, 1, 3, 5, None, None, None, None, None, 0, None, None, 0,
+                                               None) == _ffi.QMC_OK  # r = 0: nothing to do
