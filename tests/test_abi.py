@@ -95,3 +95,32 @@ def test_generalized_net_plan_argument_errors_need_no_gpu(lib):
     assert rc == _ffi.QMC_ERR_ARG and b"all dimensions" in msg
     assert create([dim()], n=1, n_start=(1 << 32))[0] == _ffi.QMC_ERR_ARG
     assert create([dim(C=None)])[0] == _ffi.QMC_ERR_ARG
+
+
+def test_header_compiles_as_c_and_links(lib, tmp_path):
+    """include/qmcgb.h is plain C (C99) and a C caller links libqmcgb.so and
+    calls it (version, last error, an argument error), as INTEGRATION.md's C
+    section shows -- no GPU needed."""
+    import shutil
+    import subprocess
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    src = tmp_path / "caller.c"
+    src.write_text(
+        '#include "qmcgb.h"\n'
+        "#include <stdio.h>\n"
+        "int main(void) {\n"
+        "    if (qmc_version() < 10000) return 2;\n"
+        "    int rc = qmc_fwht_1d_radix2(1, 1, 3, 0, 0);\n"
+        "    if (rc != QMC_ERR_DOMAIN) return 3;\n"
+        '    printf("%s\\n", qmc_last_error());\n'
+        "    return 0;\n"
+        "}\n")
+    libdir = os.path.dirname(lib._name)
+    exe = tmp_path / "caller"
+    subprocess.run([cc, "-std=c99", "-Wall", "-Werror", "-I", os.path.join(REPO, "include"), str(src), "-L", libdir,
+                    "-lqmcgb", "-Wl,-rpath," + libdir, "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe)], capture_output=True, text=True)
+    assert out.returncode == 0, out
+    assert out.stdout.strip() != ""
