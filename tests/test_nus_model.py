@@ -91,3 +91,62 @@ def test_baseb_model_matches_oracle(seed):
     got = nus_model.gdn_scramble(r, n, d, r_x, r_b, tmax, tmax_new, bases.tolist(), states, x.tolist(), seed=seed)
     assert np.array_equal(np.array(got, dtype=np.uint64).reshape(r, n, d, tmax_new), want)
     assert np.array_equal(np.array(states, dtype=np.uint64).reshape(-1), words)
+
+
+def _net_bits(rng, n_log2, d, tmax):
+    """natural-order points of random nonsingular upper-triangular matrices, MSB first in tmax bits"""
+    n = 1 << n_log2
+    xb = np.zeros((1, n, d), dtype=np.uint64)
+    for j in range(d):
+        M = np.triu(rng.integers(0, 2, (n_log2, n_log2)), 1) + np.eye(n_log2, dtype=np.int64)
+        cols = [sum(int(M[t, k]) << (tmax - 1 - t) for t in range(n_log2)) for k in range(n_log2)]
+        for i in range(n):
+            v = 0
+            for k in range(n_log2):
+                if (i >> k) & 1:
+                    v ^= cols[k]
+            xb[0, i, j] = v
+    return xb
+
+
+def test_scramble_keeps_the_net_property():
+    """Owen scrambling maps a (0, m, 1)-net to a (0, m, 1)-net: the top m bits of
+    the 2^m scrambled points stay a permutation of 0 .. 2^m - 1 in every
+    dimension (oracle and model alike)"""
+    rng = np.random.Generator(np.random.SFC64(5))
+    m, d, r, T = 7, 3, 2, 32
+    xb = _net_bits(rng, m, d, T)
+    st = _states(rng, r * d)
+    words = st.reshape(-1).copy()
+    got = np.zeros((r, 1 << m, d), dtype=np.uint64)
+    f = oracle.NusForest(r * d)
+    f.scramble(r, 1 << m, d, 1, T, T, words, xb, got)
+    f.close()
+    model = np.array(nus_model.dnb2_scramble(r, 1 << m, d, 1, T, T, [list(w) for w in st], xb.tolist()),
+                     dtype=np.uint64)
+    assert np.array_equal(model, got)
+    for l in range(r):
+        for j in range(d):
+            top = np.sort(got[l, :, j] >> np.uint64(T - m))
+            assert np.array_equal(top, np.arange(1 << m, dtype=np.uint64))
+    assert not np.array_equal(got[0], xb[0])  # and it did scramble
+
+
+def test_base_b_scramble_keeps_the_digit_net_property():
+    """the same for base b: the first m digits of the b^m scrambled points take
+    every value once"""
+    rng = np.random.Generator(np.random.SFC64(6))
+    b, m, tmax, tmax_new, r = 3, 4, 4, 6, 2
+    n = b ** m
+    bases = np.array([[b]], dtype=np.uint64)
+    C = np.tile(np.eye(tmax, dtype=np.uint64)[None, None], (1, 1, 1, 1))
+    xdig = np.zeros((1, n, 1, tmax), dtype=np.uint64)
+    oracle.call("gdn_gen_natural", 1, n, 1, 1, tmax, tmax, 0, bases, C, xdig)
+    st = _states(rng, r)
+    got = np.zeros((r, n, 1, tmax_new), dtype=np.uint64)
+    f = oracle.GdnNusForest(r)
+    assert f.scramble(r, n, 1, 1, 1, tmax, tmax_new, st.reshape(-1).copy(), bases, xdig, got) == 0
+    f.close()
+    for l in range(r):
+        prefix = sorted(tuple(int(v) for v in got[l, i, 0, :m]) for i in range(n))
+        assert len(set(prefix)) == n
