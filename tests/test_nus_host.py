@@ -91,3 +91,24 @@ def test_c_entry_points_check_arguments_before_any_launch():
     assert rc == _ffi.QMC_ERR_ARG
     assert lib.qmc_gdn_nested_uniform_scramble(0, 4, 1, 1, 1, 3, 5, None, None, None, None, None, 0, None, None, 0,
                                                None) == _ffi.QMC_OK  # r = 0: nothing to do
+
+
+def test_host_write_decision(monkeypatch):
+    """where the kernels may write a numpy result directly: the device alias of
+    pinned memory; the array's own address when the GPU reaches pageable memory
+    through the host page tables; otherwise nowhere (a device buffer and a copy)"""
+    from qmctoolscl_gb300 import _ffi
+    arr = np.zeros(8, np.uint64)
+    ptr = arr.ctypes.data
+    monkeypatch.setattr(nus, "_ATTRS", {})
+    monkeypatch.setattr(_ffi, "device_pointer_of_host", lambda p: p + 4096)
+    assert nus._host_writable(arr, True) == ptr + 4096
+    assert nus._host_writable(arr, False) is None
+    monkeypatch.setattr(_ffi, "device_pointer_of_host", lambda p: None)
+    monkeypatch.setattr(_ffi, "device_attributes",
+                        lambda: {"pageable_access": 1, "uses_host_page_tables": 1, "sms": 152})
+    assert nus._host_writable(arr, True) == ptr
+    monkeypatch.setattr(nus, "_ATTRS", {})
+    monkeypatch.setattr(_ffi, "device_attributes",
+                        lambda: {"pageable_access": 1, "uses_host_page_tables": 0, "sms": 132})
+    assert nus._host_writable(arr, True) is None
