@@ -251,8 +251,10 @@ or pageable memory through the host's page tables), else copied back."""
 class NUSNode_gdn(object):
     """Root of one generator's base-b scrambling tree, with the fields of the
     reference's node (qmctoolscl/rand_funcs.py:255-260).  A fresh node (perm
-    None) starts a tree.  The GPU form scrambles fresh trees: after a call the
-    node is marked used (perm set) and holds no tree to continue."""
+    None) starts a tree.  After a call the node is marked used (perm set) and
+    keeps what a later call needs to continue the tree by replay: the
+    generator's state before the first call and after the last, and the
+    digits of every point so far."""
 
     def __init__(self, perm=None, xdig=None, children=None):
         self.perm = perm
@@ -268,60 +270,16 @@ def gdn_workspace_bytes(n, generators):
     return out.value
 
 
-def gdn_nested_uniform_scramble(r, n, d, r_x, r_b, tmax, tmax_new, rngs, root_nodes, bases, xdig, xrdig, **kwargs):
-    """Nested uniform scramble of general digital nets
-
-Args:
-    r (np.uint64): replications
-    n (np.uint64): points
-    d (np.uint64): dimensions
-    r_x (np.uint64): replications of xb
-    r_b (np.uint64): replications of bases
-    tmax (np.uint64): maximum number digits in each point representation
-    tmax_new (np.uint64): maximum number digits in each point representation after scrambling
-    rngs (np.ndarray of numpy.random._generator.Generator): random number generators of size r*d
-    root_nodes (np.ndarray of NUSNode_gdn): root nodes of size r*d
-    bases (np.ndarray of np.uint64): array of bases of size r*d
-    xdig (np.ndarray of np.uint64): array of unrandomized points of size r*n*d*tmax
-    xrdig (np.ndarray of np.uint64): array to store scrambled points of size r*n*d*tmax_new
-
-Runs on the GPU for fresh root nodes (one call per set of nodes; a used set
-raises NotImplementedError) with bases 2..65536, tmax < tmax_new <= 255 and
-tmax * ceil(log2 b) <= 128 (ValueError otherwise).  A digit at or above its
-base raises IndexError, as the reference does.  Keyword arguments:
-``workspace_bytes`` caps the device scratch, ``stream`` selects a
-torch.cuda.Stream."""
-    t0_perf = time.perf_counter()
-    t0_process = time.process_time()
+def _gdn_fresh(r, n, d, r_x, r_b, tmax, tmax_new, states, bases_np, xdig, xrdig, kwargs):
+    """One call of qmc_gdn_nested_uniform_scramble on fresh trees.  xdig and
+    xrdig as the public function takes them (numpy arrays or CUDA tensors,
+    checked there), states the (r*d, 6) generator words before the call;
+    returns the words after it."""
     torch = _t()
-    r, n, d, r_x, r_b, tmax, tmax_new = (int(v) for v in (r, n, d, r_x, r_b, tmax, tmax_new))
     G = r * d
-    gens = _objects(rngs, r, d, "rngs")
-    roots = _objects(root_nodes, r, d, "root_nodes")
-    for node in roots:
-        assert isinstance(node, NUSNode_gdn)
-    if any(node.perm is not None for node in roots):
-        raise NotImplementedError("gdn_nested_uniform_scramble on the GPU scrambles fresh trees only; these root "
-                                  "nodes were used by an earlier call")
-    if len({id(getattr(g, "bit_generator", g)) for g in gens}) != G:
-        raise ValueError("rngs must hold r*d distinct generators: the reference draws a shared generator's "
-                         "stream across the (l, j) pairs it serves, one pair after another")
-    bases_np = np.ascontiguousarray(np.asarray(bases, dtype=np.uint64)).reshape(-1)
-    if bases_np.size < r_b * d:
-        raise ValueError("bases has %d elements, the call needs r_b*d = %d" % (bases_np.size, r_b * d))
-    bases_np = bases_np[:r_b * d]
-    if G and (bases_np.min() < 2 or bases_np.max() > 65536):
-        raise ValueError("bases must lie in 2..65536 for the GPU form")
-    if not (1 <= tmax < tmax_new <= 255):
-        raise ValueError("the GPU form needs 1 <= tmax < tmax_new <= 255 (tmax=%d, tmax_new=%d)" % (tmax, tmax_new))
-    if G and tmax * int(np.ceil(np.log2(float(bases_np.max())))) > 128:
-        raise ValueError("tmax * ceil(log2 b) must not exceed 128 bits for the GPU form")
     dxd, hxd = _u64_array(xdig, r_x * n * d * tmax, "xdig", 11)
     dxr, hxr = _u64_array(xrdig, r * n * d * tmax_new, "xrdig", 12)
-    states = np.stack([sfc64_state_words(g) for g in gens]) if G else np.zeros((0, STATE_WORDS), np.uint64)
     lib = _ffi.lib()
-    if G == 0:
-        return time.perf_counter() - t0_perf, time.process_time() - t0_process
     dev = dxd.device if dxd is not None else (dxr.device if dxr is not None else
                                               torch.device("cuda", torch.cuda.current_device()))
     stream = kwargs.get("stream") or torch.cuda.current_stream(dev)
@@ -372,7 +330,117 @@ torch.cuda.Stream."""
             torch.from_numpy(hxr.reshape(-1)[:r * n * d * tmax_new].view(np.int64)).copy_(dxr[:r * n * d * tmax_new])
         new_states = dstate.cpu().numpy().view(np.uint64).reshape(G, STATE_WORDS)
         del work, perms
+    return new_states
+
+
+def gdn_nested_uniform_scramble(r, n, d, r_x, r_b, tmax, tmax_new, rngs, root_nodes, bases, xdig, xrdig, **kwargs):
+    """Nested uniform scramble of general digital nets
+
+Args:
+    r (np.uint64): replications
+    n (np.uint64): points
+    d (np.uint64): dimensions
+    r_x (np.uint64): replications of xb
+    r_b (np.uint64): replications of bases
+    tmax (np.uint64): maximum number digits in each point representation
+    tmax_new (np.uint64): maximum number digits in each point representation after scrambling
+    rngs (np.ndarray of numpy.random._generator.Generator): random number generators of size r*d
+    root_nodes (np.ndarray of NUSNode_gdn): root nodes of size r*d
+    bases (np.ndarray of np.uint64): array of bases of size r*d
+    xdig (np.ndarray of np.uint64): array of unrandomized points of size r*n*d*tmax
+    xrdig (np.ndarray of np.uint64): array to store scrambled points of size r*n*d*tmax_new
+
+Runs on the GPU with bases 2..65536, tmax < tmax_new <= 255 and
+tmax * ceil(log2 b) <= 128 (ValueError otherwise).  A digit at or above its
+base raises IndexError, as the reference does.  A later call on the same
+root nodes continues their trees as the reference does: a point's result
+depends only on the points before it, so the call scrambles the earlier
+points again together with the new ones, from the generators' states before
+the first call, and keeps the new points' results; the generators must not
+have been drawn from in between (ValueError).  Keyword arguments:
+``workspace_bytes`` caps the device scratch, ``stream`` selects a
+torch.cuda.Stream."""
+    t0_perf = time.perf_counter()
+    t0_process = time.process_time()
+    r, n, d, r_x, r_b, tmax, tmax_new = (int(v) for v in (r, n, d, r_x, r_b, tmax, tmax_new))
+    G = r * d
+    gens = _objects(rngs, r, d, "rngs")
+    roots = _objects(root_nodes, r, d, "root_nodes")
+    for node in roots:
+        assert isinstance(node, NUSNode_gdn)
+    if len({id(getattr(g, "bit_generator", g)) for g in gens}) != G:
+        raise ValueError("rngs must hold r*d distinct generators: the reference draws a shared generator's "
+                         "stream across the (l, j) pairs it serves, one pair after another")
+    bases_np = np.ascontiguousarray(np.asarray(bases, dtype=np.uint64)).reshape(-1)
+    if bases_np.size < r_b * d:
+        raise ValueError("bases has %d elements, the call needs r_b*d = %d" % (bases_np.size, r_b * d))
+    bases_np = bases_np[:r_b * d]
+    if G and (bases_np.min() < 2 or bases_np.max() > 65536):
+        raise ValueError("bases must lie in 2..65536 for the GPU form")
+    if not (1 <= tmax < tmax_new <= 255):
+        raise ValueError("the GPU form needs 1 <= tmax < tmax_new <= 255 (tmax=%d, tmax_new=%d)" % (tmax, tmax_new))
+    if G and tmax * int(np.ceil(np.log2(float(bases_np.max())))) > 128:
+        raise ValueError("tmax * ceil(log2 b) must not exceed 128 bits for the GPU form")
+    _u64_array(xdig, r_x * n * d * tmax, "xdig", 11)
+    _u64_array(xrdig, r * n * d * tmax_new, "xrdig", 12)
+    base_of = [int(bases_np[(k // d % r_b) * d + k % d]) for k in range(G)]
+    fresh = [node.perm is None for node in roots]
+    first_call = all(fresh)
+    h = 0
+    if first_call:
+        pass
+    elif not any(fresh) and all(getattr(node, "_hist", None) is not None for node in roots):
+        hs = {node._hist["digits"].shape[0] for node in roots}
+        if len(hs) != 1:
+            raise ValueError("root_nodes hold trees of different sizes; scramble them in separate calls")
+        h = hs.pop()
+        for k, node in enumerate(roots):
+            hk = node._hist
+            if (hk["tmax"], hk["tmax_new"], hk["base"]) != (tmax, tmax_new, base_of[k]):
+                raise ValueError("root_nodes were built with another tmax, tmax_new or base")
+            if not np.array_equal(sfc64_state_words(gens[k]), hk["state_after"]):
+                raise ValueError("a generator was drawn from since its tree's last call; continuing the tree "
+                                 "replays its stream from the first call")
+    else:
+        raise ValueError("root_nodes must be all fresh or all built by earlier calls of this function")
+    if G == 0:
+        return time.perf_counter() - t0_perf, time.process_time() - t0_process
+    now = np.stack([sfc64_state_words(g) for g in gens])
+    if first_call:
+        new_states = _gdn_fresh(r, n, d, r_x, r_b, tmax, tmax_new, now, bases_np, xdig, xrdig, kwargs)
+        start = now
+        xd_np = _host_digits(xdig, r_x, n, d, tmax)
+        digits = [xd_np[(k // d) % r_x, :, k % d, :].copy() for k in range(G)]
+    else:
+        start = np.stack([node._hist["state0"] for node in roots])
+        xd_np = _host_digits(xdig, r_x, n, d, tmax)
+        digits = [np.concatenate([roots[k]._hist["digits"], xd_np[(k // d) % r_x, :, k % d, :]]) for k in range(G)]
+        full = np.empty((r, h + n, d, tmax), dtype=np.uint64)
+        for k in range(G):
+            full[k // d, :, k % d, :] = digits[k]
+        out = np.empty((r, h + n, d, tmax_new), dtype=np.uint64)
+        new_states = _gdn_fresh(r, h + n, d, r, r_b, tmax, tmax_new, start, bases_np, full, out, kwargs)
+        _store_digits(xrdig, np.ascontiguousarray(out[:, h:]))
     for k in range(G):
         set_sfc64_state(gens[k], new_states[k])
-        roots[k].perm = np.zeros(0, dtype=np.uint64)  # used: the GPU form keeps no tree
+        roots[k].perm = np.zeros(0, dtype=np.uint64)  # used; the tree lives in _hist
+        roots[k]._hist = {"state0": start[k].copy(), "state_after": new_states[k].copy(), "digits": digits[k],
+                          "tmax": tmax, "tmax_new": tmax_new, "base": base_of[k]}
     return time.perf_counter() - t0_perf, time.process_time() - t0_process
+
+
+def _host_digits(xdig, r_x, n, d, tmax):
+    """the digits as a host numpy array (r_x, n, d, tmax)"""
+    if type(xdig).__module__.startswith("torch"):
+        return xdig.reshape(-1)[:r_x * n * d * tmax].cpu().numpy().view(np.uint64).reshape(r_x, n, d, tmax)
+    return np.asarray(xdig).reshape(-1)[:r_x * n * d * tmax].reshape(r_x, n, d, tmax)
+
+
+def _store_digits(xrdig, values):
+    """values (numpy) into xrdig, a numpy array or a CUDA tensor"""
+    flat = values.reshape(-1)
+    if type(xrdig).__module__.startswith("torch"):
+        torch = _t()
+        xrdig.reshape(-1)[:flat.size].copy_(torch.from_numpy(flat.view(np.int64)))
+    else:
+        xrdig.reshape(-1)[:flat.size] = flat
