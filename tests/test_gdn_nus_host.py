@@ -105,3 +105,19 @@ def test_generators_and_nodes():
 def test_workspace_query():
     one = nus.gdn_workspace_bytes(1 << 12, 1)
     assert nus.gdn_workspace_bytes(1 << 12, 8) > 7 * one
+
+
+def test_history_digits_from_tensors_and_arrays():
+    """the digits a tree keeps for replay, read from a numpy array or a tensor
+    (here on the CPU; the drop-in passes CUDA tensors) and written back"""
+    import torch
+    x = np.arange(2 * 3 * 2 * 4, dtype=np.uint64).reshape(2, 3, 2, 4)
+    assert np.array_equal(nus._host_digits(x, 2, 3, 2, 4), x)
+    t = torch.from_numpy(x.reshape(-1).view(np.int64).copy())
+    assert np.array_equal(nus._host_digits(t, 2, 3, 2, 4), x)
+    out_t = torch.zeros(x.size, dtype=torch.int64)
+    nus._store_digits(out_t, x)
+    assert np.array_equal(out_t.numpy().view(np.uint64).reshape(x.shape), x)
+    out_a = np.zeros_like(x)
+    nus._store_digits(out_a, x)
+    assert np.array_equal(out_a, x)
