@@ -183,14 +183,6 @@ int qmc_dnb2_gen_fused(uint64_t r, uint64_t n, uint64_t d, uint64_t n_start, uin
                        uint64_t r_C, int gray, const uint64_t *lshifts, uint64_t r_x, const uint64_t *shiftsb,
                        const uint64_t *tmaxes, uint64_t *xrb, double *x, qmc_stream_t s);
 
-/* ---- tensor-core check ---------------------------------------------------
- * No reference counterpart.  One CTA computes D = A * B^T with tcgen05.mma
- * (A: 128 x K, B: N x K, row-major BF16; D: 128 x N, row-major FP32), with
- * the operand layout and descriptors the tensor-core transforms use; a
- * timed-out completion wait is recorded in the device error word.
- * N in [16, 256] and K in [16, 256], multiples of 16. */
-int qmc_tc_mma_probe(const void *A, const void *B, float *D, uint32_t N, uint32_t K, qmc_stream_t s);
-
 /* ---- tensor-core transforms ---------------------------------------------
  * The contracts of qmc_fft_bro_1d_radix2 / qmc_ifft_bro_1d_radix2 /
  * qmc_fwht_1d_radix2 (qmctoolscl/c_funcs/fft_bro_1d_radix2.c:3-80,

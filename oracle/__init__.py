@@ -34,9 +34,13 @@ _lock = threading.Lock()
 _libs = {}
 
 
-def build(ref=False):
-    """Compile the oracle (and, with ref=True, the reference C backend)."""
-    subprocess.run(["make", "-s", "-C", HERE] + (["ref"] if ref else []), check=True)
+def build(ref=False, ref_dir=None):
+    """Compile the oracle (and, with ref=True, the reference C backend from the
+    QMCToolsCL checkout at ref_dir, or at $QMCTOOLSCL_REF when ref_dir is None)."""
+    extra = ["ref"] if ref else []
+    if ref and ref_dir:
+        extra.append("REF_DIR=%s" % ref_dir)
+    subprocess.run(["make", "-s", "-C", HERE] + extra, check=True)
 
 
 def _argtype(kind):

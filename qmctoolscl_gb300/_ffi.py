@@ -25,7 +25,6 @@ INT = ctypes.c_int
 EXTRA = {
     "qmc_lat_gen_shift": [U64, U64, U64, U64, INT, PTR, PTR, PTR, PTR],
     "qmc_dnb2_gen_fused": [U64, U64, U64, U64, U64, PTR, U64, INT, PTR, U64, PTR, PTR, PTR, PTR, PTR],
-    "qmc_tc_mma_probe": [PTR, PTR, PTR, ctypes.c_uint32, ctypes.c_uint32, PTR],
     "qmc_tc_fft_bro_1d": [U64, U64, U64, PTR, PTR, PTR],
     "qmc_tc_ifft_bro_1d": [U64, U64, U64, PTR, PTR, PTR],
     "qmc_tc_fwht_1d": [U64, U64, U64, PTR, PTR],
@@ -92,6 +91,13 @@ def device_attributes():
     a, b, c = INT(), INT(), INT()
     check(lib().qmc_device_attributes(ctypes.byref(a), ctypes.byref(b), ctypes.byref(c)), "device_attributes")
     return {"pageable_access": a.value, "uses_host_page_tables": b.value, "sms": c.value}
+
+
+def writable(a):
+    """`a` itself when numpy marks it writeable, else a copy of it:
+    torch.from_numpy takes writeable arrays only (a read-only array would be
+    shared with a tensor that claims it may write)."""
+    return a if a.flags["WRITEABLE"] else a.copy()
 
 
 class QmcError(RuntimeError):

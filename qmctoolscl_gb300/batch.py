@@ -65,7 +65,7 @@ class _Args:
             self.d2h_bytes += flat.nbytes
         else:
             src = flat.view(np.int64) if dtype == np.uint64 else flat
-            d = torch.from_numpy(np.ascontiguousarray(src)).to(self.dev, non_blocking=True)
+            d = torch.from_numpy(_ffi.writable(np.ascontiguousarray(src))).to(self.dev, non_blocking=True)
             self.h2d_bytes += flat.nbytes
         self.keep.append(d)
         return d.data_ptr()

@@ -61,7 +61,7 @@ def halton_qrng_c(n, d, n0, generalized, res, randu_d_32, dvec):
     s = torch.cuda.current_stream()
     dev = []
     for a in (res, randu_d_32, dvec):
-        dev.append(a if _is_torch(a) else torch.from_numpy(a.reshape(-1)).cuda())
+        dev.append(a if _is_torch(a) else torch.from_numpy(_ffi.writable(a.reshape(-1))).cuda())
     L = _ffi.lib()
     _ffi.check(L.qmc_halton_qrng(n, d, n0, generalized, dev[0].data_ptr(), dev[1].data_ptr(), dev[2].data_ptr(),
                                  s.cuda_stream), "halton_qrng")

@@ -639,7 +639,8 @@ extern "C" int qmc_net_gen_noalloc(const qmc_net_request *req, qmc_stream_t s)
     QMC_REQUIRE(Q.C && (Q.xb || Q.x), "null matrices or no output");
     QMC_REQUIRE(!Q.shifts || Q.lshifts, "shifts without lshifts");
     QMC_REQUIRE(!Q.x || Q.tmaxes, "float output without tmaxes");
-    QMC_REQUIRE(alpha <= (u64)MAX_ALPHA && Q.d_pre == Q.d * alpha && Q.mmax <= 64 && Q.r_C > 0,
+    QMC_REQUIRE(alpha <= (u64)MAX_ALPHA && Q.d <= UINT64_MAX / alpha && Q.d_pre == Q.d * alpha && Q.mmax <= 64 &&
+                    Q.r_C > 0,
                 "bad alpha, d_pre, mmax or r_C");
     if ((!Q.gray && !gray_closed(Q.n_start, Q.n_start + Q.n)) || bitlen(Q.n_start + Q.n - 1) > Q.mmax ||
         Q.n_start + Q.n < Q.n_start) {
@@ -647,11 +648,14 @@ extern "C" int qmc_net_gen_noalloc(const qmc_net_request *req, qmc_stream_t s)
         return QMC_ERR_DOMAIN;
     }
     const bool prep = Q.S || alpha > 1;
+    // r*d*mmax bounded factor by factor, so that no product can wrap below the limit
+    const u64 per_r = Q.d <= (u64)QMC_NOALLOC_MATRIX_WORDS ? Q.d * (Q.mmax ? Q.mmax : 1) : UINT64_MAX;
+    QMC_REQUIRE(!prep || (per_r <= (u64)QMC_NOALLOC_MATRIX_WORDS && Q.r <= (u64)QMC_NOALLOC_MATRIX_WORDS / per_r),
+                "qmc_net_gen_noalloc: the request needs r*d*mmax words of matrix scratch (r=%llu, d=%llu, "
+                "mmax=%llu), above the %d this entry point holds; use a plan (qmc_net_plan_create) for it",
+                (unsigned long long)Q.r, (unsigned long long)Q.d, (unsigned long long)Q.mmax,
+                QMC_NOALLOC_MATRIX_WORDS);
     const u64 words = Q.r * Q.d * Q.mmax;
-    QMC_REQUIRE(!prep || words <= (u64)QMC_NOALLOC_MATRIX_WORDS,
-                "qmc_net_gen_noalloc: the request needs r*d*mmax = %llu words of matrix scratch, above the %d "
-                "this entry point holds; use a plan (qmc_net_plan_create) for it",
-                (unsigned long long)words, QMC_NOALLOC_MATRIX_WORDS);
     cudaStream_t st = QMC_STREAM(s);
     const u64 *C = (const u64 *)Q.C;
     u64 r_C = Q.r_C;

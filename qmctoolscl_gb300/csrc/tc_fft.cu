@@ -1,83 +1,12 @@
 // tc_fft.cu -- tensor-core (tcgen05, BF16 in / FP32 accumulate) paths of
 // the fast transforms.
-//
-// qmc_tc_mma_probe: one CTA computes D = A * B^T (A 128 x K, B N x K, BF16,
-// D FP32) through tcgen05.mma with the operand layout and descriptors of
-// tc_sm100.cuh; the tests compare it with an exact host product to pin the
-// descriptor encodings every tensor-core kernel here relies on.
 #include "fpconv.cuh"
 #include "tc_sm100.cuh"
 #include <type_traits>
 
 namespace {
-
 constexpr u32 WAIT_LIMIT = 1u << 22;  // mbarrier polls before giving up (~ a fraction of a second)
-
-__global__ void __launch_bounds__(128) tc_probe_kernel(const __nv_bfloat16 *A, const __nv_bfloat16 *B, float *D,
-                                                       u32 N, u32 K, u32 tcols, unsigned *err)
-{
-    extern __shared__ __align__(128) unsigned char sm[];
-    __shared__ __align__(8) u64 bar;
-    __shared__ u32 tmem_base;
-    unsigned char *sA = sm, *sB = sm + 128 * K * 2;
-    const u32 warp = threadIdx.x / 32, lane = threadIdx.x % 32;
-    if (warp == 0) tc::tmem_alloc(&tmem_base, tcols);
-    for (u32 e = threadIdx.x; e < 128 * K; e += blockDim.x)
-        *(__nv_bfloat16 *)(sA + tc::kmajor_offset(e / K, e % K, K)) = A[e];
-    for (u32 e = threadIdx.x; e < N * K; e += blockDim.x)
-        *(__nv_bfloat16 *)(sB + tc::kmajor_offset(e / K, e % K, K)) = B[e];
-    tc::fence_smem_to_async();
-    if (threadIdx.x == 0) tc::mbar_init(&bar, 1);
-    tc::fence_before_sync();
-    __syncthreads();
-    tc::fence_after_sync();
-    const u32 tmem = tmem_base;
-    if (threadIdx.x == 0) {
-        const u32 idesc = tc::idesc_bf16_f32(128, N);
-        const u32 sbo = (K / 8) * 128;
-        for (u32 s = 0; s < K / 16; s++)
-            tc::mma_bf16(tmem, tc::smem_desc(sA + s * 256, 128, sbo), tc::smem_desc(sB + s * 256, 128, sbo), idesc,
-                         s > 0);
-        tc::mma_commit(&bar);
-    }
-    const bool ok = __all_sync(0xFFFFFFFFu, tc::mbar_wait(&bar, 0, WAIT_LIMIT));
-    if (!ok && lane == 0) atomicOr(err, 4u);
-    tc::fence_after_sync();
-    if (ok) {
-        const u32 row = warp * 32 + lane;
-        for (u32 c0 = 0; c0 < N; c0 += 16) {
-            u32 r[16];
-            tc::tmem_ld16(tmem + ((warp * 32) << 16) + c0, r);
-            tc::tmem_wait_ld();
-#pragma unroll
-            for (int j = 0; j < 16; j++) D[row * N + c0 + j] = __uint_as_float(r[j]);
-        }
-    } else {
-        // give the MMAs one more bounded chance to finish before freeing their tensor memory
-        tc::mbar_wait(&bar, 0, WAIT_LIMIT);
-    }
-    tc::fence_before_sync();
-    __syncthreads();
-    if (warp == 0) tc::tmem_dealloc(tmem, tcols);
-}
-
 }  // namespace
-
-extern "C" int qmc_tc_mma_probe(const void *A, const void *B, float *D, uint32_t N, uint32_t K, qmc_stream_t s)
-{
-    QMC_REQUIRE(A && B && D, "null pointer");
-    QMC_REQUIRE(N >= 16 && N <= 256 && N % 16 == 0 && K >= 16 && K <= 256 && K % 16 == 0,
-                "probe shape: N in [16,256] and K in [16,256], multiples of 16");
-    unsigned *err = qmcgb::device_error_ptr();
-    QMC_REQUIRE(err, "device error word unavailable");
-    u32 tcols = 32;
-    while (tcols < N) tcols <<= 1;
-    const size_t smem = (size_t)(128 + N) * K * 2;
-    if (int rc = qmcgb::raise_smem_limit((const void *)tc_probe_kernel, smem, "tc probe smem")) return rc;
-    tc_probe_kernel<<<1, 128, smem, QMC_STREAM(s)>>>((const __nv_bfloat16 *)A, (const __nv_bfloat16 *)B, D, N, K,
-                                                     tcols, err);
-    return qmcgb::launch_status("tc_probe_kernel");
-}
 
 // ===========================================================================
 // Tensor-core FFT / inverse FFT / Walsh-Hadamard transform.

@@ -212,7 +212,7 @@ or pageable memory through the host's page tables), else copied back."""
         i64 = torch.int64
         dstate = torch.from_numpy(states.reshape(-1).view(np.int64)).to(dev)
         if dxb is None:
-            dxb = torch.from_numpy(hxb.reshape(-1)[:r_x * n * d].view(np.int64)).to(dev) if n else \
+            dxb = torch.from_numpy(_ffi.writable(hxb.reshape(-1)[:r_x * n * d].view(np.int64))).to(dev) if n else \
                 torch.empty(1, dtype=i64, device=dev)
         xrb_ptr = None
         if dxrb is None and n:
@@ -301,7 +301,7 @@ def _gdn_fresh(r, n, d, r_x, r_b, tmax, tmax_new, states, bases_np, xdig, xrdig,
         i64 = torch.int64
         dbases = torch.from_numpy(bases_np.view(np.int64)).to(dev)
         if dxd is None:
-            dxd = torch.from_numpy(hxd.reshape(-1)[:r_x * n * d * tmax].view(np.int64)).to(dev) if n else \
+            dxd = torch.from_numpy(_ffi.writable(hxd.reshape(-1)[:r_x * n * d * tmax].view(np.int64))).to(dev) if n else \
                 torch.empty(1, dtype=i64, device=dev)
         if dxr is None:
             dxr = torch.empty(max(r * n * d * tmax_new, 1), dtype=i64, device=dev)

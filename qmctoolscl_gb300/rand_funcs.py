@@ -7,7 +7,7 @@ with the same calls, shapes, bounds and dtypes, in the same order, as the
 reference helper of the same name: given a Generator in the same state they
 return identical arrays (checked against fixtures recorded from the
 reference).  The nested-uniform-scrambling routines of the reference
-(rand_funcs.py:155-356) are not part of this package.
+(rand_funcs.py:155-356) run on the GPU and live in nus.py.
 """
 import numpy as np
 

@@ -41,6 +41,8 @@ def _device_arrays(torch, arrays, count):
         else:
             if a.dtype != np.float64 or not a.flags["C_CONTIGUOUS"] or a.size < count:
                 raise ValueError("need C-contiguous float64 arrays of %d elements" % count)
+            if not a.flags["WRITEABLE"]:
+                raise ValueError("the transforms work in place: a read-only array cannot take the result")
             t = torch.from_numpy(a.reshape(-1)[:count]).cuda()
             devs.append(t)
             back.append((a, t))
@@ -70,7 +72,8 @@ def fft_mul_ifft_tc(d1, d2, n_half, lam_r, lam_i, xr, xi, divide=False, scale=1.
     with torch.cuda.stream(s):  # every copy in on the call's stream, ahead of the kernels
         lam = []
         for a in (lam_r, lam_i):
-            t = a if isinstance(a, torch.Tensor) else torch.from_numpy(np.ascontiguousarray(a, dtype=np.float64))
+            t = a if isinstance(a, torch.Tensor) else \
+                torch.from_numpy(_ffi.writable(np.ascontiguousarray(a, dtype=np.float64)))
             t = t.to(device="cuda", dtype=torch.float64).contiguous().reshape(-1)
             if t.numel() not in (n, count):
                 raise ValueError("lam needs n = %d or d1*d2*n = %d values" % (n, count))

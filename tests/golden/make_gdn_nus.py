@@ -1,6 +1,6 @@
 """Golden vectors for gdn_nested_uniform_scramble
 (qmctoolscl/rand_funcs.py:255-356) from the reference's own Python code,
-imported from a QMCToolsCL checkout (default /root/reference).
+imported from a QMCToolsCL checkout (--ref, or $QMCTOOLSCL_REF).
 
     python tests/golden/make_gdn_nus.py [--ref /path/to/QMCToolsCL]
 
@@ -67,7 +67,9 @@ def natural_digits(r_x, n, d, r_b, tmax, bases):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    env_ref = os.environ.get("QMCTOOLSCL_REF")
+    ap.add_argument("--ref", default=env_ref, required=env_ref is None,
+                    help="QMCToolsCL checkout (default: $QMCTOOLSCL_REF)")
     a = ap.parse_args()
     rf = load_ref_rand_funcs(a.ref)
     rng = np.random.Generator(np.random.SFC64(41))

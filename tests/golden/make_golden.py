@@ -1,6 +1,6 @@
 """Generate the golden fixtures from the QMCToolsCL reference itself.
 
-Run in a checkout that has the reference sources (default /root/reference):
+Run in a checkout that has the reference sources (--ref, or $QMCTOOLSCL_REF):
 
     python tests/golden/make_golden.py [--ref /path/to/QMCToolsCL]
 
@@ -344,9 +344,11 @@ def rand_cases(rf):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    env_ref = os.environ.get("QMCTOOLSCL_REF")
+    ap.add_argument("--ref", default=env_ref, required=env_ref is None,
+                    help="QMCToolsCL checkout (default: $QMCTOOLSCL_REF)")
     a = ap.parse_args()
-    oracle.build(ref=True)
+    oracle.build(ref=True, ref_dir=a.ref)
     rf = load_ref_rand_funcs(a.ref)
     rec = Recorder()
     replay_doctests(a.ref, make_shim(rec, rf, ref_docstrings(a.ref)))

@@ -65,6 +65,24 @@ def test_argument_errors_need_no_gpu(lib):
     assert rc == _ffi.QMC_ERR_DOMAIN
 
 
+def test_no_alloc_scratch_limit_holds_when_sizes_would_wrap(lib):
+    """qmc_net_gen_noalloc bounds r*d*mmax factor by factor: sizes whose
+    64-bit product wraps to 0 (r = 2^34, d = 2^30, mmax = 1) are refused on
+    the host like any request above the fixed scratch, before any CUDA call
+    and without touching the (fake) array pointers."""
+    from qmctoolscl_gb300 import _ffi, batch
+    L = _ffi.lib()
+    L.qmc_net_gen_noalloc.argtypes = [ctypes.POINTER(batch.NetRequest), ctypes.c_void_p]
+    L.qmc_net_gen_noalloc.restype = ctypes.c_int
+    fake = 0x1000
+    for r, d, alpha in ((1 << 34, 1 << 30, 1), (1, 1 << 63, 2)):
+        req = batch.NetRequest(r=r, n=2, d=d, n_start=0, mmax=1, d_pre=(d * alpha) % (1 << 64), alpha=alpha, tmax=1,
+                               tmax_new=1, tmax_alpha=1, r_C=1, gray=0, C=fake, S=fake, lshifts=None, shifts=None,
+                               tmaxes=None, xb=fake, x=None)
+        assert L.qmc_net_gen_noalloc(ctypes.byref(req), None) == _ffi.QMC_ERR_ARG
+    assert b"131072" in L.qmc_last_error() or b"d_pre" in L.qmc_last_error()
+
+
 def test_generalized_net_plan_argument_errors_need_no_gpu(lib):
     """qmc_halton_plan_create validates every dimension on the host, before
     any allocation; the array pointers are never dereferenced there."""
@@ -99,8 +117,8 @@ def test_generalized_net_plan_argument_errors_need_no_gpu(lib):
 
 def test_header_compiles_as_c_and_links(lib, tmp_path):
     """include/qmcgb.h is plain C (C99) and a C caller links libqmcgb.so and
-    calls it (version, last error, an argument error), as INTEGRATION.md's C
-    section shows -- no GPU needed."""
+    calls it (version, last error, an argument error), as a C integrator
+    would -- no GPU needed."""
     import shutil
     import subprocess
     cc = shutil.which("gcc") or shutil.which("cc")

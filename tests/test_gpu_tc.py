@@ -1,28 +1,46 @@
 """The tcgen05 (fifth-generation tensor core) building blocks: a one-CTA
 BF16 x BF16 -> FP32 MMA through tensor memory, with the shared-memory and
 instruction descriptors the tensor-core transforms use, against an exact
-host product (small integers are exact in BF16 and in the FP32 sums)."""
+host product (small integers are exact in BF16 and in the FP32 sums); then
+the tensor-core transforms against numpy."""
 import ctypes
+import os
+import subprocess
 
 import numpy as np
 import pytest
 
-from qmctoolscl_gb300 import _ffi
+from qmctoolscl_gb300 import _build, _ffi
 
 pytestmark = pytest.mark.gpu
 
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+
+@pytest.fixture(scope="module")
+def probe(tmp_path_factory):
+    """tests/cuda/tc_probe.cu built as a test-only library (it is not part of libqmcgb.so)."""
+    so = str(tmp_path_factory.mktemp("tcprobe") / "libtcprobe.so")
+    subprocess.run([_build.nvcc()] + _build.ARCH + ["-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-shared", "-o", so,
+                                                    os.path.join(HERE, "cuda", "tc_probe.cu")], check=True)
+    L = ctypes.CDLL(so)
+    L.tc_mma_probe.argtypes = [ctypes.c_void_p] * 3 + [ctypes.c_uint32] * 2 + [ctypes.c_void_p] * 2
+    L.tc_mma_probe.restype = ctypes.c_int
+    return L
+
 
 @pytest.mark.parametrize("N,K", [(16, 16), (32, 16), (32, 64), (64, 32), (128, 128), (256, 16), (32, 192)])
-def test_tcgen05_mma_probe_exact(N, K):
+def test_tcgen05_mma_probe_exact(probe, N, K):
     import torch
     g = torch.Generator().manual_seed(N * 1000 + K)
     A = torch.randint(-8, 9, (128, K), generator=g).to(torch.bfloat16).cuda()
     B = torch.randint(-8, 9, (N, K), generator=g).to(torch.bfloat16).cuda()
     D = torch.full((128, N), float("nan"), dtype=torch.float32, device="cuda")
-    L = _ffi.lib()
+    err = torch.zeros(1, dtype=torch.int32, device="cuda")
     s = torch.cuda.current_stream().cuda_stream
-    _ffi.check(L.qmc_tc_mma_probe(A.data_ptr(), B.data_ptr(), D.data_ptr(), N, K, s), "tc_mma_probe")
-    _ffi.check(L.qmc_device_error_check(ctypes.c_void_p(s)), "tc_mma_probe wait")
+    assert probe.tc_mma_probe(A.data_ptr(), B.data_ptr(), D.data_ptr(), N, K, err.data_ptr(), s) == 0
+    torch.cuda.synchronize()
+    assert int(err.item()) == 0, "the probe's completion wait ran out"
     want = A.double() @ B.double().T
     assert torch.equal(D.double(), want)
 
