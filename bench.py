@@ -109,6 +109,33 @@ def cpu_baseline(g, shifts):
             "seconds": t, "cpu_seconds": t * threads}
 
 
+AS_SHIPPED_LOG2N = 16
+
+
+def cpu_as_shipped(g, shifts):
+    """The reference as its users run it today: one call per function, the
+    whole r on one host thread (its C loops are serial), timed with
+    perf_counter around each call as qmctoolscl/util.py:104-114 times it.
+    Run on the first 2^16 rows (1/16 of the workload) and reported per point:
+    the loops are linear in n."""
+    import oracle
+    U = np.uint64
+    n = 1 << AS_SHIPPED_LOG2N
+    x, xr = np.empty((R, n, D)), np.empty((R, n, D))
+    oracle.call("lat_gen_gray", U(R), U(1 << 10), U(D), U(0), g, x)  # untimed: loads the library
+    t0 = time.perf_counter()
+    oracle.call("lat_gen_gray", U(R), U(n), U(D), U(0), g, x)
+    t1 = time.perf_counter()
+    oracle.call("lat_shift_mod_1", U(R), U(n), U(D), U(R), x, shifts, xr)
+    t2 = time.perf_counter()
+    return {"value": R * n / (t2 - t0), "unit": "points/s", "cores": 1, "kind": "port",
+            "sample": "r=16, n=2^%d, d=64 (1/16 of the rows; per-point rate, the loops are linear in n): "
+                      "lat_gen_gray then lat_shift_mod_1, one oracle call each over all r on one thread, "
+                      "timed per call like qmctoolscl/util.py:104-114" % AS_SHIPPED_LOG2N,
+            "seconds_per_call": {"lat_gen_gray": t1 - t0, "lat_shift_mod_1": t2 - t1},
+            "extrapolated_full_step_s": (t2 - t0) * (1 << (LOG2N - AS_SHIPPED_LOG2N))}
+
+
 # ---------------------------------------------------------------- clocks
 
 class ClockSampler:
@@ -179,6 +206,35 @@ def measured_peak():
         return float(pk["hbm_gbs"]), "measured (MEASURED_PEAKS.json hbm_gbs)"
     except (OSError, KeyError, ValueError):
         return FALLBACK_HBM_GBS, "fallback 6.8 TB/s"
+
+
+def profiled_value(name, key):
+    """The number after `key:` in the committed ncu summary profiles/<name>, or None."""
+    path = os.path.join(HERE, "profiles", name)
+    try:
+        with open(path) as f:
+            for ln in f:
+                if ln.startswith(key + ":"):
+                    return float(ln.split(":", 1)[1].split()[0])
+    except (OSError, ValueError):
+        pass
+    return None
+
+
+SMS = 152
+FP64_LANES_PER_SM_CLK = 2  # GB300: 1.25 TFLOP/s FP64 = 2 FMA lanes per SM per clock at 2.07 GHz
+
+
+def fp64_roofline(warp_inst, ms, sm_mhz):
+    """Fraction of the FP64 pipe's issue rate: warp-level FP64 instructions
+    (32 lanes each) against SMs x 2 lanes per clock at the sampled SM clock."""
+    if warp_inst is None or not sm_mhz:
+        return None
+    lane_ops = 32.0 * warp_inst
+    peak = SMS * FP64_LANES_PER_SM_CLK * sm_mhz * 1e6
+    ach = lane_ops / (ms / 1e3)
+    return {"bound": "fp64", "achieved": ach / 1e12, "peak": peak / 1e12, "unit": "T FP64 lane-ops/s",
+            "frac": ach / peak, "fp64_warp_inst_per_launch": warp_inst, "sm_mhz": sm_mhz}
 
 
 def profiled_traffic(name):
@@ -309,7 +365,7 @@ def run_ours(args):
         if rank == 0:
             print(json.dumps({"small": True, "n": n, "ms_per_step": ms_fused_max,
                               "gbs": 8.0 * R * n * D / (ms_fused_max / 1e3) / 1e9}), flush=True)
-        return
+        return None
 
     # plain: the reference's two calls as two launches
     x_d = torch.empty((R, n, D), dtype=torch.float64, device=dev)
@@ -374,9 +430,13 @@ def run_ours(args):
     e2e_line["link"] = {"d2h_copy_ms": 1e3 * t_link, "d2h_gbs": link_gbs,
                         "e2e_d2h_gbs": e2e_line["d2h_bytes_per_step"] / (e2e_line["ms_per_step"] / 1e3) / 1e9,
                         "note": "plain device-to-host copy of the same result into the same pinned array"}
+    del xr_t, xr_host
+    # what a reference user's code does unchanged: lat_gen_gray then lat_shift_mod_1 through
+    # the drop-in API with numpy arrays (pageable), every array copied in and out by each call
+    e2e_line["other"]["drop_in"] = drop_in_e2e(g, shifts, n, xr_sample, world)
 
     if rank != 0:
-        return
+        return None
     points = R * n
     value = world * points / (ms_fused_max / 1e3)
     peak, peak_src = measured_peak()
@@ -404,8 +464,37 @@ def run_ours(args):
         "gpu_launches": args.steps,
         "clocks": clk,
         "cpu_baseline": cpu_baseline(g, shifts),
+        "cpu_as_shipped": cpu_as_shipped(g, shifts),
     }
-    print(json.dumps(line), flush=True)
+    return line
+
+
+def drop_in_e2e(g, shifts, n, xr_sample, world):
+    """lat_gen_gray then lat_shift_mod_1 through qmctoolscl_gb300's drop-in
+    functions with numpy arrays, as the reference's documented use calls them;
+    each call copies its inputs to the GPU and its outputs back (8 GiB out of
+    lat_gen_gray, 8 GiB in and 8 GiB out of lat_shift_mod_1)."""
+    import torch
+    import qmctoolscl_gb300 as q
+    U = np.uint64
+    x, xr = np.empty((R, n, D)), np.empty((R, n, D))
+    x[:] = 0.0  # touch the pages outside the timed region, as a caller's reused arrays are
+    xr[:] = 0.0
+    q.lat_gen_gray(U(R), U(n), U(D), U(0), g, x)  # warm-up
+    steps = 2
+    torch.cuda.synchronize()
+    barrier(world)
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        q.lat_gen_gray(U(R), U(n), U(D), U(0), g, x)
+        q.lat_shift_mod_1(U(R), U(n), U(D), U(R), x, shifts, xr)
+    t = max_over_ranks((time.perf_counter() - t0) / steps, world)
+    assert np.array_equal(xr[:, :1 << 10].view(U), xr_sample.view(U)), "drop-in calls differ from the oracle"
+    nb = 8 * R * n * D
+    return {"value": world * R * n / t, "unit": "points/s", "ms_per_step": 1e3 * t, "steps": steps,
+            "h2d_bytes_per_step": g.nbytes + shifts.nbytes + nb, "d2h_bytes_per_step": 2 * nb,
+            "path": "qmctoolscl_gb300.lat_gen_gray then qmctoolscl_gb300.lat_shift_mod_1, numpy arrays in "
+                    "pageable memory, copies inside each call"}
 
 
 # ---------------------------------------------------------------- other configurations
@@ -521,7 +610,9 @@ def run_net_plain(args):
             "scaling": "weak", "vs_baseline": None, "dtype": "u64+f64", "data": "synthetic (np.random.SFC64(1))",
             "config": {"workload": "base-2 digital net, natural order + digital shift + float, r=1, d=16, m=16 "
                                    "(n=65536), tmax=63 (fused kernel, both outputs)", "r": r, "n": n, "d": d},
-            "roofline": roofline(16.0 * r * n * d, ms_fused),
+            "roofline": dict(roofline(16.0 * r * n * d, ms_fused), kernel="dnb2_gen_kernel (fused shift + float)",
+                             note="16.8 MB per launch: launch-latency bound, below the HBM ramp; the output fits "
+                                  "in the 129 MB L2, so one launch's DRAM bytes do not measure it (traffic null)"),
             "plain": {"ms_per_step": ms_plain, "points_per_s": pts / (ms_plain / 1e3), "launches_per_step": 3,
                       "fused_speedup": ms_plain / ms_fused},
             "e2e": {"value": pts / t_e2e, "unit": "points/s", "ms_per_step": 1e3 * t_e2e,
@@ -656,7 +747,10 @@ def run_net_lms(args):
             "config": {"workload": "base-2 net LMS + interlacing (alpha=2) + natural order + digital shift, r=64, "
                                    "d_pre=64 -> d=32, m=20 (n=2^20), tmax=64 (batched plan, graph replay)",
                        "r": r, "n": n, "d": d},
-            "roofline": roofline(8.0 * r * n * d, ms_graph),
+            "roofline": dict(roofline(8.0 * r * n * d, ms_graph), kernel="net_batch_kernel (graph replay)",
+                             traffic=(lambda t: None if t is None else t * r / 8.0)(
+                                 profiled_traffic("net_batch_kernel_lms_interlace_shift_r8_n2p20_d32.md")),
+                             traffic_note="ncu DRAM bytes of the r=8 capture, scaled by r/8 (the coordinates)"),
             "batched_uniform": {"plan_ms": ms_plan, "graph_ms": ms_graph, "plain_ms": ms_plain,
                                 "plain_launches": 4, "speedup_vs_plain": ms_plain / ms_graph},
             "uneven_batch": {"requests": 256, "points": total_pts, "coords": total_coords,
@@ -910,9 +1004,9 @@ def run_halton(args):
         sweep[share] = gpu_ms(lambda: plan.run(st), 3, 1, st)
     best_share = min(sweep, key=sweep.get)
     plan.set_fp64_share(best_share)
-    ms_gen = gpu_ms(lambda: plan.run(st), args.steps, args.warmup, st)
     clocks = ClockSampler(0)
     clocks.start()
+    ms_gen = gpu_ms(lambda: plan.run(st), max(args.steps, 10), args.warmup, st)
     ms_fused = gpu_ms(fused, args.steps, args.warmup, st)
     clk = clocks.stop()
     _ffi.check(lib.qmc_device_error_check(h), "halton plan")
@@ -1013,6 +1107,7 @@ def run_halton(args):
     cpu_pts = sum(p[2] for p in pieces)
     pts = r * n
     alg = 8.0 * r * n * d
+    fp64_r8 = profiled_value("halton_gen_kernel_r32_n2p18_d100.md", "fp64_warp_inst_per_launch_r8")
     return {"metric": METRIC, "value": pts / (ms_fused / 1e3), "unit": "points/s", "n_gpus": 1,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_fused, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "u32 digits, f64 adds (split FP64 unit / integer by the tuned share)",
@@ -1025,6 +1120,11 @@ def run_halton(args):
                              traffic=profiled_traffic("halton_gen_kernel_r32_n2p18_d100.md"),
                              note="generation kernel alone; bound by the FP64 unit's digit adds (one per digit, "
                                   "the FP64 pipe about 70 % busy in the ncu capture) and integer issue, not HBM"),
+            "fp64_roofline": dict(fp64_roofline(
+                None if fp64_r8 is None else fp64_r8 * r / 8.0, ms_gen, clk.get("sm_mhz")) or {},
+                note="generation kernel against the FP64 pipe's issue rate (2 lanes per SM per clock at the median "
+                     "SM clock sampled while timing); executed FP64 instructions from the ncu capture of the r=8 case "
+                     "in profiles/halton_gen_kernel_r32_n2p18_d100.md, scaled by r/8"),
             "generate_only_ms": ms_gen,
             "uneven_batch": {"requests": 64, "points": upoints, "coords": ucoords, "graph_ms": ms_u_graph,
                              "per_request_plans_ms": ms_u_single, "speedup": ms_u_single / ms_u_graph,
@@ -1430,18 +1530,53 @@ def run_gdn_nus(args):
             "config": {"workload": "gdn_nested_uniform_scramble, r=%d, n=2^%d, d=8 (first 8 primes), tmax=16, "
                                    "tmax_new=20, fresh trees" % (r, m), "r": r, "n": n, "d": d},
             "roofline": dict(roofline(8.0 * (n * d * tmax + pts * tmax_new), ms), kernel="the whole pipeline",
-                             note="bound by the serial permutation draws: per generator numpy's Fisher-Yates "
-                                  "(b-1 masked draws per level) for every level below each point's branch, "
-                                  "one thread per generator; achieved counts only the digit I/O"),
+                             note="bound by the serial SFC64 stream per generator (numpy's masked draws for "
+                                  "b-1 swap indices per level, for every level below each point's branch, one "
+                                  "thread per generator); the swaps themselves run one thread per permutation; "
+                                  "achieved counts only the digit I/O"),
             "e2e": {"value": pts / t_e2e, "unit": "points/s", "seconds_per_call": t_e2e,
                     "h2d_bytes_per_step": int(8 * n * d * tmax + 48 * G),
                     "d2h_bytes_per_step": int(8 * pts * tmax_new + 48 * G),
                     "path": "qmctoolscl_gb300.gdn_nested_uniform_scramble with numpy arrays and Generators"},
-            "gpu_launches": args.steps * (8 + 3 * min(8, (n.bit_length() + 4 + 7) // 8)),  # one chunk
+            "gpu_launches": args.steps * (10 + 3 * min(8, (n.bit_length() + 4 + 7) // 8)),  # one chunk
             "cpu_baseline": {"value": gs * n / t_cpu, "unit": "points/s", "cores": threads, "kind": "port",
                              "sample": "%d whole generators (2^%d points each, bases 2..19), one per thread, by the "
                                        "oracle (C restatement of the reference's tree walk)" % (gs, m),
                              "seconds": t_cpu}}
+
+
+# the default run's "configs" object: every other configuration of the benchmark, each its own
+# workload function (the same as --workload <name>), with at most this many timed steps
+CONFIGS = [("cfg1_net_plain", "net_plain", 10), ("cfg3_net_lms", "net_lms", 10), ("cfg4_halton", "halton", 10),
+           ("cfg5_fft", "fft", 10), ("plain_drop_in", "plain", 10), ("halton_qrng", "qrng", 10),
+           ("nus_base2", "nus", 3), ("nus_base_b", "gdn_nus", 3)]
+_REPEATED = ("metric", "n_gpus", "higher_is_better", "scaling", "vs_baseline")
+
+
+def run_configs(args):
+    """Each configuration in CONFIGS on this GPU, one after another, freeing its
+    device and pinned memory before the next; an entry holds its workload's
+    line (without the keys the headline line already states) and its wall
+    time, or the error that stopped it."""
+    import copy
+    import gc
+    import torch
+    out = {}
+    for key, name, max_steps in CONFIGS:
+        a = copy.copy(args)
+        a.steps = max(1, min(args.steps, max_steps))
+        t0 = time.perf_counter()
+        try:
+            entry = {k: v for k, v in WORKLOADS[name](a).items() if k not in _REPEATED}
+        except Exception as e:  # a failing configuration is reported in its entry, the others still run
+            entry = {"error": "%s: %s" % (type(e).__name__, e)}
+        entry["workload_flag"] = "--workload " + name
+        entry["wall_s"] = time.perf_counter() - t0
+        out[key] = entry
+        gc.collect()
+        torch.cuda.synchronize()
+        torch.cuda.empty_cache()
+    return out
 
 
 WORKLOADS = {"net_plain": run_net_plain, "net_lms": run_net_lms, "fft": run_fft, "halton": run_halton,
@@ -1457,6 +1592,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="lattice", choices=["lattice"] + sorted(WORKLOADS),
                     help="lattice (default): the headline configuration; the others print their own line")
+    ap.add_argument("--no-configs", action="store_true",
+                    help="default workload only: leave out the other configurations' entries")
     ap.add_argument("--small", action="store_true",
                     help="profiling mode: the fused kernel only, on n=2^%d (512 MiB output)" % PROFILE_LOG2N)
     args = ap.parse_args()
@@ -1469,7 +1606,11 @@ def main():
         torch.cuda.set_device(0)
         print(json.dumps(WORKLOADS[args.workload](args)), flush=True)
     else:
-        run_ours(args)
+        line = run_ours(args)
+        if line is not None:  # rank 0
+            if line.get("n_gpus") == 1 and not args.small and not args.no_configs:
+                line["configs"] = run_configs(args)
+            print(json.dumps(line), flush=True)
 
 
 if __name__ == "__main__":
