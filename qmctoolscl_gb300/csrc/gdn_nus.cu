@@ -26,12 +26,15 @@
 // up its ancestors.
 #include "nus_dev.cuh"
 
+#include <vector>
+
 namespace {
 
 struct GdnArgs {
     const u64 *bases;
     u64 r_b;
     u32 tmax, tmax_new;
+    const u64 *hist_keys;  // (r*d, H0, 2) keys (high, low word) of the trees' earlier entries, or null
 };
 
 // base b and bits per digit w of generator s
@@ -55,7 +58,13 @@ __global__ void __launch_bounds__(NUS_THREADS) gdn_keys_kernel(NusDims m, GdnArg
     u32 b, w;
     gdn_base_of(m, a, s, b, w);
     u64 hi = 0, lo = 0;
-    if (v >= m.H0) {
+    if (v < m.H0) {  // an entry of an earlier call (the phantom root is entry 0, key 0)
+        if (a.hist_keys) {
+            const u64 *hk = a.hist_keys + (s * m.H0 + v) * 2;
+            hi = hk[0];
+            lo = hk[1];
+        }
+    } else {
         if ((u64)a.tmax * w > 128 || b == 0 || b > 65536) atomicOr(err, 1u);
         const u64 l = s / m.d, j = s - l * m.d, i = v - m.H0;
         const u64 *x = xdig + (((l % m.r_x) * m.n + i) * m.d + j) * a.tmax;
@@ -78,6 +87,19 @@ __global__ void __launch_bounds__(NUS_THREADS) gdn_keys_kernel(NusDims m, GdnArg
     key[off + v] = hi;
     khi_idx[off + v] = hi;
     klo_idx[off + v] = lo;
+}
+
+// every entry's key (point order) for a later call on the same trees
+__global__ void __launch_bounds__(NUS_THREADS) gdn_keys_out_kernel(NusDims m, const u64 *__restrict__ khi_idx,
+                                                                   const u64 *__restrict__ klo_idx,
+                                                                   u64 *__restrict__ keys_out)
+{
+    const u32 v = blockIdx.x * NUS_THREADS + threadIdx.x, g = blockIdx.y;
+    if (v >= m.N) return;
+    const u64 off = (u64)g * m.NP;
+    u64 *o = keys_out + ((m.s0 + g) * m.N + v) * 2;
+    o[0] = khi_idx[off + v];
+    o[1] = klo_idx[off + v];
 }
 
 // ---- sort finish: runs equal in the sorted top bits, by the full 128-bit key ----------
@@ -210,68 +232,120 @@ __global__ void __launch_bounds__(1024) gdn_offsets_kernel(NusDims m, GdnArgs a,
     if (threadIdx.x == 1023) tot[g] = run;
 }
 
-// the chunk's generators one after another: a base per generator, the total in *total
-__global__ void gdn_bases_kernel(u32 S, const u64 *__restrict__ tot, u64 *__restrict__ base, u64 *total)
+// the chunk's generators one after another: a base per generator; the total
+// in ctl[0] and the most permutation rows of any generator in ctl[1]
+__global__ void gdn_bases_kernel(NusDims m, GdnArgs a, const u64 *__restrict__ tot, u64 *__restrict__ base, u64 *ctl)
 {
     if (threadIdx.x != 0 || blockIdx.x != 0) return;
-    u64 run = 0;
-    for (u32 g = 0; g < S; g++) {
+    u64 run = 0, most = 0;
+    for (u32 g = 0; g < m.S; g++) {
+        u32 b, w;
+        gdn_base_of(m, a, m.s0 + g, b, w);
         base[g] = run;
         run += tot[g];
+        const u64 rows = b ? tot[g] / b : 0;
+        most = rows > most ? rows : most;
     }
-    *total = run;
+    ctl[0] = run;
+    ctl[1] = most;
 }
 
-// ---- the draws: Generator.permutation(b) per level, one thread per generator ---------
-// numpy's Generator.shuffle walks i = b-1 .. 1 and swaps with random_interval(i):
-// a value masked to the bits of i, drawn again while above i (32-bit draws).
+// permutation entries of generator g that earlier calls drew (its entries
+// below H0); none for fresh trees, where the phantom root draws here
+__device__ __forceinline__ u64 old_entries(const NusDims &m, const u64 *offs, const u64 *tot, u32 g)
+{
+    if (m.fresh) return 0;
+    return m.H0 < m.N ? offs[(u64)g * m.NP + m.H0] : tot[g];
+}
+
+// the rows of the trees' earlier entries, copied in front of this call's
+// rows; a history whose length disagrees with the entries' levels sets bit 64
+// of the device error word and copies nothing
+__global__ void __launch_bounds__(NUS_THREADS) gdn_hist_rows_kernel(NusDims m, const u64 *__restrict__ offs,
+                                                                    const u64 *__restrict__ tot,
+                                                                    const u64 *__restrict__ base,
+                                                                    const unsigned short *__restrict__ hist_perms,
+                                                                    const u64 *__restrict__ hist_off,
+                                                                    unsigned short *__restrict__ perms,
+                                                                    unsigned int *err)
+{
+    const u32 g = blockIdx.y;
+    const u64 s = m.s0 + g, beg = hist_off[s], len = hist_off[s + 1] - beg;
+    if (len != old_entries(m, offs, tot, g)) {
+        if (blockIdx.x == 0 && threadIdx.x == 0) atomicOr(err, 64u);
+        return;
+    }
+    unsigned short *dst = perms + base[g];
+    for (u64 e = (u64)blockIdx.x * NUS_THREADS + threadIdx.x; e < len; e += (u64)gridDim.x * NUS_THREADS)
+        dst[e] = hist_perms[beg + e];
+}
+
+// ---- the draws: Generator.permutation(b) per level ---------------------------------
+// numpy's Generator.shuffle walks i = b-1 .. 1 and swaps position i with
+// random_interval(i): a 32-bit draw masked to the bits of i, drawn again
+// while above i.  The stream is serial per generator, the swaps are not: one
+// thread per generator runs the stream and writes each accepted index j_i
+// into entry i of its row (rows in draw order: the phantom's, then each
+// point's levels, as the offsets lay them out); then one thread per row
+// replays the swaps on arange(b) in shared memory and writes the permutation
+// over the indices.
 
 constexpr int INTERVAL_TRIES = 256;  // each try fails with probability below 1/2
 
-__global__ void __launch_bounds__(32) gdn_draw_kernel(NusDims m, GdnArgs a, u64 *__restrict__ states,
-                                                      const unsigned char *__restrict__ Lv,
-                                                      const u64 *__restrict__ offs, const u64 *__restrict__ base,
-                                                      unsigned short *__restrict__ perms, unsigned int *err)
+__global__ void __launch_bounds__(32) gdn_stream_kernel(NusDims m, GdnArgs a, u64 *__restrict__ states,
+                                                        const u64 *__restrict__ offs, const u64 *__restrict__ tot,
+                                                        const u64 *__restrict__ base,
+                                                        unsigned short *__restrict__ perms, unsigned int *err)
 {
-    const u32 g = blockIdx.x * blockDim.x + threadIdx.x;
-    if (g >= m.S) return;
+    const u32 g = blockIdx.x;
+    if (threadIdx.x != 0 || g >= m.S) return;
     u64 *st = states + (m.s0 + g) * 6;
     Sfc64 r{st[0], st[1], st[2], st[3], st[5], (u32)(st[4] != 0)};
     u32 b, w;
     gdn_base_of(m, a, m.s0 + g, b, w);
-    if (b == 0 || b > 65536) {  // reported by the keys pass; nothing to draw from
+    if (b < 2 || b > 65536) {  // reported by the keys pass; nothing to draw from
         atomicOr(err, 1u);
         return;
     }
-    const u64 off = (u64)g * m.NP;
+    const u64 rows = tot[g] / b;
+    u64 q = old_entries(m, offs, tot, g) / b;  // rows before q came from earlier calls
+    unsigned short *row = perms + base[g] + q * b;
+    u32 i = b - 1, mask = 0xFFFFFFFFu >> __clz((int)i), fails = 0;
     bool ok = true;
-    for (u32 v = 0; v < m.N; v++) {
-        const u32 lev = levels_of(v, Lv + off, w, a);
-        unsigned short *row = perms + base[g] + offs[off + v];
-        for (u32 k = 0; k < lev; k++, row += b) {
-            for (u32 q = 0; q < b; q++) row[q] = (unsigned short)q;
-            for (u32 i = b - 1; i >= 1; i--) {
-                u32 mask = i;
-                mask |= mask >> 1;
-                mask |= mask >> 2;
-                mask |= mask >> 4;
-                mask |= mask >> 8;
-                mask |= mask >> 16;
-                u32 jv = 0;
-                int tries = 0;
-                for (;; tries++) {
-                    jv = (u32)r.next32() & mask;
-                    if (jv <= i) break;
-                    if (tries >= INTERVAL_TRIES) {
-                        ok = false;
-                        jv = 0;
-                        break;
-                    }
-                }
-                const unsigned short t = row[i];
-                row[i] = row[jv];
-                row[jv] = t;
+    // one 32-bit candidate; true once the last row is complete
+    auto feed = [&](u32 x) -> bool {
+        u32 jv = x & mask;
+        bool acc = jv <= i;
+        if (!acc && ++fails > INTERVAL_TRIES) {  // a broken stream: record it, stay bounded
+            ok = false;
+            acc = true;
+            jv = 0;
+        }
+        if (!acc) return false;
+        fails = 0;
+        row[i] = (unsigned short)jv;
+        if (--i == 0) {
+            if (++q == rows) return true;
+            row += b;
+            i = b - 1;
+        }
+        mask = 0xFFFFFFFFu >> __clz((int)i);
+        return false;
+    };
+    if (q < rows) {
+        bool done = false;
+        if (r.has) {  // the buffered upper half of the last 64-bit output comes first
+            r.has = 0;
+            done = feed((u32)r.half);
+        }
+        while (!done) {
+            const u64 y = r.next64();
+            r.half = y >> 32;  // numpy keeps the high half in its buffer word even once it is used
+            if (feed((u32)y)) {
+                r.has = 1;
+                break;
             }
+            done = feed((u32)(y >> 32));
         }
     }
     if (!ok) atomicOr(err, 16u);
@@ -281,6 +355,32 @@ __global__ void __launch_bounds__(32) gdn_draw_kernel(NusDims m, GdnArgs a, u64 
     st[3] = r.w;
     st[4] = r.has;
     st[5] = r.half;
+}
+
+// rows of one generator per blockIdx.y; thread t of a block holds its row's
+// permutation in column t of a (b x T) shared-memory array, so that lanes
+// never meet in a bank (T a multiple of 64: entry k of lane t sits in word
+// (k*T + t)/2)
+__global__ void gdn_shuffle_kernel(NusDims m, GdnArgs a, const u64 *__restrict__ offs, const u64 *__restrict__ tot,
+                                   const u64 *__restrict__ base, unsigned short *__restrict__ perms)
+{
+    extern __shared__ unsigned short col[];
+    const u32 g = blockIdx.y, T = blockDim.x, t = threadIdx.x;
+    u32 b, w;
+    gdn_base_of(m, a, m.s0 + g, b, w);
+    if (b < 2 || b > 65536) return;  // reported by the keys pass
+    const u64 q = old_entries(m, offs, tot, g) / b + (u64)blockIdx.x * T + t;
+    if (q >= tot[g] / b) return;
+    unsigned short *row = perms + base[g] + q * b;
+    unsigned short *A = col + t;
+    for (u32 k = 0; k < b; k++) A[(u64)k * T] = (unsigned short)k;
+    for (u32 k = b - 1; k >= 1; k--) {
+        const u32 j = row[k];
+        const unsigned short x = A[(u64)k * T], y = A[(u64)j * T];
+        A[(u64)k * T] = y;
+        A[(u64)j * T] = x;
+    }
+    for (u32 k = 0; k < b; k++) row[k] = A[(u64)k * T];
 }
 
 // ---- output: each point's digits through its owners' permutations -------------------
@@ -387,10 +487,10 @@ u64 gdn_tiles(u64 N) { return (N + WT - 1) / WT; }
 
 extern "C" {
 
-int qmc_gdn_nus_workspace_size(uint64_t n, uint64_t generators, uint64_t *bytes)
+int qmc_gdn_nus_workspace_size(uint64_t n, uint64_t h0, uint64_t generators, uint64_t *bytes)
 {
     QMC_REQUIRE(bytes, "gdn_nus_workspace_size: null output pointer");
-    const u64 N = 1 + n;
+    const u64 N = (h0 ? h0 : 1) + n;
     QMC_REQUIRE(N < MAX_ENTRIES, "gdn_nested_uniform_scramble: %llu points per generator (at most 2^30 - 2)",
                 (unsigned long long)n);
     *bytes = gdn_layout(nullptr, generators ? generators : 1, gdn_padded(N), gdn_tiles(N)).bytes;
@@ -398,23 +498,27 @@ int qmc_gdn_nus_workspace_size(uint64_t n, uint64_t generators, uint64_t *bytes)
 }
 
 int qmc_gdn_nested_uniform_scramble(uint64_t r, uint64_t n, uint64_t d, uint64_t r_x, uint64_t r_b, uint64_t tmax,
-                                    uint64_t tmax_new, uint64_t *states, const uint64_t *bases,
-                                    const uint64_t *xdig, uint64_t *xrdig, uint16_t *perms, uint64_t perm_capacity,
+                                    uint64_t tmax_new, uint64_t *states, const uint64_t *bases, uint64_t h0,
+                                    const uint64_t *hist_keys, const uint16_t *hist_perms,
+                                    const uint64_t *hist_perm_off, const uint64_t *xdig, uint64_t *xrdig,
+                                    uint64_t *keys_out, uint16_t *perms, uint64_t perm_capacity, uint64_t *perm_off,
                                     uint64_t *perm_needed, void *work, uint64_t work_bytes, qmc_stream_t s)
 {
     if (perm_needed) *perm_needed = 0;
     if (r == 0 || d == 0) return QMC_OK;
     QMC_REQUIRE(r_x >= 1 && r_b >= 1, "gdn_nested_uniform_scramble: r_x or r_b = 0");
-    QMC_REQUIRE(states && work && bases && perms, "gdn_nested_uniform_scramble: null states, bases, "
-                "permutation buffer or workspace");
+    QMC_REQUIRE(states && work && bases && perms && perm_off, "gdn_nested_uniform_scramble: null states, bases, "
+                "permutation buffer, permutation offsets or workspace");
+    QMC_REQUIRE(h0 == 0 || (hist_keys && hist_perms && hist_perm_off),
+                "gdn_nested_uniform_scramble: h0 > 0 needs the trees' keys, permutations and offsets");
     QMC_REQUIRE(n == 0 || (xdig && xrdig), "gdn_nested_uniform_scramble: null xdig or xrdig");
     QMC_REQUIRE(tmax_new > tmax && tmax_new <= 255 && tmax >= 1,
                 "gdn_nested_uniform_scramble: needs 1 <= tmax < tmax_new <= 255 (tmax = %llu, tmax_new = %llu)",
                 (unsigned long long)tmax, (unsigned long long)tmax_new);
     QMC_REQUIRE(((uintptr_t)work & 255) == 0, "gdn_nested_uniform_scramble: workspace not 256-byte aligned");
-    const u64 N = 1 + n;
-    QMC_REQUIRE(N < MAX_ENTRIES, "gdn_nested_uniform_scramble: %llu points per generator (at most 2^30 - 2)",
-                (unsigned long long)n);
+    const u64 H0 = h0 ? h0 : 1, N = H0 + n;
+    QMC_REQUIRE(N < MAX_ENTRIES && N > n, "gdn_nested_uniform_scramble: %llu entries per generator (at most 2^30 - 1)",
+                (unsigned long long)N);
     const u64 NP = gdn_padded(N), NT = gdn_tiles(N), G = r * d;
     const u64 per = gdn_layout(nullptr, 1, NP, NT).bytes;
     QMC_REQUIRE(work_bytes >= per, "gdn_nested_uniform_scramble: workspace of %llu bytes, one generator needs %llu",
@@ -435,16 +539,36 @@ int qmc_gdn_nested_uniform_scramble(uint64_t r, uint64_t n, uint64_t d, uint64_t
     m.T = 255;  // the tree pass records bit-level prefix lengths as they are
     m.N = (u32)N;
     m.NP = (u32)NP;
-    m.H0 = 1;
+    m.H0 = (u32)H0;
     m.NT = (u32)NT;
-    m.fresh = 1;
-    GdnArgs a{(const u64 *)bases, r_b, (u32)tmax, (u32)tmax_new};
+    m.fresh = h0 == 0;
+    GdnArgs a{(const u64 *)bases, r_b, (u32)tmax, (u32)tmax_new, h0 ? (const u64 *)hist_keys : nullptr};
     const u64 *xd = (const u64 *)xdig;
     u64 *xr = (u64 *)xrdig;
     u64 *stw = (u64 *)states;
     unsigned short *pm = (unsigned short *)perms;
     const dim3 ng((unsigned)((N + NUS_THREADS - 1) / NUS_THREADS), 1);
-    u64 need_max = 0;
+    u64 filled = 0;       // permutation entries of the generators before this chunk
+    bool sizing = false;  // the buffer ran short: the remaining chunks only count their entries
+    std::vector<u64> tot_h(count);
+    perm_off[0] = 0;
+    // rows per block of the shuffle: b x T 16-bit entries in shared memory
+    u64 bmax = 2;
+    {
+        std::vector<u64> hb(r_b * d);
+        int rc = qmcgb::cuda_status(cudaMemcpyAsync(hb.data(), bases, r_b * d * 8, cudaMemcpyDefault, st),
+                                    "gdn_nus bases");
+        if (rc) return rc;
+        rc = qmcgb::cuda_status(cudaStreamSynchronize(st), "gdn_nus bases");
+        if (rc) return rc;
+        for (u64 v : hb) bmax = v > bmax ? v : bmax;
+    }
+    QMC_REQUIRE(bmax <= 65536, "gdn_nested_uniform_scramble: bases above 65536");
+    u32 shuffle_T = 128;
+    while (shuffle_T > 1 && (u64)shuffle_T * bmax * 2 > 98304) shuffle_T >>= 1;
+    const size_t shuffle_smem = (size_t)shuffle_T * bmax * 2;
+    if (int rc = qmcgb::raise_smem_limit((const void *)gdn_shuffle_kernel, shuffle_smem, "gdn_nus shuffle smem"))
+        return rc;
 
     for (u64 s0 = 0; s0 < G; s0 += count) {
         m.s0 = s0;
@@ -453,6 +577,11 @@ int qmc_gdn_nested_uniform_scramble(uint64_t r, uint64_t n, uint64_t d, uint64_t
         gdn_keys_kernel<<<gg, NUS_THREADS, 0, st>>>(m, a, xd, w.keyA, w.khi, w.klo, err);
         int rc = qmcgb::launch_status("gdn_nus keys");
         if (rc) return rc;
+        if (keys_out && !sizing) {
+            gdn_keys_out_kernel<<<gg, NUS_THREADS, 0, st>>>(m, w.khi, w.klo, (u64 *)keys_out);
+            rc = qmcgb::launch_status("gdn_nus keys out");
+            if (rc) return rc;
+        }
         u64 *kf = w.keyA, *ko = w.keyB;
         u32 *vf = w.valA, *vo = w.valB;
         if (n > 0) {
@@ -524,31 +653,54 @@ int qmc_gdn_nested_uniform_scramble(uint64_t r, uint64_t n, uint64_t d, uint64_t
             if (rc) return rc;
         }
         gdn_offsets_kernel<<<m.S, 1024, 0, st>>>(m, a, w.Lv, w.offs, w.tot);
-        gdn_bases_kernel<<<1, 32, 0, st>>>(m.S, w.tot, w.base, w.total);
-        u64 total = 0;
-        rc = qmcgb::cuda_status(cudaMemcpyAsync(&total, w.total, 8, cudaMemcpyDeviceToHost, st), "gdn_nus sizes");
+        gdn_bases_kernel<<<1, 32, 0, st>>>(m, a, w.tot, w.base, w.total);
+        u64 sizes[2] = {0, 0};
+        rc = qmcgb::cuda_status(cudaMemcpyAsync(sizes, w.total, 16, cudaMemcpyDeviceToHost, st), "gdn_nus sizes");
+        if (rc) return rc;
+        rc = qmcgb::cuda_status(cudaMemcpyAsync(tot_h.data(), w.tot, (u64)m.S * 8, cudaMemcpyDeviceToHost, st),
+                                "gdn_nus sizes");
         if (rc) return rc;
         rc = qmcgb::cuda_status(cudaStreamSynchronize(st), "gdn_nus sizes");
         if (rc) return rc;
-        if (total > need_max) need_max = total;
-        if (total > perm_capacity) {
-            if (perm_needed) *perm_needed = need_max;
-            qmcgb::set_error("gdn_nested_uniform_scramble: the permutations of %u generators need %llu entries, "
-                             "the buffer holds %llu", m.S, (unsigned long long)total,
-                             (unsigned long long)perm_capacity);
-            return QMC_ERR_ARG;
+        const u64 total = sizes[0], most_rows = sizes[1];
+        for (u32 g = 0; g < m.S; g++) perm_off[s0 + g + 1] = perm_off[s0 + g] + tot_h[g];
+        if (sizing || filled + total > perm_capacity) {
+            sizing = true;
+            filled += total;
+            continue;
         }
-        gdn_draw_kernel<<<(m.S + 31) / 32, 32, 0, st>>>(m, a, stw, w.Lv, w.offs, w.base, pm, err);
+        unsigned short *pc = pm + filled;  // this chunk's rows
+        filled += total;
+        if (h0) {
+            const dim3 hg((unsigned)qmcgb::grid_for(most_rows * bmax, NUS_THREADS, 4096), m.S);
+            gdn_hist_rows_kernel<<<hg, NUS_THREADS, 0, st>>>(m, w.offs, w.tot, w.base, (const unsigned short *)hist_perms,
+                                                             (const u64 *)hist_perm_off, pc, err);
+            rc = qmcgb::launch_status("gdn_nus earlier rows");
+            if (rc) return rc;
+        }
+        gdn_stream_kernel<<<m.S, 32, 0, st>>>(m, a, stw, w.offs, w.tot, w.base, pc, err);
         rc = qmcgb::launch_status("gdn_nus draws");
         if (rc) return rc;
+        if (most_rows > 0) {
+            const dim3 sg((unsigned)((most_rows + shuffle_T - 1) / shuffle_T), m.S);
+            gdn_shuffle_kernel<<<sg, shuffle_T, shuffle_smem, st>>>(m, a, w.offs, w.tot, w.base, pc);
+            rc = qmcgb::launch_status("gdn_nus permutations");
+            if (rc) return rc;
+        }
         if (n > 0) {
             gdn_walk_kernel<<<gg, NUS_THREADS, 0, st>>>(m, a, vf, w.lam, w.pleaf, w.pint, vo, w.Lv, w.offs, w.base,
-                                                        pm, xd, xr, err);
+                                                        pc, xd, xr, err);
             rc = qmcgb::launch_status("gdn_nus output");
             if (rc) return rc;
         }
     }
-    if (perm_needed) *perm_needed = need_max;
+    if (perm_needed) *perm_needed = filled;
+    if (sizing) {
+        qmcgb::set_error("gdn_nested_uniform_scramble: the permutations of %llu generators need %llu entries, the "
+                         "buffer holds %llu", (unsigned long long)G, (unsigned long long)filled,
+                         (unsigned long long)perm_capacity);
+        return QMC_ERR_ARG;
+    }
     return QMC_OK;
 }
 

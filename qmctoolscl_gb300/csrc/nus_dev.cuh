@@ -2,10 +2,11 @@
 // base-2 nets (nus.cu) and generalized base-b nets (gdn_nus.cu): the launch
 // constants and chunk dimensions, the stable LSD radix sort of (key, point)
 // pairs on 64-bit keys, Apetrei's bottom-up radix-tree pass with the earliest
-// point per node, and numpy's SFC64 generator.  Each including file gets its
-// own copy (anonymous namespace).
+// point per node; numpy's SFC64 generator comes from numpy_rng.cuh.  Each
+// including file gets its own copy (anonymous namespace).
 #pragma once
 #include "common.cuh"
+#include "numpy_rng.cuh"
 
 namespace {
 
@@ -259,43 +260,5 @@ __global__ void __launch_bounds__(NUS_THREADS) nus_build_kernel(NusDims m, const
         node = par;
     }
 }
-
-// ---- numpy's SFC64 stream -------------------------------------------------------
-
-struct Sfc64 {
-    u64 a, b, c, w, half;
-    u32 has;
-
-    __device__ __forceinline__ u64 next64()
-    {
-        const u64 out = a + b + w++;
-        a = b ^ (b >> 11);
-        b = c + (c << 3);
-        c = ((c << 24) | (c >> 40)) + out;
-        return out;
-    }
-    __device__ __forceinline__ u64 next32()
-    {
-        if (has) {
-            has = 0;
-            return half;
-        }
-        const u64 x = next64();
-        has = 1;
-        half = x >> 32;
-        return x & 0xFFFFFFFFull;
-    }
-    // Generator.integers(0, 2**bits) (bits <= 63) and random_tbit_uint64s(rng,
-    // bits, 1) (bits <= 64): with a power-of-two range numpy's Lemire rule
-    // never rejects, so the value is the top bits of one 32-bit output (range
-    // up to 2^32) or one 64-bit output; no draw for bits = 0
-    __device__ __forceinline__ u64 bits(u32 nb)
-    {
-        if (nb == 0) return 0;
-        if (nb <= 32) return next32() >> (32 - nb);
-        const u64 x = next64();
-        return nb == 64 ? x : x >> (64 - nb);
-    }
-};
 
 }  // namespace

@@ -252,9 +252,9 @@ class NUSNode_gdn(object):
     """Root of one generator's base-b scrambling tree, with the fields of the
     reference's node (qmctoolscl/rand_funcs.py:255-260).  A fresh node (perm
     None) starts a tree.  After a call the node is marked used (perm set) and
-    keeps what a later call needs to continue the tree by replay: the
-    generator's state before the first call and after the last, and the
-    digits of every point so far."""
+    keeps its tree on the GPU: the keys of every entry so far (the phantom
+    root and every point, in call order) and the permutation rows they drew,
+    which a later call on the same node continues from."""
 
     def __init__(self, perm=None, xdig=None, children=None):
         self.perm = perm
@@ -262,75 +262,24 @@ class NUSNode_gdn(object):
         self.children = children
 
 
-def gdn_workspace_bytes(n, generators):
-    """Device bytes the kernels need to scramble `generators` base-b generators at once."""
+def gdn_workspace_bytes(n, h0, generators):
+    """Device bytes the kernels need to scramble `generators` base-b generators
+    at once, n new points on trees of h0 entries so far (0: fresh trees)."""
     lib = _ffi.lib()
     out = ctypes.c_uint64(0)
-    _ffi.check(lib.qmc_gdn_nus_workspace_size(n, generators, ctypes.byref(out)), "gdn_nested_uniform_scramble")
+    _ffi.check(lib.qmc_gdn_nus_workspace_size(n, h0, generators, ctypes.byref(out)), "gdn_nested_uniform_scramble")
     return out.value
 
 
-def _gdn_fresh(r, n, d, r_x, r_b, tmax, tmax_new, states, bases_np, xdig, xrdig, kwargs):
-    """One call of qmc_gdn_nested_uniform_scramble on fresh trees.  xdig and
-    xrdig as the public function takes them (numpy arrays or CUDA tensors,
-    checked there), states the (r*d, 6) generator words before the call;
-    returns the words after it."""
-    torch = _t()
-    G = r * d
-    dxd, hxd = _u64_array(xdig, r_x * n * d * tmax, "xdig", 11)
-    dxr, hxr = _u64_array(xrdig, r * n * d * tmax_new, "xrdig", 12)
-    lib = _ffi.lib()
-    dev = dxd.device if dxd is not None else (dxr.device if dxr is not None else
-                                              torch.device("cuda", torch.cuda.current_device()))
-    stream = kwargs.get("stream") or torch.cuda.current_stream(dev)
-    per = gdn_workspace_bytes(n, 1)
-    budget = kwargs.get("workspace_bytes")
-    if budget is None:
-        free, _total = torch.cuda.mem_get_info(dev)
-        budget = min(free // 4, 32 << 30)
-    # a first guess at the permutation entries per generator: every level below
-    # the digits that n points share, for every point (exact sizes come back
-    # from the call when the guess is short)
-    bmax = int(bases_np.max())
-    share = int(np.floor(np.log(max(n, 1)) / np.log(max(int(bases_np.min()), 2))))
-    perm_per = (n + 1) * bmax * max(1, tmax_new - max(share - 1, 0))
-    count = max(1, min(G, int(budget) // (per + 2 * perm_per)))
-    wbytes = gdn_workspace_bytes(n, count)
-    capacity = count * perm_per
-    with torch.cuda.device(dev), torch.cuda.stream(stream):
-        i64 = torch.int64
-        dbases = torch.from_numpy(bases_np.view(np.int64)).to(dev)
-        if dxd is None:
-            dxd = torch.from_numpy(_ffi.writable(hxd.reshape(-1)[:r_x * n * d * tmax].view(np.int64))).to(dev) if n else \
-                torch.empty(1, dtype=i64, device=dev)
-        if dxr is None:
-            dxr = torch.empty(max(r * n * d * tmax_new, 1), dtype=i64, device=dev)
-        work = torch.empty(wbytes, dtype=torch.uint8, device=dev)
-        needed = ctypes.c_uint64(0)
-        for _attempt in range(3):
-            dstate = torch.from_numpy(states.reshape(-1).view(np.int64)).to(dev)
-            perms = torch.empty(max(capacity, 1), dtype=torch.int16, device=dev)
-            rc = lib.qmc_gdn_nested_uniform_scramble(
-                r, n, d, r_x, r_b, tmax, tmax_new, dstate.data_ptr(), dbases.data_ptr(), dxd.data_ptr(),
-                dxr.data_ptr(), perms.data_ptr(), capacity, ctypes.byref(needed), work.data_ptr(), wbytes,
-                stream.cuda_stream)
-            if rc == _ffi.QMC_ERR_ARG and needed.value > capacity:
-                del perms
-                capacity = int(needed.value * 1.25) + 1
-                continue
-            _ffi.check(rc, "gdn_nested_uniform_scramble")
-            break
-        else:
-            raise _ffi.QmcError("gdn_nested_uniform_scramble: permutation buffer sizing did not settle")
-        rc = lib.qmc_device_error_check(stream.cuda_stream)
-        if rc == _ffi.QMC_ERR_DEVICE:
-            raise IndexError("gdn_nested_uniform_scramble: a digit at or above its base")
-        _ffi.check(rc, "gdn_nested_uniform_scramble")
-        if hxr is not None and n:
-            torch.from_numpy(hxr.reshape(-1)[:r * n * d * tmax_new].view(np.int64)).copy_(dxr[:r * n * d * tmax_new])
-        new_states = dstate.cpu().numpy().view(np.uint64).reshape(G, STATE_WORDS)
-        del work, perms
-    return new_states
+def _perm_guess(n, h0_entries, tmax_new, base_of):
+    """A first guess at the permutation entries all trees need: every point
+    below the digits n points share draws the remaining levels (exact sizes
+    come back from the call when the guess is short)."""
+    total = h0_entries
+    for b in base_of:
+        share = int(np.floor(np.log(max(n, 1)) / np.log(b) + 1e-9))
+        total += (n + 1) * b * max(1, tmax_new - share + 1)
+    return total
 
 
 def gdn_nested_uniform_scramble(r, n, d, r_x, r_b, tmax, tmax_new, rngs, root_nodes, bases, xdig, xrdig, **kwargs):
@@ -353,15 +302,15 @@ Args:
 Runs on the GPU with bases 2..65536, tmax < tmax_new <= 255 and
 tmax * ceil(log2 b) <= 128 (ValueError otherwise).  A digit at or above its
 base raises IndexError, as the reference does.  A later call on the same
-root nodes continues their trees as the reference does: a point's result
-depends only on the points before it, so the call scrambles the earlier
-points again together with the new ones, from the generators' states before
-the first call, and keeps the new points' results; the generators must not
-have been drawn from in between (ValueError).  Keyword arguments:
+root nodes continues their trees as the reference's nodes do: each node
+keeps, on the GPU, the keys of every point its tree has seen (16 bytes each)
+and the permutations they drew (2 bytes per entry, b entries per level), and
+new points draw from the generators' current states.  Keyword arguments:
 ``workspace_bytes`` caps the device scratch, ``stream`` selects a
 torch.cuda.Stream."""
     t0_perf = time.perf_counter()
     t0_process = time.process_time()
+    torch = _t()
     r, n, d, r_x, r_b, tmax, tmax_new = (int(v) for v in (r, n, d, r_x, r_b, tmax, tmax_new))
     G = r * d
     gens = _objects(rngs, r, d, "rngs")
@@ -381,66 +330,90 @@ torch.cuda.Stream."""
         raise ValueError("the GPU form needs 1 <= tmax < tmax_new <= 255 (tmax=%d, tmax_new=%d)" % (tmax, tmax_new))
     if G and tmax * int(np.ceil(np.log2(float(bases_np.max())))) > 128:
         raise ValueError("tmax * ceil(log2 b) must not exceed 128 bits for the GPU form")
-    _u64_array(xdig, r_x * n * d * tmax, "xdig", 11)
-    _u64_array(xrdig, r * n * d * tmax_new, "xrdig", 12)
+    dxd, hxd = _u64_array(xdig, r_x * n * d * tmax, "xdig", 11)
+    dxr, hxr = _u64_array(xrdig, r * n * d * tmax_new, "xrdig", 12)
     base_of = [int(bases_np[(k // d % r_b) * d + k % d]) for k in range(G)]
     fresh = [node.perm is None for node in roots]
-    first_call = all(fresh)
-    h = 0
-    if first_call:
+    h0 = 0
+    if all(fresh):
         pass
     elif not any(fresh) and all(getattr(node, "_hist", None) is not None for node in roots):
-        hs = {node._hist["digits"].shape[0] for node in roots}
+        hs = {int(node._hist["keys"].shape[0]) for node in roots}
         if len(hs) != 1:
             raise ValueError("root_nodes hold trees of different sizes; scramble them in separate calls")
-        h = hs.pop()
+        h0 = hs.pop()
         for k, node in enumerate(roots):
             hk = node._hist
             if (hk["tmax"], hk["tmax_new"], hk["base"]) != (tmax, tmax_new, base_of[k]):
                 raise ValueError("root_nodes were built with another tmax, tmax_new or base")
-            if not np.array_equal(sfc64_state_words(gens[k]), hk["state_after"]):
-                raise ValueError("a generator was drawn from since its tree's last call; continuing the tree "
-                                 "replays its stream from the first call")
     else:
         raise ValueError("root_nodes must be all fresh or all built by earlier calls of this function")
     if G == 0:
         return time.perf_counter() - t0_perf, time.process_time() - t0_process
-    now = np.stack([sfc64_state_words(g) for g in gens])
-    if first_call:
-        new_states = _gdn_fresh(r, n, d, r_x, r_b, tmax, tmax_new, now, bases_np, xdig, xrdig, kwargs)
-        start = now
-        xd_np = _host_digits(xdig, r_x, n, d, tmax)
-        digits = [xd_np[(k // d) % r_x, :, k % d, :].copy() for k in range(G)]
-    else:
-        start = np.stack([node._hist["state0"] for node in roots])
-        xd_np = _host_digits(xdig, r_x, n, d, tmax)
-        digits = [np.concatenate([roots[k]._hist["digits"], xd_np[(k // d) % r_x, :, k % d, :]]) for k in range(G)]
-        full = np.empty((r, h + n, d, tmax), dtype=np.uint64)
-        for k in range(G):
-            full[k // d, :, k % d, :] = digits[k]
-        out = np.empty((r, h + n, d, tmax_new), dtype=np.uint64)
-        new_states = _gdn_fresh(r, h + n, d, r, r_b, tmax, tmax_new, start, bases_np, full, out, kwargs)
-        _store_digits(xrdig, np.ascontiguousarray(out[:, h:]))
+    states = np.stack([sfc64_state_words(g) for g in gens])
+    lib = _ffi.lib()
+    dev = dxd.device if dxd is not None else (dxr.device if dxr is not None else
+                                              torch.device("cuda", torch.cuda.current_device()))
+    stream = kwargs.get("stream") or torch.cuda.current_stream(dev)
+    H0 = h0 if h0 else 1
+    N = H0 + n
+    per = gdn_workspace_bytes(n, h0, 1)
+    budget = kwargs.get("workspace_bytes")
+    if budget is None:
+        free, _total = torch.cuda.mem_get_info(dev)
+        budget = min(free // 4, 32 << 30)
+    count = max(1, min(G, int(budget) // per))
+    wbytes = gdn_workspace_bytes(n, h0, count)
+    with torch.cuda.device(dev), torch.cuda.stream(stream):
+        i64 = torch.int64
+        dbases = torch.from_numpy(bases_np.view(np.int64)).to(dev)
+        if dxd is None:
+            dxd = torch.from_numpy(_ffi.writable(hxd.reshape(-1)[:r_x * n * d * tmax].view(np.int64))).to(dev) \
+                if n else torch.empty(1, dtype=i64, device=dev)
+        if dxr is None:
+            dxr = torch.empty(max(r * n * d * tmax_new, 1), dtype=i64, device=dev)
+        if h0:
+            hist_keys = torch.stack([node._hist["keys"] for node in roots]).contiguous()
+            hist_rows = torch.cat([node._hist["perms"] for node in roots]) if G else None
+            lens = np.array([int(node._hist["perms"].numel()) for node in roots], dtype=np.int64)
+            hist_off = torch.from_numpy(np.concatenate([[0], np.cumsum(lens)])).to(dev)
+            old_entries = int(lens.sum())
+        else:
+            hist_keys = hist_rows = hist_off = None
+            old_entries = 0
+        keys_out = torch.empty((G, N, 2), dtype=i64, device=dev)
+        work = torch.empty(wbytes, dtype=torch.uint8, device=dev)
+        capacity = _perm_guess(n, old_entries, tmax_new, base_of)
+        needed = ctypes.c_uint64(0)
+        perm_off = np.zeros(G + 1, dtype=np.uint64)
+        for _attempt in range(2):
+            dstate = torch.from_numpy(states.reshape(-1).view(np.int64)).to(dev)
+            perms = torch.empty(max(capacity, 1), dtype=torch.int16, device=dev)
+            rc = lib.qmc_gdn_nested_uniform_scramble(
+                r, n, d, r_x, r_b, tmax, tmax_new, dstate.data_ptr(), dbases.data_ptr(), h0,
+                hist_keys.data_ptr() if h0 else None, hist_rows.data_ptr() if h0 else None,
+                hist_off.data_ptr() if h0 else None, dxd.data_ptr(), dxr.data_ptr(), keys_out.data_ptr(),
+                perms.data_ptr(), capacity, perm_off.ctypes.data, ctypes.byref(needed), work.data_ptr(), wbytes,
+                stream.cuda_stream)
+            if rc == _ffi.QMC_ERR_ARG and needed.value > capacity:
+                del perms
+                capacity = int(needed.value)
+                continue
+            _ffi.check(rc, "gdn_nested_uniform_scramble")
+            break
+        else:
+            raise _ffi.QmcError("gdn_nested_uniform_scramble: permutation buffer sizing did not settle")
+        rc = lib.qmc_device_error_check(stream.cuda_stream)
+        if rc == _ffi.QMC_ERR_DEVICE:
+            raise IndexError("gdn_nested_uniform_scramble: a digit at or above its base")
+        _ffi.check(rc, "gdn_nested_uniform_scramble")
+        if hxr is not None and n:
+            torch.from_numpy(hxr.reshape(-1)[:r * n * d * tmax_new].view(np.int64)).copy_(dxr[:r * n * d * tmax_new])
+        new_states = dstate.cpu().numpy().view(np.uint64).reshape(G, STATE_WORDS)
+        del work, hist_keys, hist_rows, hist_off
     for k in range(G):
         set_sfc64_state(gens[k], new_states[k])
         roots[k].perm = np.zeros(0, dtype=np.uint64)  # used; the tree lives in _hist
-        roots[k]._hist = {"state0": start[k].copy(), "state_after": new_states[k].copy(), "digits": digits[k],
+        roots[k]._hist = {"keys": keys_out[k], "perms": perms[int(perm_off[k]):int(perm_off[k + 1])],
                           "tmax": tmax, "tmax_new": tmax_new, "base": base_of[k]}
     return time.perf_counter() - t0_perf, time.process_time() - t0_process
-
-
-def _host_digits(xdig, r_x, n, d, tmax):
-    """the digits as a host numpy array (r_x, n, d, tmax)"""
-    if type(xdig).__module__.startswith("torch"):
-        return xdig.reshape(-1)[:r_x * n * d * tmax].cpu().numpy().view(np.uint64).reshape(r_x, n, d, tmax)
-    return np.asarray(xdig).reshape(-1)[:r_x * n * d * tmax].reshape(r_x, n, d, tmax)
-
-
-def _store_digits(xrdig, values):
-    """values (numpy) into xrdig, a numpy array or a CUDA tensor"""
-    flat = values.reshape(-1)
-    if type(xrdig).__module__.startswith("torch"):
-        torch = _t()
-        xrdig.reshape(-1)[:flat.size].copy_(torch.from_numpy(flat.view(np.int64)))
-    else:
-        xrdig.reshape(-1)[:flat.size] = flat

@@ -2,10 +2,11 @@
 (qmctoolscl_gb300.gdn_nested_uniform_scramble, C entry point
 qmc_gdn_nested_uniform_scramble) against the reference's own results (golden
 vectors from qmctoolscl/rand_funcs.py:262-356, the documented example
-included; first call of each case: the GPU form scrambles fresh trees) and
+included, every call of the multi-call cases on the same root nodes) and
 against the oracle on seeded inputs: digits bit for bit and the numpy
-generator states after the call, over bases 2..541, replicated bases and
-points, repeated points, chunked workspaces and device tensors."""
+generator states after each call, over bases 2..541, replicated bases and
+points, repeated points, chunked workspaces, device tensors, and trees
+continued after their generators were drawn from between calls."""
 import os
 
 import numpy as np
@@ -43,6 +44,57 @@ def test_golden_first_call(c):
                                   GOLD["case%d_bases" % c], GOLD["case%d_xdig0" % c], xr)
     assert np.array_equal(xr, GOLD["case%d_xrdig0" % c])
     assert np.array_equal(_states(gens), GOLD["case%d_state1" % c])
+
+
+@pytest.mark.parametrize("c", range(NCASES))
+@pytest.mark.parametrize("tensors", [False, True])
+def test_golden_every_call(c, tensors):
+    """later calls on the same root nodes continue the trees from the kept
+    keys and permutations, as the reference's nodes do; with numpy arrays or
+    CUDA tensors for xdig and xrdig"""
+    import torch
+    r, n, d, r_x, r_b, tmax, tmax_new, calls = (int(v) for v in GOLD["case%d_args" % c])
+    if calls < 2 and tensors:
+        pytest.skip("single-call case")
+    gens = _gens(GOLD["case%d_state0" % c])
+    rngs = np.array(gens, dtype=object).reshape(r, d)
+    roots = np.array([NUSNode_gdn() for _ in range(r * d)]).reshape(r, d)
+    for k in range(calls):
+        xd = GOLD["case%d_xdig%d" % (c, k)]
+        if tensors:
+            xd = torch.from_numpy(np.ascontiguousarray(xd).reshape(-1).view(np.int64)).cuda()
+            xr = torch.full((r * n * d * tmax_new,), 9, dtype=torch.int64, device="cuda")
+        else:
+            xr = np.full((r, n, d, tmax_new), 9, dtype=np.uint64)
+        q.gdn_nested_uniform_scramble(r, n, d, r_x, r_b, tmax, tmax_new, rngs, roots, GOLD["case%d_bases" % c], xd,
+                                      xr)
+        got = xr.cpu().numpy().view(np.uint64).reshape(r, n, d, tmax_new) if tensors else xr
+        assert np.array_equal(got, GOLD["case%d_xrdig%d" % (c, k)]), (c, k)
+        assert np.array_equal(_states(gens), GOLD["case%d_state%d" % (c, k + 1)]), (c, k)
+
+
+def test_generators_drawn_from_between_calls_continue_their_streams():
+    """the reference's nodes keep their trees and the generators simply go on:
+    draws taken from a generator between calls shift the next call's draws"""
+    rng = np.random.Generator(np.random.SFC64(83))
+    r, n, d, tmax, tmax_new = 2, 400, 2, 6, 8
+    bases = np.array([[3, 7]], dtype=np.uint64)
+    gens = [np.random.Generator(np.random.SFC64(s)) for s in range(r * d)]
+    roots = np.array([NUSNode_gdn() for _ in range(r * d)]).reshape(r, d)
+    f = oracle.GdnNusForest(r * d)
+    for call in range(3):
+        xdig = _digits(rng, 1, n, d, tmax, bases)
+        words = _states(gens).reshape(-1).copy()
+        want = np.zeros((r, n, d, tmax_new), dtype=np.uint64)
+        assert f.scramble(r, n, d, 1, 1, tmax, tmax_new, words, bases, xdig, want) == 0
+        got = np.zeros((r, n, d, tmax_new), dtype=np.uint64)
+        q.gdn_nested_uniform_scramble(r, n, d, 1, 1, tmax, tmax_new, np.array(gens, dtype=object).reshape(r, d),
+                                      roots, bases, xdig, got)
+        assert np.array_equal(got, want), call
+        assert np.array_equal(_states(gens).reshape(-1), words), call
+        for g in gens[::2]:
+            g.integers(0, 1000, 3)  # between calls
+    f.close()
 
 
 def _check(rng, r, n, d, r_x, r_b, tmax, tmax_new, bases, xdig, **kw):
@@ -104,7 +156,7 @@ def test_chunked_workspace_matches():
     bases = np.array([[3, 2, 7]], dtype=np.uint64)
     n = 700
     xdig = _digits(rng, 1, n, 3, 6, bases)
-    per = q.nus.gdn_workspace_bytes(n, 1)
+    per = q.nus.gdn_workspace_bytes(n, 0, 1)
     _check(rng, 2, n, 3, 1, 1, 6, 9, bases, xdig, workspace_bytes=per + 1000)
 
 

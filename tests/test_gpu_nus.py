@@ -133,7 +133,7 @@ def test_device_tensors_in_place():
     want = np.zeros((r, n, d), np.uint64)
     q.dnb2_nested_uniform_scramble(r, n, d, 1, 64, 64, np.array(gens_a, dtype=object).reshape(r, d),
                                    np.array([NUSNode_dnb2() for _ in range(r * d)]).reshape(r, d), xb, want)
-    dx = torch.from_numpy(xb.reshape(-1).view(np.int64)).cuda()
+    dx = torch.from_numpy(xb.reshape(-1).view(np.int64).copy()).cuda()
     dout = torch.zeros(r * n * d, dtype=torch.int64, device="cuda")
     q.dnb2_nested_uniform_scramble(r, n, d, 1, 64, 64, np.array(gens_b, dtype=object).reshape(r, d),
                                    np.array([NUSNode_dnb2() for _ in range(r * d)]).reshape(r, d), dx, dout)

@@ -83,14 +83,22 @@ def test_c_entry_points_check_arguments_before_any_launch():
                                               64, None)  # workspace far too small
     assert rc == _ffi.QMC_ERR_ARG and b"workspace" in lib.qmc_last_error()
     needed = ctypes.c_uint64(7)
-    rc = lib.qmc_gdn_nested_uniform_scramble(1, 4, 1, 1, 1, 3, 3, fake, fake, fake, fake, fake, 1 << 20,
-                                             ctypes.byref(needed), fake, 1 << 30, None)
+    off = (ctypes.c_uint64 * 2)()
+
+    def gdn(r, tmax_new, states=fake, h0=0, hist=None, off_=off):
+        # (r, n, d, r_x, r_b, tmax, tmax_new, states, bases, h0, hist_keys, hist_perms, hist_perm_off, xdig,
+        #  xrdig, keys_out, perms, perm_capacity, perm_off, perm_needed, work, work_bytes, stream)
+        return lib.qmc_gdn_nested_uniform_scramble(r, 4, 1, 1, 1, 3, tmax_new, states, fake, h0, hist, hist, hist,
+                                                   fake, fake, None, fake, 1 << 20, off_, ctypes.byref(needed), fake,
+                                                   1 << 30, None)
+
+    rc = gdn(1, 3)
     assert rc == _ffi.QMC_ERR_ARG and b"tmax < tmax_new" in lib.qmc_last_error() and needed.value == 0
-    rc = lib.qmc_gdn_nested_uniform_scramble(1, 4, 1, 1, 1, 3, 5, None, fake, fake, fake, fake, 1 << 20,
-                                             ctypes.byref(needed), fake, 1 << 30, None)
-    assert rc == _ffi.QMC_ERR_ARG
-    assert lib.qmc_gdn_nested_uniform_scramble(0, 4, 1, 1, 1, 3, 5, None, None, None, None, None, 0, None, None, 0,
-                                               None) == _ffi.QMC_OK  # r = 0: nothing to do
+    assert gdn(1, 5, states=None) == _ffi.QMC_ERR_ARG
+    assert gdn(1, 5, off_=None) == _ffi.QMC_ERR_ARG  # no permutation offsets
+    rc = gdn(1, 5, h0=3)  # earlier entries without their keys and permutations
+    assert rc == _ffi.QMC_ERR_ARG and b"h0" in lib.qmc_last_error()
+    assert gdn(0, 5, states=None) == _ffi.QMC_OK  # r = 0: nothing to do
 
 
 def test_host_write_decision(monkeypatch):
