@@ -942,6 +942,33 @@ def halton_inputs(r, log2n, d, seed=4):
     return dims
 
 
+def halton_inputs_gpu(r, log2n, d, seed=4):
+    """halton_inputs with every random array drawn on the GPU (the same
+    helpers with a device-resident generator: the same numpy streams, bit for
+    bit); the generating matrices (identity, no randomness) are built on the
+    host as the reference builds them."""
+    import math
+    import qmctoolscl_gb300 as q
+    rng = np.random.Generator(np.random.SFC64(seed))
+    dg = q.DeviceGenerator(rng)
+    dims = []
+    for b in first_primes(d):
+        tmax = math.ceil(64 / math.log2(b))
+        mmax, v = 0, (1 << log2n) - 1
+        while v:
+            v //= b
+            mmax += 1
+        mmax = max(mmax, math.ceil(log2n / math.log2(b)))
+        bb = np.array([[b]], np.uint64)
+        C = np.ascontiguousarray(q.gdn_get_halton_generating_matrix(1, 1, max(mmax, tmax))[:, :, :mmax, :tmax])
+        dims.append(dict(b=b, tmax=tmax, mmax=mmax, C=C,
+                         S=q.gdn_get_linear_scramble_matrix(dg, r, 1, tmax, tmax, 1, bb),
+                         perms=q.gdn_get_digital_permutations(dg, r, 1, tmax, 1, bb),
+                         shifts=q.gdn_get_digital_shifts(dg, r, 1, tmax, 1, bb)))
+    dg.sync()
+    return dims
+
+
 def halton_oracle(dims, l, i0, cnt):
     """The reference chain on the oracle, one dimension per call, for
     randomisation l and points [i0, i0+cnt): an (cnt, d) float64 array."""
@@ -980,6 +1007,7 @@ def run_halton(args):
     lib = _ffi.lib()
     r, log2n, d = (8 if args.small else 32), 18, 100
     n = 1 << log2n
+    pts_e2e = r * n
     dims = halton_inputs(r, log2n, d)
     st = torch.cuda.current_stream()
     h = st.cuda_stream
@@ -1056,6 +1084,29 @@ def run_halton(args):
         A = halton.generalized_net_fused(r, n, 0, dims, xh, check=False)
     t_e2e = (time.perf_counter() - t0) / e2e_steps
     assert np.array_equal(xh.view(np.uint64), x.cpu().numpy().view(np.uint64))
+    # e2e with the randomisation inputs drawn every step: by numpy on the host (the reference's
+    # helpers, then copied in), or on the GPU from a device-resident generator (no input copies)
+    dims_gpu = halton_inputs_gpu(r, log2n, d)
+    for dh, dg_ in zip(dims, dims_gpu):  # the GPU draws are numpy's, bit for bit
+        for key in ("S", "perms", "shifts"):
+            assert np.array_equal(dg_[key].cpu().numpy().view(np.uint64), dh[key]), "device inputs differ"
+    e2e_inputs = {}
+    for mode, make in (("host_numpy_inputs", lambda: halton_inputs(r, log2n, d)),
+                       ("gpu_inputs", lambda: halton_inputs_gpu(r, log2n, d))):
+        make()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(e2e_steps):
+            A_in = halton.generalized_net_fused(r, n, 0, make(), xh, check=False)
+        t_in = (time.perf_counter() - t0) / e2e_steps
+        assert np.array_equal(xh.view(np.uint64), x.cpu().numpy().view(np.uint64))
+        t_gen = time.perf_counter()
+        make()
+        torch.cuda.synchronize()
+        t_gen = time.perf_counter() - t_gen
+        e2e_inputs[mode] = {"value": pts_e2e / t_in, "unit": "points/s", "ms_per_step": 1e3 * t_in,
+                            "input_generation_ms": 1e3 * t_gen, "h2d_bytes_per_step": A_in.h2d_bytes,
+                            "d2h_bytes_per_step": A_in.d2h_bytes}
 
     # uneven batch: 64 requests of random r (1-4), n (2^10-2^16), n_start, d (4-100, first d primes);
     # one plan (graph replay: preparation + one generation launch) against one plan per request
@@ -1136,7 +1187,12 @@ def run_halton(args):
             "e2e": {"value": pts / t_e2e, "unit": "points/s", "ms_per_step": 1e3 * t_e2e,
                     "h2d_bytes_per_step": A.h2d_bytes, "d2h_bytes_per_step": A.d2h_bytes,
                     "direct_host_write": A.direct,
-                    "path": "qmctoolscl_gb300.halton.generalized_net_fused, numpy inputs, pinned numpy output"},
+                    "path": "qmctoolscl_gb300.halton.generalized_net_fused, numpy inputs, pinned numpy output",
+                    "other": {k: dict(v, path="randomisation inputs drawn every step (%s), then "
+                                              "generalized_net_fused into the pinned output"
+                                              % ("numpy on the host, copied in" if k.startswith("host")
+                                                 else "on the GPU from a DeviceGenerator, no input copies"))
+                              for k, v in e2e_inputs.items()}},
             "gpu_launches": 3 * args.steps, "clocks": clk,
             "cpu_baseline": {"value": cpu_pts / t_cpu, "unit": "points/s", "cores": threads, "kind": "port",
                              "sample": "randomisation 0, %d points in %d pieces of 4096, all 100 dimensions; the "

@@ -224,6 +224,29 @@ int qmc_halton_qrng(int n, int d, int n0, int generalized, double *res, const do
 int qmc_tc_fft_mul_ifft(uint64_t d1, uint64_t d2, uint64_t n_half, const double *lam_r, const double *lam_i,
                         uint64_t lam_per_element, int divide, double scale, double *xr, double *xi, qmc_stream_t s);
 
+/* The Walsh-Hadamard analog (docs/index.md:1929-1978: u = fwht(fwht(y) * kt),
+ * v = fwht(fwht(y) / kt), fwht = fwht_1d_radix2) in one call, in place on x:
+ *     y <- FWHT(FWHT(y) * lam) * scale     (divide = 0)
+ *     y <- FWHT(FWHT(y) / lam) * scale     (divide != 0)
+ * with the tensor-core WHT above; lam real, n values for every vector or one
+ * per element.  The first transform's last pass, the pointwise step and the
+ * second transform's first pass run as one kernel on each tile. */
+int qmc_tc_fwht_mul_fwht(uint64_t d1, uint64_t d2, uint64_t n_half, const double *lam, uint64_t lam_per_element,
+                         int divide, double scale, double *x, qmc_stream_t s);
+
+/* The same two fused forms in FP64 (the arithmetic of qmc_fft_bro_1d_radix2 /
+ * qmc_ifft_bro_1d_radix2 / qmc_fwht_1d_radix2, to FP64 rounding of numpy's
+ * result): forward passes but the last, one fused pass (forward steps, the
+ * pointwise product or quotient, inverse steps), inverse passes but the first.
+ * qmc_fft_mul_ifft writes the forward twiddle table into twiddler/twiddlei (n
+ * doubles each, as qmc_fft_bro_1d_radix2 does) and runs the inverse steps on
+ * its conjugates. */
+int qmc_fft_mul_ifft(uint64_t d1, uint64_t d2, uint64_t n_half, double *twiddler, double *twiddlei, const double *lam_r,
+                     const double *lam_i, uint64_t lam_per_element, int divide, double scale, double *xr, double *xi,
+                     qmc_stream_t s);
+int qmc_fwht_mul_fwht(uint64_t d1, uint64_t d2, uint64_t n_half, const double *lam, uint64_t lam_per_element,
+                      int divide, double scale, double *x, qmc_stream_t s);
+
 /* ---- batched plans: many requests of uneven size, one persistent launch -----
  * No single reference counterpart: a plan runs, for every request, the chain
  * of reference calls written next to each struct, bit for bit, in two
@@ -386,25 +409,77 @@ int qmc_dnb2_nested_uniform_scramble(uint64_t r, uint64_t n, uint64_t d, uint64_
 /* ---- nested uniform (Owen) scrambling of generalized (base-b) nets ----------
  * Replaces the reference's Python routine gdn_nested_uniform_scramble
  * (qmctoolscl/rand_funcs.py:262-356): bit for bit its xrdig and its
- * generators' advanced states, for fresh trees (one call per set of root
- * nodes).  Generator g = l*d + j with base bases[(l % r_b)*d + j] (2..65536)
- * and numpy's SFC64 state in six words (states, r*d*6, updated in place).
- * xdig (r_x, n, d, tmax) digits, xrdig (r, n, d, tmax_new); needs
- * 1 <= tmax < tmax_new <= 255 and tmax * ceil(log2 b) <= 128 (the digits are
- * compared as 128-bit keys).  `perms` holds perm_capacity 16-bit entries for
- * the drawn permutations of one chunk of generators; when a chunk needs more,
- * the call returns QMC_ERR_ARG with the entries needed in *perm_needed (the
- * largest chunk so far) before drawing for that chunk -- states of earlier
- * chunks are then already advanced, so a caller retries from its own copy.
+ * generators' advanced states.  Generator g = l*d + j with base
+ * bases[(l % r_b)*d + j] (2..65536) and numpy's SFC64 state in six words
+ * (states, r*d*6, updated in place).  xdig (r_x, n, d, tmax) digits, xrdig
+ * (r, n, d, tmax_new); needs 1 <= tmax < tmax_new <= 255 and
+ * tmax * ceil(log2 b) <= 128 (the digits are compared as 128-bit keys).
+ *
+ * Trees.  h0 = 0 starts fresh trees (the call adds the phantom root as entry
+ * 0).  A later call on the same trees passes what the earlier calls left:
+ * h0 entries per tree (the phantom root and every earlier point, in call
+ * order), their keys hist_keys (r*d, h0, 2) as the earlier call wrote them to
+ * keys_out, and their permutation rows: generator g's at
+ * hist_perms[hist_perm_off[g] .. hist_perm_off[g+1]) (device memory, r*d+1
+ * offsets), as perm_off gave them.  The new points then continue each tree
+ * exactly as the reference's nodes continue (draws from the generators'
+ * current states).
+ *
+ * Outputs besides xrdig: keys_out (r*d, h0 + n, 2) (or h0 = 1 when fresh; may
+ * be NULL) and every tree's rows, earlier ones copied in front: generator g's
+ * at perms[perm_off[g] .. perm_off[g+1]), perm_off a HOST array of r*d+1
+ * entries.  When perm_capacity 16-bit entries are too few, the call counts the
+ * rest without drawing and returns QMC_ERR_ARG with the entries needed in
+ * *perm_needed -- states of the generators drawn so far are then already
+ * advanced, so a caller retries from its own copy.
  * A digit at or above its base sets bit 1 of the device error word (the
- * reference raises IndexError).  Device memory throughout; `work` is a
- * 256-byte aligned workspace of work_bytes (qmc_gdn_nus_workspace_size);
- * synchronises its stream twice per chunk. */
-int qmc_gdn_nus_workspace_size(uint64_t n, uint64_t generators, uint64_t *bytes);
+ * reference raises IndexError); history rows whose length disagrees with the
+ * tree set bit 64.  Device memory throughout; `work` is a 256-byte aligned
+ * workspace of work_bytes (qmc_gdn_nus_workspace_size with the same n and
+ * h0); synchronises its stream twice per chunk of generators. */
+int qmc_gdn_nus_workspace_size(uint64_t n, uint64_t h0, uint64_t generators, uint64_t *bytes);
 int qmc_gdn_nested_uniform_scramble(uint64_t r, uint64_t n, uint64_t d, uint64_t r_x, uint64_t r_b, uint64_t tmax,
-                                    uint64_t tmax_new, uint64_t *states, const uint64_t *bases,
-                                    const uint64_t *xdig, uint64_t *xrdig, uint16_t *perms, uint64_t perm_capacity,
+                                    uint64_t tmax_new, uint64_t *states, const uint64_t *bases, uint64_t h0,
+                                    const uint64_t *hist_keys, const uint16_t *hist_perms,
+                                    const uint64_t *hist_perm_off, const uint64_t *xdig, uint64_t *xrdig,
+                                    uint64_t *keys_out, uint16_t *perms, uint64_t perm_capacity, uint64_t *perm_off,
                                     uint64_t *perm_needed, void *work, uint64_t work_bytes, qmc_stream_t s);
+
+/* ---- randomisation inputs on the GPU ----------------------------------------
+ * The reference's numpy helpers (qmctoolscl/rand_funcs.py:4-153) bit for bit:
+ * the same draws in the same order from one numpy Generator on an SFC64 bit
+ * generator, whose six state words (a, b, c, w, has_uint32, uinteger -- the
+ * fields of numpy's SFC64 state) are read from and written back to `state`
+ * (device memory) in stream order.  One GPU thread runs the stream (it is
+ * serial); fills and the permutations' swaps run wide.  Outputs are device
+ * arrays laid out as the helpers return them; uint64 results as their bits.
+ *   qmc_lat_get_shifts               rand_funcs.py:34-41   Generator.random((r, d))
+ *   qmc_random_tbit_uint64s          rand_funcs.py:4-20    count values of t bits (0 <= t <= 64)
+ *   qmc_dnb2_get_digital_shifts      rand_funcs.py:43-51   (r, d) values of tmax_new bits
+ *   qmc_dnb2_get_linear_scramble_matrix  rand_funcs.py:53-78  (r, d, tmax_new); 1 <= tmax <= tmax_new
+ *                                    (numpy's broadcasting refuses tmax > tmax_new)
+ *   qmc_gdn_get_linear_scramble_matrix   rand_funcs.py:80-104 (r, d, tmax_new, tmax), bases r_b*d
+ *   qmc_gdn_get_digital_shifts       rand_funcs.py:115-132 (r, d, tmax_new)
+ *   qmc_gdn_get_digital_permutations rand_funcs.py:134-153 (r, d, tmax_new, bmax), zero padded;
+ *                                    bmax = the largest base, at most 65536
+ *   qmc_random_uint64_permutations   rand_funcs.py:22-32   (n, b), b at most 65536
+ * Bases live in device memory.  A base numpy would refuse (below 2 for the
+ * scrambling matrices, 0 for the shifts) or one above bmax sets bit 128 of
+ * the device error word and stops the stream; a rejection loop that runs out
+ * sets bit 32. */
+int qmc_lat_get_shifts(uint64_t *state, uint64_t r, uint64_t d, double *shifts, qmc_stream_t s);
+int qmc_random_tbit_uint64s(uint64_t *state, uint64_t t, uint64_t count, uint64_t *out, qmc_stream_t s);
+int qmc_dnb2_get_digital_shifts(uint64_t *state, uint64_t r, uint64_t d, uint64_t tmax_new, uint64_t *shifts,
+                                qmc_stream_t s);
+int qmc_dnb2_get_linear_scramble_matrix(uint64_t *state, uint64_t r, uint64_t d, uint64_t tmax, uint64_t tmax_new,
+                                        uint64_t *S, qmc_stream_t s);
+int qmc_gdn_get_linear_scramble_matrix(uint64_t *state, uint64_t r, uint64_t d, uint64_t tmax, uint64_t tmax_new,
+                                       uint64_t r_b, const uint64_t *bases, uint64_t *S, qmc_stream_t s);
+int qmc_gdn_get_digital_shifts(uint64_t *state, uint64_t r, uint64_t d, uint64_t tmax_new, uint64_t r_b,
+                               const uint64_t *bases, uint64_t *shifts, qmc_stream_t s);
+int qmc_gdn_get_digital_permutations(uint64_t *state, uint64_t r, uint64_t d, uint64_t tmax_new, uint64_t r_b,
+                                     const uint64_t *bases, uint64_t bmax, uint64_t *perms, qmc_stream_t s);
+int qmc_random_uint64_permutations(uint64_t *state, uint64_t n, uint64_t b, uint64_t *out, qmc_stream_t s);
 
 #ifdef __cplusplus
 }

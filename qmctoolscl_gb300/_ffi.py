@@ -29,11 +29,23 @@ EXTRA = {
     "qmc_tc_ifft_bro_1d": [U64, U64, U64, PTR, PTR, PTR],
     "qmc_tc_fwht_1d": [U64, U64, U64, PTR, PTR],
     "qmc_tc_fft_mul_ifft": [U64, U64, U64, PTR, PTR, U64, INT, ctypes.c_double, PTR, PTR, PTR],
+    "qmc_tc_fwht_mul_fwht": [U64, U64, U64, PTR, U64, INT, ctypes.c_double, PTR, PTR],
+    "qmc_fft_mul_ifft": [U64, U64, U64, PTR, PTR, PTR, PTR, U64, INT, ctypes.c_double, PTR, PTR, PTR],
+    "qmc_fwht_mul_fwht": [U64, U64, U64, PTR, U64, INT, ctypes.c_double, PTR, PTR],
     "qmc_halton_qrng": [INT, INT, INT, INT, PTR, PTR, PTR, PTR],
     "qmc_dnb2_nus_workspace_size": [U64, U64, U64, PTR],
     "qmc_dnb2_nested_uniform_scramble": [U64] * 6 + [PTR, U64, PTR, PTR, PTR, PTR, PTR, PTR, PTR, U64, PTR],
-    "qmc_gdn_nus_workspace_size": [U64, U64, PTR],
-    "qmc_gdn_nested_uniform_scramble": [U64] * 7 + [PTR, PTR, PTR, PTR, PTR, U64, PTR, PTR, U64, PTR],
+    "qmc_lat_get_shifts": [PTR, U64, U64, PTR, PTR],
+    "qmc_random_tbit_uint64s": [PTR, U64, U64, PTR, PTR],
+    "qmc_dnb2_get_digital_shifts": [PTR, U64, U64, U64, PTR, PTR],
+    "qmc_dnb2_get_linear_scramble_matrix": [PTR, U64, U64, U64, U64, PTR, PTR],
+    "qmc_gdn_get_linear_scramble_matrix": [PTR, U64, U64, U64, U64, U64, PTR, PTR, PTR],
+    "qmc_gdn_get_digital_shifts": [PTR, U64, U64, U64, U64, PTR, PTR, PTR],
+    "qmc_gdn_get_digital_permutations": [PTR, U64, U64, U64, U64, PTR, U64, PTR, PTR],
+    "qmc_random_uint64_permutations": [PTR, U64, U64, PTR, PTR],
+    "qmc_gdn_nus_workspace_size": [U64, U64, U64, PTR],
+    "qmc_gdn_nested_uniform_scramble": [U64] * 7 + [PTR, PTR, U64, PTR, PTR, PTR, PTR, PTR, PTR, PTR, U64, PTR,
+                                                     PTR, PTR, U64, PTR],
 }
 
 

@@ -59,7 +59,8 @@ constexpr u32 FT_KS = 96;              // K of the operands: 3 splits x 32 reals
 constexpr u32 FT_THREADS = 256;
 constexpr u32 TMEM_COLS = 128;         // three 32-column FP32 accumulators
 constexpr u32 FT_PAD = FT_TILE + FT_TILE / 16;  // shared-memory words per component, padded
-enum TcKind { TC_FFT = 0, TC_IFFT = 1, TC_WHT = 2, TC_CONV = 3 };  // CONV: FFT steps, pointwise, IFFT steps
+// CONV: FFT steps, pointwise, IFFT steps; WCONV: WHT steps, pointwise (real), WHT steps
+enum TcKind { TC_FFT = 0, TC_IFFT = 1, TC_WHT = 2, TC_CONV = 3, TC_WCONV = 4 };
 
 // Shared-memory slot of tile element e: one padding word per 16, so that the
 // 32 groups a warp handles (16 consecutive elements apart in the first step)
@@ -211,16 +212,17 @@ __global__ void __launch_bounds__(FT_THREADS, 3) tc_pass_kernel(TcPassArgs a, un
     float2 *tab = (float2 *)(sB + 32 * FT_KS * 2);      // [1024] exp(-2 pi i r / 4096)
     __shared__ __align__(8) u64 bar;
     __shared__ u32 tmem_base;
+    constexpr bool REAL = KIND == TC_WHT || KIND == TC_WCONV;
     const u32 warp = threadIdx.x / 32, lane = threadIdx.x % 32;
-    const u32 NOUT = (KIND == TC_WHT) ? 16u : 32u;      // GEMM N
-    const u32 KIN = (KIND == TC_WHT) ? 16u : 32u;       // reals per group and split
+    const u32 NOUT = REAL ? 16u : 32u;      // GEMM N
+    const u32 KIN = REAL ? 16u : 32u;       // reals per group and split
 
     if (warp == 0) tc::tmem_alloc(&tmem_base, TMEM_COLS);
     // operand B: the split step matrix, B[n][KIN*z + kk] = m_z[kk][n] (z = 0, 1, 2)
     for (u32 e = threadIdx.x; e < NOUT * 3 * KIN; e += FT_THREADS) {
         const u32 n = e / (3 * KIN), rest = e % (3 * KIN), z = rest / KIN, kk = rest % KIN;
         __nv_bfloat16 m[3];
-        split3(step_matrix<KIND == TC_CONV ? (int)TC_FFT : KIND>(kk, n), m[0], m[1], m[2]);
+        split3(step_matrix<KIND == TC_CONV ? (int)TC_FFT : REAL ? (int)TC_WHT : KIND>(kk, n), m[0], m[1], m[2]);
         *(__nv_bfloat16 *)(sB + tc::kmajor_offset(n, z * KIN + kk, 3 * KIN)) = m[z];
     }
     for (u32 r = threadIdx.x; r < 1024; r += FT_THREADS) {
@@ -258,7 +260,7 @@ __global__ void __launch_bounds__(FT_THREADS, 3) tc_pass_kernel(TcPassArgs a, un
         // thread's raw bits in flight before the conversions (whose rare out-of-line fallback
         // would otherwise serialise the loads).  Q * ct is even and ct is 1 (pass 1) or even,
         // so a pair never straddles two rows; a.total is a multiple of n >= 2.
-        if (KIND != TC_WHT && a.in32) {
+        if (!REAL && a.in32) {
             // the FP32 intermediate of the previous pass: element f's (re, im) in the 8 bytes of xr[f]
             constexpr u32 PAIRS = FT_TILE / (2 * FT_THREADS);  // 8
             float4 b[PAIRS];
@@ -287,7 +289,7 @@ __global__ void __launch_bounds__(FT_THREADS, 3) tc_pass_kernel(TcPassArgs a, un
                 const u64 f = base + ((u64)(e >> ctl) << a.k0) + (e & ctm);
                 const bool in = e < Q * ct && f < a.total;
                 br[i] = in ? *(const ulonglong2 *)(a.xr + f) : make_ulonglong2(0, 0);
-                bi[i] = (in && KIND != TC_WHT) ? *(const ulonglong2 *)(a.xi + f) : make_ulonglong2(0, 0);
+                bi[i] = (in && !REAL) ? *(const ulonglong2 *)(a.xi + f) : make_ulonglong2(0, 0);
             }
 #pragma unroll
             for (u32 i = 0; i < PAIRS; i++) {
@@ -295,7 +297,7 @@ __global__ void __launch_bounds__(FT_THREADS, 3) tc_pass_kernel(TcPassArgs a, un
                 if (e < Q * ct) {
                     sr[slot(e)] = to_f32(br[i].x);
                     sr[slot(e + 1)] = to_f32(br[i].y);
-                    if (KIND != TC_WHT) {
+                    if (!REAL) {
                         si[slot(e)] = to_f32(bi[i].x);
                         si[slot(e + 1)] = to_f32(bi[i].y);
                     }
@@ -519,6 +521,21 @@ __global__ void __launch_bounds__(FT_THREADS, 3) tc_pass_kernel(TcPassArgs a, un
                 tc::fence_smem_to_async();
                 __syncthreads();
             }
+        } else if constexpr (KIND == TC_WCONV) {
+            ok = steps(std::integral_constant<int, TC_WHT>{});
+            if (ok) {
+                // y <- y * lam * s or y / lam * s (real lam), then the same WHT steps again
+                for (u32 e = threadIdx.x; e < Q * ct; e += FT_THREADS) {
+                    const u64 f = base + ((u64)(e >> ctl) << a.k0) + (e & ctm);
+                    if (f >= a.total) continue;
+                    const u64 li_ = a.lam_all ? f : (f & ((1ull << a.L) - 1));
+                    const float lr = to_f32((u64)__double_as_longlong(a.lr[li_]));
+                    const u32 sl = slot(e);
+                    sr[sl] = a.divide ? sr[sl] * __fdiv_rn(a.lam_scale, lr) : sr[sl] * lr * a.lam_scale;
+                }
+                __syncthreads();
+                ok = steps(std::integral_constant<int, TC_WHT>{});
+            }
         } else {
             ok = steps(std::integral_constant<int, KIND>{});
         }
@@ -526,13 +543,13 @@ __global__ void __launch_bounds__(FT_THREADS, 3) tc_pass_kernel(TcPassArgs a, un
         // store, pairs of adjacent elements as 16-byte stores
         for (u32 e = 2 * threadIdx.x; e < Q * ct; e += 2 * FT_THREADS) {
             const u64 f = base + ((u64)(e >> ctl) << a.k0) + (e & ctm);
-            if (KIND != TC_WHT && a.out32) {
+            if (!REAL && a.out32) {
                 // FP32 intermediate for the next pass, in the bytes of this tile's own xr elements
                 if (f < a.total)
                     *(float4 *)(a.xr + f) = make_float4(sr[slot(e)], si[slot(e)], sr[slot(e + 1)], si[slot(e + 1)]);
             } else if (f < a.total) {
                 *(double2 *)(a.xr + f) = make_double2(to_f64(sr[slot(e)] * a.scale), to_f64(sr[slot(e + 1)] * a.scale));
-                if (KIND != TC_WHT)
+                if (!REAL)
                     *(double2 *)(a.xi + f) =
                         make_double2(to_f64(si[slot(e)] * a.scale), to_f64(si[slot(e + 1)] * a.scale));
             }
@@ -608,14 +625,14 @@ int run_tc(int kind, u64 d1, u64 d2, u64 n_half, double *xr, double *xi, cudaStr
 // pass over the highest bits (forward steps, the pointwise operation, inverse steps), the
 // inverse passes but the first; FP32 intermediates throughout, the orthonormal factors 1/n
 // folded into the pointwise scale
-int run_conv(u64 d1, u64 d2, u64 n_half, const double *lr, const double *li, u64 lam_all, int divide, double scale,
-             double *xr, double *xi, cudaStream_t s, const char *what)
+int run_conv(bool real, u64 d1, u64 d2, u64 n_half, const double *lr, const double *li, u64 lam_all, int divide,
+             double scale, double *xr, double *xi, cudaStream_t s, const char *what)
 {
     QMC_REQUIRE_DOMAIN(n_half > 0 && (n_half & (n_half - 1)) == 0 && n_half <= (1ull << 23),
                        "%s: n = 2*n_half must be a power of two up to 2^24", what);
     const u64 nvec = d1 * d2, n = 2 * n_half;
     if (nvec == 0) return QMC_OK;
-    QMC_REQUIRE(xr && xi && lr && li, "%s: null data pointer", what);
+    QMC_REQUIRE(xr && lr && (real || (xi && li)), "%s: null data pointer", what);
     QMC_REQUIRE(lam_all <= 1, "%s: lam_all is 0 (n values for every vector) or 1 (one per element)", what);
     QMC_REQUIRE((((uintptr_t)xr | (uintptr_t)xi) & 15) == 0, "%s: data arrays must be 16-byte aligned", what);
     unsigned *err = qmcgb::device_error_ptr();
@@ -627,12 +644,15 @@ int run_conv(u64 d1, u64 d2, u64 n_half, const double *lr, const double *li, u64
     passes[np++] = {0, L < 12 ? L : 12};
     for (u32 k0 = 12; k0 < L; k0 += 8) passes[np++] = {k0, (k0 + 8 < L) ? k0 + 8 : L};
     const size_t smem = FT_PAD * 8 + 128 * FT_KS * 2 + 32 * FT_KS * 2 + 1024 * 8;
-    tc_stepB_kernel<<<1, FT_THREADS, 0, s>>>();
-    if (int rc = qmcgb::launch_status(what)) return rc;
+    if (!real) {
+        tc_stepB_kernel<<<1, FT_THREADS, 0, s>>>();
+        if (int rc = qmcgb::launch_status(what)) return rc;
+    }
     // launch order: forward passes 0 .. np-2, the fused pass np-1, inverse passes np-2 .. 0
     for (int li_ = 0; li_ < 2 * np - 1; li_++) {
         const int pi = li_ < np ? li_ : 2 * np - 2 - li_;
-        const int kind = li_ < np - 1 ? TC_FFT : li_ == np - 1 ? TC_CONV : TC_IFFT;
+        const int kind = real ? (li_ == np - 1 ? TC_WCONV : TC_WHT)
+                              : (li_ < np - 1 ? TC_FFT : li_ == np - 1 ? TC_CONV : TC_IFFT);
         const P p = passes[pi];
         TcPassArgs A{};
         A.total = nvec * n;
@@ -650,8 +670,8 @@ int run_conv(u64 d1, u64 d2, u64 n_half, const double *lr, const double *li, u64
         A.xr = xr;
         A.xi = xi;
         A.scale = 1.0f;
-        A.in32 = li_ > 0 ? 1u : 0u;
-        A.out32 = li_ < 2 * np - 2 ? 1u : 0u;
+        A.in32 = (!real && li_ > 0) ? 1u : 0u;
+        A.out32 = (!real && li_ < 2 * np - 2) ? 1u : 0u;
         A.lr = lr;
         A.li = li;
         A.lam_all = (u32)lam_all;
@@ -665,6 +685,12 @@ int run_conv(u64 d1, u64 d2, u64 n_half, const double *lr, const double *li, u64
         } else if (kind == TC_IFFT) {
             if (int rc = qmcgb::raise_smem_limit((const void *)tc_pass_kernel<TC_IFFT>, smem, what)) return rc;
             tc_pass_kernel<TC_IFFT><<<grid, FT_THREADS, smem, s>>>(A, err);
+        } else if (kind == TC_WHT) {
+            if (int rc = qmcgb::raise_smem_limit((const void *)tc_pass_kernel<TC_WHT>, smem, what)) return rc;
+            tc_pass_kernel<TC_WHT><<<grid, FT_THREADS, smem, s>>>(A, err);
+        } else if (kind == TC_WCONV) {
+            if (int rc = qmcgb::raise_smem_limit((const void *)tc_pass_kernel<TC_WCONV>, smem, what)) return rc;
+            tc_pass_kernel<TC_WCONV><<<grid, FT_THREADS, smem, s>>>(A, err);
         } else {
             if (int rc = qmcgb::raise_smem_limit((const void *)tc_pass_kernel<TC_CONV>, smem, what)) return rc;
             tc_pass_kernel<TC_CONV><<<grid, FT_THREADS, smem, s>>>(A, err);
@@ -681,8 +707,15 @@ extern "C" {
 int qmc_tc_fft_mul_ifft(uint64_t d1, uint64_t d2, uint64_t n_half, const double *lam_r, const double *lam_i,
                         uint64_t lam_per_element, int divide, double scale, double *xr, double *xi, qmc_stream_t s)
 {
-    return run_conv(d1, d2, n_half, lam_r, lam_i, lam_per_element, divide, scale, xr, xi, QMC_STREAM(s),
+    return run_conv(false, d1, d2, n_half, lam_r, lam_i, lam_per_element, divide, scale, xr, xi, QMC_STREAM(s),
                     "tc_fft_mul_ifft");
+}
+
+int qmc_tc_fwht_mul_fwht(uint64_t d1, uint64_t d2, uint64_t n_half, const double *lam, uint64_t lam_per_element,
+                         int divide, double scale, double *x, qmc_stream_t s)
+{
+    return run_conv(true, d1, d2, n_half, lam, nullptr, lam_per_element, divide, scale, x, nullptr, QMC_STREAM(s),
+                    "tc_fwht_mul_fwht");
 }
 
 int qmc_tc_fft_bro_1d(uint64_t d1, uint64_t d2, uint64_t n_half, double *xr, double *xi, qmc_stream_t s)
