@@ -20,10 +20,11 @@
 // word, finished by an insertion sort of runs on the full key; the prefix
 // lengths of sorted neighbours in bits; the bottom-up tree pass of
 // nus_dev.cuh (bit-level L; the digit L is L / w); per point the number of
-// permutations it draws and their offsets; the draws, one thread per
-// generator (Fisher-Yates on arange(b) with numpy's masked rejection); each
-// point's digits through its owners' permutations, level by level on the way
+// permutations it draws and their offsets; the draws, one CTA per generator
+// (the swap indices of numpy's Fisher-Yates from the stream, fy_stream.cuh),
+// then the swaps themselves, one thread per permutation; each point's digits through its owners' permutations, level by level on the way
 // up its ancestors.
+#include "fy_stream.cuh"
 #include "nus_dev.cuh"
 
 #include <vector>
@@ -282,79 +283,53 @@ __global__ void __launch_bounds__(NUS_THREADS) gdn_hist_rows_kernel(NusDims m, c
 
 // ---- the draws: Generator.permutation(b) per level ---------------------------------
 // numpy's Generator.shuffle walks i = b-1 .. 1 and swaps position i with
-// random_interval(i): a 32-bit draw masked to the bits of i, drawn again
-// while above i.  The stream is serial per generator, the swaps are not: one
-// thread per generator runs the stream and writes each accepted index j_i
-// into entry i of its row (rows in draw order: the phantom's, then each
-// point's levels, as the offsets lay them out); then one thread per row
-// replays the swaps on arange(b) in shared memory and writes the permutation
-// over the indices.
+// random_interval(i).  The stream is serial per generator, the swaps are not:
+// one CTA per generator runs the stream (fy_stream.cuh: a producer lane and
+// decoding warps) and writes each accepted index j_i into entry i of its row
+// (rows in draw order: the phantom's, then each point's levels, as the offsets
+// lay them out); then one thread per row replays the swaps on arange(b) in
+// shared memory and writes the permutation over the indices.
 
-constexpr int INTERVAL_TRIES = 256;  // each try fails with probability below 1/2
+// the rows of one generator this call draws: entry i of row q at row0[q*b + i]
+struct GdnRows {
+    unsigned short *row0;
+    u32 b;
+    u64 rows;
+    bool given;
+    __device__ bool next(u32 &bo, u64 &ro)
+    {
+        if (given) return false;
+        given = true;
+        bo = b;
+        ro = rows;
+        return true;
+    }
+    __device__ void put(u64 q, u32 i, u32 j) { row0[q * b + i] = (unsigned short)j; }
+};
 
-__global__ void __launch_bounds__(32) gdn_stream_kernel(NusDims m, GdnArgs a, u64 *__restrict__ states,
-                                                        const u64 *__restrict__ offs, const u64 *__restrict__ tot,
-                                                        const u64 *__restrict__ base,
-                                                        unsigned short *__restrict__ perms, unsigned int *err)
+__global__ void __launch_bounds__(FY_THREADS) gdn_stream_kernel(NusDims m, GdnArgs a, u64 *__restrict__ states,
+                                                                const u64 *__restrict__ offs,
+                                                                const u64 *__restrict__ tot,
+                                                                const u64 *__restrict__ base,
+                                                                unsigned short *__restrict__ perms, unsigned int *err)
 {
+    __shared__ FyShared sh;
     const u32 g = blockIdx.x;
-    if (threadIdx.x != 0 || g >= m.S) return;
-    u64 *st = states + (m.s0 + g) * 6;
-    Sfc64 r{st[0], st[1], st[2], st[3], st[5], (u32)(st[4] != 0)};
+    if (g >= m.S) return;
     u32 b, w;
     gdn_base_of(m, a, m.s0 + g, b, w);
     if (b < 2 || b > 65536) {  // reported by the keys pass; nothing to draw from
-        atomicOr(err, 1u);
+        if (threadIdx.x == 0) atomicOr(err, 1u);
         return;
     }
     const u64 rows = tot[g] / b;
-    u64 q = old_entries(m, offs, tot, g) / b;  // rows before q came from earlier calls
-    unsigned short *row = perms + base[g] + q * b;
-    u32 i = b - 1, mask = 0xFFFFFFFFu >> __clz((int)i), fails = 0;
-    bool ok = true;
-    // one 32-bit candidate; true once the last row is complete
-    auto feed = [&](u32 x) -> bool {
-        u32 jv = x & mask;
-        bool acc = jv <= i;
-        if (!acc && ++fails > INTERVAL_TRIES) {  // a broken stream: record it, stay bounded
-            ok = false;
-            acc = true;
-            jv = 0;
-        }
-        if (!acc) return false;
-        fails = 0;
-        row[i] = (unsigned short)jv;
-        if (--i == 0) {
-            if (++q == rows) return true;
-            row += b;
-            i = b - 1;
-        }
-        mask = 0xFFFFFFFFu >> __clz((int)i);
-        return false;
-    };
-    if (q < rows) {
-        bool done = false;
-        if (r.has) {  // the buffered upper half of the last 64-bit output comes first
-            r.has = 0;
-            done = feed((u32)r.half);
-        }
-        while (!done) {
-            const u64 y = r.next64();
-            r.half = y >> 32;  // numpy keeps the high half in its buffer word even once it is used
-            if (feed((u32)y)) {
-                r.has = 1;
-                break;
-            }
-            done = feed((u32)(y >> 32));
-        }
-    }
-    if (!ok) atomicOr(err, 16u);
-    st[0] = r.a;
-    st[1] = r.b;
-    st[2] = r.c;
-    st[3] = r.w;
-    st[4] = r.has;
-    st[5] = r.half;
+    const u64 q0 = old_entries(m, offs, tot, g) / b;  // rows before q0 came from earlier calls
+    if (q0 >= rows) return;
+    GdnRows R{perms + base[g] + q0 * b, b, rows - q0, false};
+    if (b <= FY_SMALL_MAX)
+        fy_stream_small(sh, states + (m.s0 + g) * 6, b, rows - q0, R, err, 16u);
+    else
+        fy_stream(sh, states + (m.s0 + g) * 6, R, err, 16u);
 }
 
 // rows of one generator per blockIdx.y; thread t of a block holds its row's
@@ -523,9 +498,12 @@ int qmc_gdn_nested_uniform_scramble(uint64_t r, uint64_t n, uint64_t d, uint64_t
     const u64 per = gdn_layout(nullptr, 1, NP, NT).bytes;
     QMC_REQUIRE(work_bytes >= per, "gdn_nested_uniform_scramble: workspace of %llu bytes, one generator needs %llu",
                 (unsigned long long)work_bytes, (unsigned long long)per);
+    // the most generators whose sub-arrays fit; work_bytes / per alone comes out one short for
+    // a workspace sized for exactly that many, as the fixed words count once in any layout
+    const u64 cap = G < 65535 ? G : 65535;
     u64 count = work_bytes / per;
-    if (count > G) count = G;
-    if (count > 65535) count = 65535;
+    if (count > cap) count = cap;
+    while (count < cap && gdn_layout(nullptr, count + 1, NP, NT).bytes <= work_bytes) count++;
     while (count > 1 && gdn_layout(nullptr, count, NP, NT).bytes > work_bytes) count--;
     GdnWork w = gdn_layout((char *)work, count, NP, NT);
     cudaStream_t st = QMC_STREAM(s);
@@ -678,7 +656,7 @@ int qmc_gdn_nested_uniform_scramble(uint64_t r, uint64_t n, uint64_t d, uint64_t
             rc = qmcgb::launch_status("gdn_nus earlier rows");
             if (rc) return rc;
         }
-        gdn_stream_kernel<<<m.S, 32, 0, st>>>(m, a, stw, w.offs, w.tot, w.base, pc, err);
+        gdn_stream_kernel<<<m.S, FY_THREADS, 0, st>>>(m, a, stw, w.offs, w.tot, w.base, pc, err);
         rc = qmcgb::launch_status("gdn_nus draws");
         if (rc) return rc;
         if (most_rows > 0) {

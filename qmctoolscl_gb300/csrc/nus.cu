@@ -331,9 +331,12 @@ int qmc_dnb2_nested_uniform_scramble(uint64_t r, uint64_t n, uint64_t d, uint64_
     const u64 per = nus_layout(nullptr, 1, NP, NT).bytes;
     QMC_REQUIRE(work_bytes >= per, "dnb2_nested_uniform_scramble: workspace of %llu bytes, one generator needs %llu",
                 (unsigned long long)work_bytes, (unsigned long long)per);
+    // the most generators whose sub-arrays fit; work_bytes / per alone comes out one short for
+    // a workspace sized for exactly that many, as the fixed words count once in any layout
+    const u64 cap = G < 65535 ? G : 65535;
     u64 count = work_bytes / per;
-    if (count > G) count = G;
-    if (count > 65535) count = 65535;
+    if (count > cap) count = cap;
+    while (count < cap && nus_layout(nullptr, count + 1, NP, NT).bytes <= work_bytes) count++;
     while (count > 1 && nus_layout(nullptr, count, NP, NT).bytes > work_bytes) count--;
     NusWork w = nus_layout((char *)work, count, NP, NT);
     cudaStream_t st = QMC_STREAM(s);

@@ -5,18 +5,20 @@
 //
 // A Generator's stream is serial (SFC64 has no jump-ahead), so one thread runs
 // it: it draws exactly what numpy draws, in numpy's order, and stores each
-// value where the helper puts it.  What does not depend on the stream runs
-// wide: the zero fill before it, and for the permutation helpers the
-// Fisher-Yates swaps themselves -- the stream thread only writes the swap
-// index j_i into entry i of each row, and one thread per row then replays
-// the swaps on arange(b) in shared memory and writes the permutation over
-// the indices.
+// value where the helper puts it.  The permutation helpers, which draw the
+// most, run their stream in one CTA instead: a producer lane steps the
+// generator and a warp decides which outputs the masked rejection accepts, 32
+// at a time (fy_stream.cuh).  What does not depend on the stream runs wide:
+// the zero fill before it, and for the permutation helpers the Fisher-Yates
+// swaps themselves -- the stream only writes the swap index j_i into entry i
+// of each row, and one thread per row then replays the swaps on arange(b) in
+// shared memory and writes the permutation over the indices.
 //
 // Every rejection loop is bounded; a loop that runs out (an impossible stream)
 // sets bit 32 of the device error word.  A base for which numpy would raise
 // (below 2 for the scrambling matrices, 0 for the shifts) or one above the
 // permutation width sets bit 128 and stops the stream there.
-#include "numpy_rng.cuh"
+#include "fy_stream.cuh"
 
 namespace {
 
@@ -122,30 +124,64 @@ __global__ void __launch_bounds__(32) gdn_shift_rand_kernel(u64 *state, u64 r, u
 
 // the swap indices of Generator.permutation(b) for every row: rows of `width`
 // entries, row q = (l*d + j)*levels + t with base b(l, j) (bases == nullptr:
-// one base b0 for every row); entry i of a row gets j_i, i = b-1 .. 1
-__global__ void __launch_bounds__(32) perm_stream_kernel(u64 *state, u64 r, u64 d, u64 levels, u64 r_b,
-                                                         const u64 *bases, u64 b0, u64 width, u64 *out,
-                                                         unsigned *err)
-{
-    if (threadIdx.x != 0) return;
-    Sfc64 g;
-    g.load(state);
-    bool bad = false;
-    for (u64 l = 0; l < r; l++)
-        for (u64 j = 0; j < d; j++) {
-            const u64 bb = bases ? base_of(bases, r_b, d, l, j) : b0;
-            if (bb > width) {  // a row holds `width` entries
-                atomicOr(err, ERR_BASE);
-                g.store(state);
-                return;
-            }
-            const u32 b = (u32)bb;
-            u64 *row = out + (l * d + j) * levels * width;
-            for (u64 t = 0; t < levels; t++, row += width)
-                for (u32 i = b - 1; i >= 1 && b >= 2; i--) row[i] = g.interval(i, &bad);
+// one base b0 for every row); entry i of a row gets j_i, i = b-1 .. 1.  One
+// CTA runs the stream (fy_stream.cuh), the (l, j) pairs as runs of rows; a
+// base above the row width stops the stream there.  Rows that all share one
+// base of at most FY_SMALL_MAX take the small-base decoder as one run.
+struct PermRows {
+    const u64 *bases;
+    u64 r, d, levels, r_b, b0, width;
+    u64 *out;
+    unsigned *err;
+    u64 lj;   // the next (l, j) pair
+    u64 *cur;  // rows of the current pair
+    __device__ bool next(u32 &b, u64 &rows)
+    {
+        if (lj >= r * d) return false;
+        const u64 bb = bases ? base_of(bases, r_b, d, lj / d, lj % d) : b0;
+        if (bb > width) {  // a row holds `width` entries
+            atomicOr(err, ERR_BASE);
+            lj = r * d;
+            return false;
         }
-    if (bad) atomicOr(err, ERR_STREAM);
-    g.store(state);
+        cur = out + lj * levels * width;
+        lj++;
+        b = (u32)bb;
+        rows = levels;
+        return true;
+    }
+    __device__ void put(u64 q, u32 i, u32 j) { cur[q * width + i] = j; }
+};
+
+// all rows of one small base: row q at out + q*width
+struct PermRowsFlat {
+    u64 *out;
+    u64 width;
+    __device__ void put(u64 q, u32 i, u32 j) { out[q * width + i] = j; }
+};
+
+__global__ void __launch_bounds__(FY_THREADS) perm_stream_kernel(u64 *state, u64 r, u64 d, u64 levels, u64 r_b,
+                                                                 const u64 *bases, u64 b0, u64 width, u64 *out,
+                                                                 unsigned *err)
+{
+    __shared__ FyShared sh;
+    __shared__ u64 one_base;  // the base of every row, or 0
+    if (threadIdx.x == 0) {
+        u64 bb = bases ? base_of(bases, r_b, d, 0, 0) : b0;
+        if (bases)
+            for (u64 lj = 0; lj < (r < r_b ? r : r_b) * d && bb; lj++)
+                if (base_of(bases, r_b, d, lj / d, lj % d) != bb) bb = 0;
+        one_base = bb;
+    }
+    __syncthreads();
+    const u64 bb = one_base;
+    if (bb >= 2 && bb <= FY_SMALL_MAX && bb <= width) {  // one run of a small base
+        PermRowsFlat P{out, width};
+        fy_stream_small(sh, state, (u32)bb, r * d * levels, P, err, ERR_STREAM);
+    } else {
+        PermRows R{bases, r, d, levels, r_b, b0, width, out, err, 0, out};
+        fy_stream(sh, state, R, err, ERR_STREAM);
+    }
 }
 
 // ---- wide passes ------------------------------------------------------------------
@@ -190,7 +226,7 @@ int permutations(u64 *state, u64 r, u64 d, u64 levels, u64 r_b, const u64 *bases
     unsigned *err = qmcgb::device_error_ptr();
     QMC_REQUIRE(err, "device error word unavailable");
     if (int rc = qmcgb::cuda_status(cudaMemsetAsync(out, 0, rows * bmax * 8, st), "permutation fill")) return rc;
-    perm_stream_kernel<<<1, 32, 0, st>>>(state, r, d, levels, r_b, bases, b0, bmax, out, err);
+    perm_stream_kernel<<<1, FY_THREADS, 0, st>>>(state, r, d, levels, r_b, bases, b0, bmax, out, err);
     if (int rc = one_thread("perm_stream_kernel")) return rc;
     u32 T = 128;
     while (T > 1 && (u64)T * bmax * 2 > 98304) T >>= 1;
