@@ -1212,7 +1212,7 @@ def run_gdn_plain(args):
     import qmctoolscl_gb300 as q
     from qmctoolscl_gb300 import _ffi
     lib = _ffi.lib()
-    r, n = 32, 1 << 18
+    r, n = (4 if args.small else 32), 1 << 18  # small: the gdn chain only, r = 4 (0.5 GB digit arrays)
     st = torch.cuda.current_stream()
     h = st.cuda_stream
     U = np.uint64
@@ -1261,6 +1261,8 @@ def run_gdn_plain(args):
         assert np.array_equal(got.view(U), want[:, 0].view(U)), "plain gdn chain differs from the oracle"
         res["b=%d (tmax=%d, mmax=%d)" % (b, tmax, mmax)] = per
     gdn_ms = total_ms
+    if args.small:
+        return {"small": True, "r": r, "kernels": res}
     # the other plain families at their benchmark shapes: base-2 nets (r=64, n=2^20, d=32, from the
     # LMS + interlacing inputs) and rank-1 lattices (r=16, n=2^20, d=64)
     rng3 = np.random.Generator(np.random.SFC64(3))

@@ -219,17 +219,25 @@ __global__ void __launch_bounds__(THREADS) gdn_gen_kernel(u64 r, u64 n, u64 d, u
 // digit times an entry cannot wrap, so reducing first gives the reference's
 // digits).  Per group, the index splits as hi * b^K + lo with b^K >= 32: the
 // 32 points have at most two distinct hi, whose contributions to every
-// output digit the warp computes together; each lane adds its K low digits.
-// Digits are staged per 32-digit chunk in shared memory and written as
-// contiguous runs.  A CTA outside the case runs the per-element code above
-// for its block instead.
+// output digit the warp computes together.  When b^K * tmax words fit, the
+// low digits' contributions to every output digit, reduced mod b, are a
+// shared-memory table over lo built once per CTA, so an output word is two
+// table reads, an add, a conditional subtract of b and a store, the words of
+// a group written in order by consecutive lanes (coalesced runs); otherwise
+// each lane adds its K low digits and the digits are staged per 32-digit
+// chunk in shared memory.  A CTA outside the case runs the per-element code
+// above for its block instead.
 constexpr u32 GT_MAX_CW = 8192;    // matrix words staged per CTA (32 KB as u32)
 constexpr u32 GT_MAX_TMAX = 256;
 constexpr u32 GT_WARPS = THREADS / 32;
 
+constexpr u32 GT_LT_WORDS = GT_WARPS * 32 * 33;  // the low-digit table, or the staging of the general loop
+constexpr u32 GT_MAX_HD = 64;                      // high digits per index (indices below 2^32)
+
 inline size_t gt_smem(u64 mmax, u64 tmax)
 {
-    return (mmax * tmax + GT_WARPS * 2 * tmax + GT_WARPS * 32 * 33) * sizeof(u32);
+    return (((mmax * tmax + 3) & ~3ull) + GT_WARPS * 2 * tmax + GT_LT_WORDS + GT_WARPS * (64 + 2 * GT_MAX_HD)) *
+           sizeof(u32);
 }
 
 __global__ void __launch_bounds__(THREADS) gdn_gen_tiled_kernel(u64 r, u64 n, u64 d, u64 r_b, u64 mmax, u64 tmax,
@@ -239,8 +247,10 @@ __global__ void __launch_bounds__(THREADS) gdn_gen_tiled_kernel(u64 r, u64 n, u6
 {
     extern __shared__ __align__(16) u32 gsm[];
     u32 *Cs = gsm;                                  // [mmax][tmax] entries mod b
-    u32 *hi_tab = Cs + mmax * tmax;                 // [warp][2][tmax]
-    u32 *stage = hi_tab + GT_WARPS * 2 * tmax;      // [warp][32][33]
+    u32 *hi_tab = Cs + ((mmax * tmax + 3) & ~3ull); // [warp][2][tmax] (after the matrix, 16-byte aligned)
+    u32 *stage = hi_tab + GT_WARPS * 2 * tmax;      // [warp][32][33], or the low-digit table [b^K][tmax]
+    u32 *ptab = stage + GT_LT_WORDS;                // [warp][32][2] per point: high-sum and low-table offsets
+    u32 *hdig = ptab + GT_WARPS * 64;               // [warp][2][GT_MAX_HD] high digits of the two high parts
     __shared__ u32 big;
     const u64 unit = unit_off + blockIdx.y;         // = l * d + j
     if (unit >= r * d) return;
@@ -295,6 +305,70 @@ __global__ void __launch_bounds__(THREADS) gdn_gen_tiled_kernel(u64 r, u64 n, u6
     const FastDiv32 fK = fastdiv32_make(bK);
     const u32 KL = K < M ? K : M;  // low digits that can be nonzero (indices below b^mmax)
     u32 *ht = hi_tab + warp * 2 * T;
+    if ((u64)bK * T <= GT_LT_WORDS && M - KL <= GT_MAX_HD && T >= 2) {
+        // LT[lo * T + t]: the low digits' part of output digit t, mod b, for every lo < b^K
+        u32 *LT = stage;
+        for (u32 w = threadIdx.x; w < bK * T; w += THREADS) {
+            const u32 lo = w / T, t = w - lo * T;
+            u32 x = lo, acc = 0;
+            for (u32 k = 0; k < KL; k++) {
+                const u32 q = x / b32;
+                acc += (x - q * b32) * Cs[k * T + t];  // < 5 * 4096^2
+                x = q;
+            }
+            LT[w] = acc % b32;
+        }
+        __syncthreads();
+        u32 *pw = ptab + warp * 64, *hd = hdig + warp * 2 * GT_MAX_HD;
+        const u32 HD = M - KL;                               // high digits that can be nonzero
+        const u32 mT = (u32)((0x100000000ull + T - 1) / T);  // e / T = umulhi(e, mT) for e < 2^13
+        const u64 dT = d * tmax;
+        for (u64 g = g0 + warp; g < g1; g += GT_WARPS) {
+            const u64 i0 = g * 32;
+            const u32 base = (u32)(n_start + i0);
+            const u32 itrue = i0 + lane < n ? base + lane : base;
+            const u32 h0 = fd_div(fK, base), hi = fd_div(fK, itrue);
+            __syncwarp();  // the previous group's reads of hd, ht and pw are done
+            // the base-b digits of the two high parts h0 and h0 + 1, lane k digit k
+            for (u32 k = lane; k < HD; k += 32) {
+#pragma unroll
+                for (u32 sx = 0; sx < 2; sx++) {
+                    u32 h = h0 + sx;
+                    for (u32 e = 0; e < k && h; e++) h = fd_div(fb, h);
+                    hd[sx * GT_MAX_HD + k] = h - fd_div(fb, h) * b32;
+                }
+            }
+            pw[2 * lane] = (hi - h0) * T;
+            pw[2 * lane + 1] = (itrue - hi * bK) * T;
+            __syncwarp();
+            // high-digit sums of both high parts for every output digit (gdn_gen_natural.c:37-50, k >= K)
+            for (u32 t = lane; t < T; t += 32) {
+                u32 a0 = 0, a1 = 0;
+                for (u32 k = 0; k < HD; k++) {
+                    const u32 c = Cs[(KL + k) * T + t];
+                    a0 += hd[k] * c;  // < 64 * 4096^2 = 2^30
+                    a1 += hd[GT_MAX_HD + k] * c;
+                }
+                ht[t] = fd_mod(fb, a0);
+                ht[T + t] = fd_mod(fb, a1);
+            }
+            __syncwarp();
+            // the group's npts x T words in output order, one per lane
+            const u32 words = (u32)min((u64)32, n - i0) * T;
+            u64 *ot = out + i0 * dT;
+            for (u32 e = lane; e < words; e += 32) {
+                const u32 p = __umulhi(e, mT), t = e - p * T;
+                const uint2 po = *(const uint2 *)&pw[2 * p];
+                u32 acc = ht[po.x + t] + LT[po.y + t];  // both below b
+                acc = min(acc, acc - b32);
+                if (dT == T)
+                    ot[e] = acc;
+                else
+                    ot[(u64)p * dT + t] = acc;
+            }
+        }
+        return;
+    }
     u32 *sg = stage + warp * 32 * 33;
     for (u64 g = g0 + warp; g < g1; g += GT_WARPS) {
         const u64 i0 = g * 32;

@@ -231,6 +231,27 @@ def test_gdn_pipeline_random(big_c):
     assert same_bits(*xf)
 
 
+@pytest.mark.parametrize("b", [2, 3, 5, 31, 32, 33, 541, 1021, 4093])
+@pytest.mark.parametrize("d,n_start", [(1, 0), (1, 45), (3, 1000)])
+def test_gdn_gen_natural_tiled_forms(b, d, n_start):
+    """gdn_gen_natural on a base-b Halton-like matrix with random unit-triangular
+    scrambling, tmax = ceil(64/log2 b): the low-digit table form (b^K * tmax
+    small), the staged form (large b) and both output layouts (d = 1: the
+    group's words in order; d > 1: runs per point), ragged n, against the
+    oracle bit for bit."""
+    rng = np.random.Generator(np.random.SFC64(b * 7 + d))
+    r, n = 2, (1 << 13) + 17
+    tmax = int(np.ceil(64 / np.log2(b)))
+    mmax = 1
+    while b ** mmax < n_start + n:
+        mmax += 1
+    bases = np.full((1, d), b, U)
+    C = rng.integers(0, b, (r, d, mmax, tmax), dtype=U)
+    x = both("gdn_gen_natural", [U(r), U(n), U(d), U(1), U(mmax), U(tmax), U(n_start), bases, C,
+                                 poison((r, n, d, tmax), U)], ["xdig"])["xdig"]
+    assert same_bits(*x)
+
+
 @pytest.mark.parametrize("tmax", [1, 12, 64, 80])
 def test_gdn_integer_to_float_depths(tmax):
     rng = np.random.Generator(np.random.SFC64(tmax))
