@@ -369,17 +369,27 @@ __global__ void __launch_bounds__(FT_THREADS, 3) tc_pass_kernel(TcPassArgs a, un
                         const u32 cgrp = ((u32)base + (qlo << a.k0) + cc) & ((1u << k) - 1);
                         const u32 cg = cgrp << (28 - k), cgh = half ? cg : 0u;
                         u32 pr[3][4], pim[3][4];  // [split][pair of members]: two BF16 per word
+                        // member pp+1's twiddle is member pp's times w^8 (its angle is 8*cg more): one
+                        // table lookup per pair, plus w^8 once, and one complex product
+                        float w8r = 1.0f, w8i = 0.0f;
+                        if (SK == TC_FFT && k > 0) twiddle_turn(tab, 8u * cg, k + 4, -1.0f, w8r, w8i);
 #pragma unroll
                         for (u32 pp = 0; pp < 8; pp += 2) {
                             float xr2[2], xi2[2];
+                            float wr = 1.0f, wi = 0.0f;
+                            if (SK == TC_FFT && k > 0 && (half || pp))
+                                twiddle_turn(tab, cgh + 2u * cg * (brev4(pp) >> 1), k + 4, -1.0f, wr, wi);
 #pragma unroll
                             for (u32 h = 0; h < 2; h++) {
                                 const u32 e = slot(e0 + (pp + h) * S);
                                 xr2[h] = sr[e];
                                 xi2[h] = (SK == TC_WHT) ? 0.0f : si[e];
                                 if (SK == TC_FFT && k > 0) {  // pre-twiddle w^br(p) (w = 1 on the first step)
-                                    float wr, wi;
-                                    twiddle_turn(tab, cgh + 2u * cg * (brev4(pp + h) >> 1), k + 4, -1.0f, wr, wi);
+                                    if (h) {
+                                        const float t = wr * w8r - wi * w8i;
+                                        wi = wr * w8i + wi * w8r;
+                                        wr = t;
+                                    }
                                     const float tr = xr2[h] * wr - xi2[h] * wi;
                                     xi2[h] = xr2[h] * wi + xi2[h] * wr;
                                     xr2[h] = tr;
@@ -474,11 +484,18 @@ __global__ void __launch_bounds__(FT_THREADS, 3) tc_pass_kernel(TcPassArgs a, un
                         const u32 cgrp = ((u32)base + (qlo << a.k0) + cc) & ((1u << k) - 1);
                         const u32 cg = cgrp << (28 - k), cgh = half ? cg : 0u;
                         if (k > 0) {
+                            float w8r, w8i, wr = 1.0f, wi = 0.0f;  // as in the forward step: w^8 per pair
+                            twiddle_turn(tab, 8u * cg, k + 4, 1.0f, w8r, w8i);
 #pragma unroll
                             for (u32 pp = 0; pp < 8; pp++) {
                                 const u32 e = slot(e0 + pp * S);
-                                float wr, wi;
-                                twiddle_turn(tab, cgh + 2u * cg * (brev4(pp) >> 1), k + 4, 1.0f, wr, wi);
+                                if (pp & 1) {
+                                    const float t = wr * w8r - wi * w8i;
+                                    wi = wr * w8i + wi * w8r;
+                                    wr = t;
+                                } else if (half || pp) {
+                                    twiddle_turn(tab, cgh + 2u * cg * (brev4(pp) >> 1), k + 4, 1.0f, wr, wi);
+                                }
                                 const float xr_ = sr[e], xi_ = si[e];
                                 sr[e] = xr_ * wr - xi_ * wi;
                                 si[e] = xr_ * wi + xi_ * wr;
