@@ -104,14 +104,9 @@ __device__ __forceinline__ u32 fy_acquire(const volatile u32 *p)
 // thread wrote (or saw, after __syncwarp) before is visible to whoever acquires the value
 __device__ __forceinline__ void fy_publish(volatile u32 *p, u32 v)
 {
-#ifdef FY_PUBLISH_FENCE
-    __threadfence_block();
-    *p = v;
-#else
     asm volatile("st.release.cta.shared::cta.u32 [%0], %1;" ::"r"((u32)__cvta_generic_to_shared((const void *)p)),
                  "r"(v)
                  : "memory");
-#endif
 }
 
 // lane 0 waits until *ctr > c; false (for the whole warp) once the stream stopped or the wait
