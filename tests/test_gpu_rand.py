@@ -104,17 +104,24 @@ def test_gdn_digital_shifts_with_64_bit_lemire_rejections():
 
 
 @pytest.mark.parametrize("bases", [np.array([[2, 3, 5, 541]], U), np.array([[1, 2], [17, 3]], U),
-                                   np.array([[65536, 3]], U)])
-def test_gdn_get_digital_permutations(bases):
+                                   np.array([[65536, 3]], U), np.array([[5, 5, 5]], U), np.array([[33, 34]], U),
+                                   np.array([[19], [19]], U)])
+@pytest.mark.parametrize("pre32", [0, 1])
+def test_gdn_get_digital_permutations(bases, pre32):
+    """mixed bases (runs of rows of changing base), one small base for every
+    row (the all-start-positions decoder over merged rows), bases either side
+    of its limit of 33, with and without a buffered half"""
     r_b, d = bases.shape
-    ga, gb = _pair(600 + int(bases.max()) % 97, 1)
+    ga, gb = _pair(600 + int(bases.max()) % 97, pre32)
     _same(q.gdn_get_digital_permutations(ga, 2, d, 3, r_b, bases),
           q.gdn_get_digital_permutations(gb, 2, d, 3, r_b, bases, device="cuda"), ga, gb)
 
 
-@pytest.mark.parametrize("n,b", [(1, 1), (5, 2), (40, 7), (300, 541), (3, 4097)])
-def test_random_uint64_permutations(n, b):
-    ga, gb = _pair(700 + b)
+@pytest.mark.parametrize("n,b", [(1, 1), (5, 2), (40, 7), (300, 541), (3, 4097), (2000, 19), (70, 33), (70, 34),
+                                 (5000, 2)])
+@pytest.mark.parametrize("pre32", [0, 1])
+def test_random_uint64_permutations(n, b, pre32):
+    ga, gb = _pair(700 + b, pre32)
     _same(q.random_uint64_permutations(ga, n, b), q.random_uint64_permutations(gb, n, b, device="cuda"), ga, gb)
 
 
