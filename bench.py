@@ -514,6 +514,33 @@ def gpu_ms(fn, steps, warmup, stream):
     return e0.elapsed_time(e1) / steps
 
 
+def graph_ms(fn_h, steps, warmup):
+    """Average milliseconds per call of fn_h(stream_handle) when `steps` calls
+    are captured in one CUDA graph and replayed: the device time of a
+    workload too small to cover its host launch overhead (CUDA events on the
+    replay stream)."""
+    import torch
+    side = torch.cuda.Stream()
+    side.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(side):
+        for _ in range(warmup):
+            fn_h(side.cuda_stream)
+    torch.cuda.synchronize()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g, stream=side):
+        for _ in range(steps):
+            fn_h(side.cuda_stream)
+    g.replay()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with torch.cuda.stream(side):
+        e0.record(side)
+        g.replay()
+        e1.record(side)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / steps
+
+
 def dev_tensor(a):
     import torch
     a = np.ascontiguousarray(a)
@@ -564,18 +591,23 @@ def run_net_plain(args):
     st = torch.cuda.current_stream()
     h = st.cuda_stream
 
-    def plain():
-        _ffi.check(lib.qmc_dnb2_gen_natural(r, n, d, 0, m, Cd.data_ptr(), xb.data_ptr(), h), "gen")
+    def plain_on(hs):
+        _ffi.check(lib.qmc_dnb2_gen_natural(r, n, d, 0, m, Cd.data_ptr(), xb.data_ptr(), hs), "gen")
         _ffi.check(lib.qmc_dnb2_digital_shift(r, n, d, r, ld.data_ptr(), xb.data_ptr(), sd.data_ptr(),
-                                              xrb.data_ptr(), h), "shift")
-        _ffi.check(lib.qmc_dnb2_integer_to_float(r, n, d, td.data_ptr(), xrb.data_ptr(), x.data_ptr(), h), "float")
+                                              xrb.data_ptr(), hs), "shift")
+        _ffi.check(lib.qmc_dnb2_integer_to_float(r, n, d, td.data_ptr(), xrb.data_ptr(), x.data_ptr(), hs), "float")
 
-    def fused():
+    def fused_on(hs):
         _ffi.check(lib.qmc_dnb2_gen_fused(r, n, d, 0, m, Cd.data_ptr(), r, 0, ld.data_ptr(), r, sd.data_ptr(),
-                                          td.data_ptr(), xrb.data_ptr(), x.data_ptr(), h), "fused")
+                                          td.data_ptr(), xrb.data_ptr(), x.data_ptr(), hs), "fused")
 
-    ms_plain = gpu_ms(plain, args.steps, args.warmup, st)
-    ms_fused = gpu_ms(fused, args.steps, args.warmup, st)
+    # one call per step from Python (the host's launch overhead is inside: 16.8 MB is about 2.5 us of
+    # HBM time), and the same calls replayed from one captured CUDA graph (the device's time)
+    ms_plain_eager = gpu_ms(lambda: plain_on(h), args.steps, args.warmup, st)
+    ms_fused_eager = gpu_ms(lambda: fused_on(h), args.steps, args.warmup, st)
+    graph_steps = max(args.steps, 20)
+    ms_plain = graph_ms(plain_on, graph_steps, args.warmup)
+    ms_fused = graph_ms(fused_on, graph_steps, args.warmup)
     # parity of the timed outputs against the oracle chain
     import oracle
     U = np.uint64
@@ -609,18 +641,23 @@ def run_net_plain(args):
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_fused, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "u64+f64", "data": "synthetic (np.random.SFC64(1))",
             "config": {"workload": "base-2 digital net, natural order + digital shift + float, r=1, d=16, m=16 "
-                                   "(n=65536), tmax=63 (fused kernel, both outputs)", "r": r, "n": n, "d": d},
+                                   "(n=65536), tmax=63 (fused kernel, both outputs; steps replayed from one "
+                                   "captured CUDA graph)", "r": r, "n": n, "d": d},
             "roofline": dict(roofline(16.0 * r * n * d, ms_fused), kernel="dnb2_gen_kernel (fused shift + float)",
-                             note="16.8 MB per launch: launch-latency bound, below the HBM ramp; the output fits "
-                                  "in the 129 MB L2, so one launch's DRAM bytes do not measure it (traffic null)"),
+                             note="16.8 MB per launch, below the HBM ramp: launch-latency bound even from a graph; "
+                                  "the output fits in the 129 MB L2, so one launch's DRAM bytes do not measure it "
+                                  "(traffic null)"),
+            "eager": {"ms_per_step": ms_fused_eager, "points_per_s": pts / (ms_fused_eager / 1e3),
+                      "plain_ms_per_step": ms_plain_eager,
+                      "note": "one ctypes call per step from Python: the host's launch overhead is inside"},
             "plain": {"ms_per_step": ms_plain, "points_per_s": pts / (ms_plain / 1e3), "launches_per_step": 3,
-                      "fused_speedup": ms_plain / ms_fused},
+                      "fused_speedup": ms_plain / ms_fused, "note": "the three reference calls, graph replay"},
             "e2e": {"value": pts / t_e2e, "unit": "points/s", "ms_per_step": 1e3 * t_e2e,
                     "h2d_bytes_per_step": C.nbytes + shifts.nbytes + 16 + 2 * r * n * d * 8,
                     "d2h_bytes_per_step": 3 * r * n * d * 8,
                     "path": "drop-in API, numpy arrays, dnb2_gen_natural -> dnb2_digital_shift -> "
                             "dnb2_integer_to_float"},
-            "gpu_launches": args.steps,
+            "gpu_launches": graph_steps, "graph_steps": graph_steps,
             "cpu_baseline": {"value": pts / t_cpu, "unit": "points/s", "cores": 1, "kind": "port",
                              "sample": "the full workload, oracle chain, one thread (r=1)"}}
 

@@ -258,6 +258,9 @@ int launch_gen(GenArgs a, cudaStream_t s, const char *what)
     a.K = net::pick_K(a.mmax, ncols);
     a.col_tiles = (u32)((a.d + MAX_COLS - 1) / MAX_COLS);
     const u64 units = a.r * a.col_tiles;
+    // a small problem takes a smaller table, so that row runs of at least four table lengths
+    // still give every SM two CTAs (the high bits' XOR is redone once per 2^K rows)
+    while (a.K > 4 && units * ((a.n + (4ull << a.K) - 1) / (4ull << a.K)) < (u64)qmcgb::sm_count() * 2) a.K--;
     // enough CTAs to fill the GPU several times; each CTA covers a row run of
     // at least four table lengths so building the table stays a small cost
     const size_t smem = net::table_words(a.K, a.mmax, ncols) * sizeof(u64);
