@@ -373,15 +373,20 @@ __device__ __forceinline__ void dim_value(const HDim &D, const u32 *Cj, const u6
                     y[q][u] = done[q] ? 0ull : Yj[(t + u) * D.b + dim_mod(D, acc)];
                 }
             }
+            // the padded rows past tmax add +0, which leaves v as it is: a group that reaches past
+            // tmax (the same for the whole warp: it owns the dimension) skips those adds
+            const u32 nu = min(HT_GROUP, D.tmax - t);
             if (ADD == ADD_INT) {
 #pragma unroll
                 for (u32 u = 0; u < HT_GROUP; u++) {
+                    if (u >= nu) break;
 #pragma unroll
                     for (u32 q = 0; q < PPL; q++) add_term_int(vi[q], y[q][u]);
                 }
             } else {
 #pragma unroll
                 for (u32 u = 0; u < HT_GROUP; u++) {
+                    if (u >= nu) break;
 #pragma unroll
                     for (u32 q = 0; q < PPL; q++)
                         vd[q] = __dadd_rn(vd[q], as_double(y[q][u]));  // gdn_integer_to_float.c:37
