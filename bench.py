@@ -1461,7 +1461,7 @@ def run_nus(args):
     stw = torch.empty_like(st0)
     free, _tot = torch.cuda.mem_get_info()
     per = nus.workspace_bytes(n, 0, 1)
-    count = max(1, min(G, min(free // 3, 64 << 30) // per))
+    count = max(1, min(G, min(free // 2, 160 << 30) // per))  # every generator in one chunk where it fits
     wbytes = nus.workspace_bytes(n, 0, count)
     work = torch.empty(wbytes, dtype=torch.uint8, device="cuda")
     st = torch.cuda.current_stream()

@@ -161,7 +161,8 @@ Args:
     xrb (np.ndarray of np.uint64): array to store scrambled points of size r*n*d
 
 Keyword arguments (beyond the reference): ``workspace_bytes`` caps the
-device scratch (default: half the free device memory, at most 48 GiB);
+device scratch (default: half the free device memory, at most 160 GiB, so that every
+generator runs in one chunk with one serial draw pass where that fits);
 generators run in chunks that fit it.  ``stream`` selects a
 torch.cuda.Stream.  ``host_writes`` (default True): a numpy ``xrb`` is
 written by the kernels directly where the GPU can reach it (pinned memory,
@@ -205,7 +206,7 @@ or pageable memory through the host's page tables), else copied back."""
     budget = kwargs.get("workspace_bytes")
     if budget is None:
         free, _total = torch.cuda.mem_get_info(dev)
-        budget = min(free // 2, 48 << 30)
+        budget = min(free // 2, 160 << 30)  # one chunk, one serial draw pass, where it fits
     count = max(1, min(G, int(budget) // per))
     wbytes = workspace_bytes(n, h0, count)
     with torch.cuda.device(dev), torch.cuda.stream(stream):
