@@ -58,7 +58,10 @@ constexpr u32 FY_RING = 16;              // slots of 16 outputs (32 candidates)
 // (warps 4 and 8 leave at once) and the workers share sub-partitions 2 and 3.
 constexpr u32 FY_WORKERS = 6;  // small-base decoders
 constexpr u32 FY_THREADS = 32 * 12;
-__device__ __forceinline__ int fy_worker_of(u32 warp) { return (warp & 3) >= 2 ? (int)((warp >> 2) * 2 + (warp & 3) - 2) : -1; }
+__device__ __forceinline__ int fy_worker_of(u32 warp)
+{
+    return (warp & 3) >= 2 ? (int)((warp >> 2) * 2 + (warp & 3) - 2) : -1;
+}
 constexpr u32 FY_SMALL_MAX = 33;         // largest base of the small-base decoder
 constexpr u32 FY_SPIN_LIMIT = 1u << 26;  // polls per wait (no sleep: a sleeping warp wakes microseconds late)
 

@@ -22,8 +22,9 @@
 // nus_dev.cuh (bit-level L; the digit L is L / w); per point the number of
 // permutations it draws and their offsets; the draws, one CTA per generator
 // (the swap indices of numpy's Fisher-Yates from the stream, fy_stream.cuh),
-// then the swaps themselves, one thread per permutation; each point's digits through its owners' permutations, level by level on the way
-// up its ancestors.
+// then the swaps themselves, one thread per permutation; each point's digits
+// through its owners' permutations, level by level on the way up its
+// ancestors.
 #include "fy_stream.cuh"
 #include "nus_dev.cuh"
 
