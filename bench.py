@@ -88,6 +88,7 @@ def host_threads():
 
 
 CPU_SAMPLE_LOG2N = 18
+REF_LOG2N = LOG2N  # rows per step of the reference arm: the whole workload
 
 
 def cpu_baseline(g, shifts):
@@ -306,8 +307,9 @@ def run_reference(args):
     oracle.oracle_lib()
     g, shifts = workload_inputs()
     threads = host_threads()
-    n = 1 << CPU_SAMPLE_LOG2N
-    parts = (1 << LOG2N) // n
+    rows = 1 << REF_LOG2N
+    n = min(1 << CPU_SAMPLE_LOG2N, rows)
+    parts = rows // n
     bufs = (np.empty((R, n, D)), np.empty((R, n, D)))
 
     def step():

@@ -39,6 +39,7 @@ def _rank_main(rank, world, port, out):
     res["g_sum"] = int(g.astype(np.uint64).sum() % (1 << 61))
     # the reference arm: rank 0 runs (on a small sample) and prints one line, other ranks print nothing
     bench.CPU_SAMPLE_LOG2N = 6
+    bench.REF_LOG2N = 6
 
     class A:
         steps, warmup, gpus = 1, 3, w
