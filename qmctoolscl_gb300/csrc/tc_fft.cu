@@ -184,6 +184,63 @@ __device__ __forceinline__ void twiddle(const float2 *tab, u32 t, u32 bits, floa
     twiddle_turn(tab, t << (32 - bits), bits, sign, wr, wi);
 }
 
+__device__ __forceinline__ void cmul(float ar, float ai, float br, float bi, float &cr, float &ci)
+{
+    cr = ar * br - ai * bi;
+    ci = ar * bi + ai * br;
+}
+
+// Twiddles of one half of a radix-16 group: member pp (pp < 8) of half h has br = h + 2j with
+// j = brev3(pp), so its twiddle is T_j = u W^j with u = w^h and W = w^2, w = exp(sign 2 pi i c / 2^bits)
+// (cg = c << (32 - bits), the angle of w as a fraction of a turn).  Table lookups give W, T_5 and, on
+// the upper half, T_1 (T_1 = W on the lower one); the member pair (j, j + 4), that is pp and pp + 1,
+// then takes T_j = T_1 f_j and T_(j+4) = T_5 f_j with f_j = conj(W), 1, W, W^2 for j = 0..3.  Every
+// twiddle is a lookup times at most a square of one, so the angle error of a looked-up value is
+// carried at most twice (powers W^4 and up would carry it four times and more: about 3.5 times the
+// error per twiddle).
+struct HalfTwiddles {
+    float t1r, t1i, t5r, t5i, wr, wi, w2r, w2i;
+};
+
+__device__ __forceinline__ HalfTwiddles half_twiddles(const float2 *tab, u32 cg, u32 half, u32 bits, float sign)
+{
+    HalfTwiddles t;
+    twiddle_turn(tab, 2u * cg, bits, sign, t.wr, t.wi);
+    if (half) {
+        twiddle_turn(tab, 3u * cg, bits, sign, t.t1r, t.t1i);
+        twiddle_turn(tab, 11u * cg, bits, sign, t.t5r, t.t5i);
+    } else {  // T_1 = W
+        t.t1r = t.wr;
+        t.t1i = t.wi;
+        twiddle_turn(tab, 10u * cg, bits, sign, t.t5r, t.t5i);
+    }
+    cmul(t.wr, t.wi, t.wr, t.wi, t.w2r, t.w2i);
+    return t;
+}
+
+// the twiddles of members j and j + 4 (j < 4, known at compile time after unrolling)
+__device__ __forceinline__ void pair_twiddles(const HalfTwiddles &t, u32 j, float &ar, float &ai, float &br, float &bi)
+{
+    if (j == 1) {
+        ar = t.t1r;
+        ai = t.t1i;
+        br = t.t5r;
+        bi = t.t5i;
+        return;
+    }
+    const float fr = j == 3 ? t.w2r : t.wr, fi = j == 0 ? -t.wi : j == 3 ? t.w2i : t.wi;
+    cmul(t.t1r, t.t1i, fr, fi, ar, ai);
+    cmul(t.t5r, t.t5i, fr, fi, br, bi);
+}
+
+// bytes [p, p + bytes) of global memory into L2 by the bulk-copy unit (p 16-byte aligned, bytes a
+// multiple of 16); the issuing thread does not wait for it
+__device__ __forceinline__ void prefetch_l2(const void *p, u32 bytes)
+{
+    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"((u64)__cvta_generic_to_global(p)), "r"(bytes)
+                 : "memory");
+}
+
 // The split step matrices of the forward and the inverse FFT in operand-B layout, for the
 // fused pass that runs both kinds of step on one tile (filled by tc_stepB_kernel on the
 // caller's stream before every fused transform: the same values each time)
@@ -247,15 +304,37 @@ __global__ void __launch_bounds__(FT_THREADS, 3) tc_pass_kernel(TcPassArgs a, un
     const u32 cchl = (a.k0 == 0) ? 0 : a.k0 - ctl;       // log2 column chunks: 2^k0 / ct
     const u32 tpvl = (a.k0 == 0) ? 0 : cchl + (a.L - a.k1);  // log2 tiles per vector
     const u64 ntiles = (a.k0 == 0) ? (a.total + FT_TILE - 1) / FT_TILE : (a.total >> a.L) << tpvl;
+    // first element of tile t: pass 1 a block of 4096; later passes Q rows 2^k0 apart of ct
+    // consecutive elements
+    auto tile_base = [&](u64 t) -> u64 {
+        if (a.k0 == 0) return t * FT_TILE;
+        const u64 v = t >> tpvl, rem = t & ((1ull << tpvl) - 1);
+        return (v << a.L) + ((rem >> cchl) << a.k1) + ((rem & ((1ull << cchl) - 1)) << ctl);
+    };
+    // tile t's input into L2 while the CTA works on the tile before it, so that the load phase
+    // waits on L2 rather than HBM: pass 1 one block per array (an even count of elements from a
+    // multiple of 4096), later passes one row of ct (even) elements per thread (Q <= 256 rows);
+    // the FP32 intermediate is xr's bytes alone
+    auto prefetch_tile = [&](u64 t) {
+        if (t >= ntiles) return;
+        const u64 b0 = tile_base(t);
+        const bool both = !REAL && !a.in32;
+        if (a.k0 == 0) {
+            if (threadIdx.x == 0) {
+                const u32 bytes = (u32)(a.total - b0 < FT_TILE ? a.total - b0 : FT_TILE) * 8;
+                prefetch_l2(a.xr + b0, bytes);
+                if (both) prefetch_l2(a.xi + b0, bytes);
+            }
+        } else if (threadIdx.x < Q) {
+            const u64 f = b0 + ((u64)threadIdx.x << a.k0);
+            prefetch_l2(a.xr + f, ct * 8);
+            if (both) prefetch_l2(a.xi + f, ct * 8);
+        }
+    };
+    prefetch_tile(blockIdx.x);
 
     for (u64 tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
-        u64 base;
-        if (a.k0 == 0) {
-            base = tile * FT_TILE;
-        } else {
-            const u64 v = tile >> tpvl, rem = tile & ((1ull << tpvl) - 1);
-            base = (v << a.L) + ((rem >> cchl) << a.k1) + ((rem & ((1ull << cchl) - 1)) << ctl);
-        }
+        const u64 base = tile_base(tile);
         // load (zeros beyond the data): pairs of adjacent elements as 16-byte loads, all of a
         // thread's raw bits in flight before the conversions (whose rare out-of-line fallback
         // would otherwise serialise the loads).  Q * ct is even and ct is 1 (pass 1) or even,
@@ -305,6 +384,7 @@ __global__ void __launch_bounds__(FT_THREADS, 3) tc_pass_kernel(TcPassArgs a, un
             }
         }
         __syncthreads();
+        prefetch_tile(tile + gridDim.x);
         // the steps over the pass's bits for step kind SK (FFT, IFFT or WHT): false when a wait ran out
         auto steps = [&](auto skc) -> bool {
             constexpr int SK = decltype(skc)::value;
@@ -367,29 +447,23 @@ __global__ void __launch_bounds__(FT_THREADS, 3) tc_pass_kernel(TcPassArgs a, un
                         // half*8 + p (p < 8) has br = 2*brev3(p) + half, so its twiddle angle as a
                         // fraction of a turn is J = cg*half + 2*cg*brev3(p) with cg = c << (28 - k)
                         const u32 cgrp = ((u32)base + (qlo << a.k0) + cc) & ((1u << k) - 1);
-                        const u32 cg = cgrp << (28 - k), cgh = half ? cg : 0u;
+                        const u32 cg = cgrp << (28 - k);
                         u32 pr[3][4], pim[3][4];  // [split][pair of members]: two BF16 per word
-                        // member pp+1's twiddle is member pp's times w^8 (its angle is 8*cg more): one
-                        // table lookup per pair, plus w^8 once, and one complex product
-                        float w8r = 1.0f, w8i = 0.0f;
-                        if (SK == TC_FFT && k > 0) twiddle_turn(tab, 8u * cg, k + 4, -1.0f, w8r, w8i);
+                        // members pp, pp+1 (pp even) have j = brev3(pp) < 4 and j + 4
+                        HalfTwiddles tw{};
+                        if (SK == TC_FFT && k > 0) tw = half_twiddles(tab, cg, half, k + 4, -1.0f);
 #pragma unroll
                         for (u32 pp = 0; pp < 8; pp += 2) {
-                            float xr2[2], xi2[2];
-                            float wr = 1.0f, wi = 0.0f;
-                            if (SK == TC_FFT && k > 0 && (half || pp))
-                                twiddle_turn(tab, cgh + 2u * cg * (brev4(pp) >> 1), k + 4, -1.0f, wr, wi);
+                            float xr2[2], xi2[2], pwr[2] = {1.0f, 1.0f}, pwi[2] = {0.0f, 0.0f};
+                            const u32 jj = ((pp >> 1) & 1u) * 2u + ((pp >> 2) & 1u);  // brev3(pp)
+                            if (SK == TC_FFT && k > 0) pair_twiddles(tw, jj, pwr[0], pwi[0], pwr[1], pwi[1]);
 #pragma unroll
                             for (u32 h = 0; h < 2; h++) {
                                 const u32 e = slot(e0 + (pp + h) * S);
                                 xr2[h] = sr[e];
                                 xi2[h] = (SK == TC_WHT) ? 0.0f : si[e];
                                 if (SK == TC_FFT && k > 0) {  // pre-twiddle w^br(p) (w = 1 on the first step)
-                                    if (h) {
-                                        const float t = wr * w8r - wi * w8i;
-                                        wi = wr * w8i + wi * w8r;
-                                        wr = t;
-                                    }
+                                    const float wr = pwr[h], wi = pwi[h];
                                     const float tr = xr2[h] * wr - xi2[h] * wi;
                                     xi2[h] = xr2[h] * wi + xi2[h] * wr;
                                     xr2[h] = tr;
@@ -482,23 +556,22 @@ __global__ void __launch_bounds__(FT_THREADS, 3) tc_pass_kernel(TcPassArgs a, un
                         const u32 S = (1u << lo) * ct;
                         const u32 e0 = (qlo | (qhi << (lo + 4))) * ct + cc + half * 8 * S;
                         const u32 cgrp = ((u32)base + (qlo << a.k0) + cc) & ((1u << k) - 1);
-                        const u32 cg = cgrp << (28 - k), cgh = half ? cg : 0u;
+                        const u32 cg = cgrp << (28 - k);
                         if (k > 0) {
-                            float w8r, w8i, wr = 1.0f, wi = 0.0f;  // as in the forward step: w^8 per pair
-                            twiddle_turn(tab, 8u * cg, k + 4, 1.0f, w8r, w8i);
+                            const HalfTwiddles tw = half_twiddles(tab, cg, half, k + 4, 1.0f);  // as in the forward step
 #pragma unroll
-                            for (u32 pp = 0; pp < 8; pp++) {
-                                const u32 e = slot(e0 + pp * S);
-                                if (pp & 1) {
-                                    const float t = wr * w8r - wi * w8i;
-                                    wi = wr * w8i + wi * w8r;
-                                    wr = t;
-                                } else if (half || pp) {
-                                    twiddle_turn(tab, cgh + 2u * cg * (brev4(pp) >> 1), k + 4, 1.0f, wr, wi);
+                            for (u32 pp = 0; pp < 8; pp += 2) {
+                                const u32 jj = ((pp >> 1) & 1u) * 2u + ((pp >> 2) & 1u);  // brev3(pp)
+                                float pwr[2], pwi[2];
+                                pair_twiddles(tw, jj, pwr[0], pwi[0], pwr[1], pwi[1]);
+#pragma unroll
+                                for (u32 h = 0; h < 2; h++) {
+                                    const u32 e = slot(e0 + (pp + h) * S);
+                                    const float wr = pwr[h], wi = pwi[h];
+                                    const float xr_ = sr[e], xi_ = si[e];
+                                    sr[e] = xr_ * wr - xi_ * wi;
+                                    si[e] = xr_ * wi + xi_ * wr;
                                 }
-                                const float xr_ = sr[e], xi_ = si[e];
-                                sr[e] = xr_ * wr - xi_ * wi;
-                                si[e] = xr_ * wi + xi_ * wr;
                             }
                         }
                         __syncthreads();
