@@ -546,8 +546,14 @@ __global__ void __launch_bounds__(FT_THREADS, 3) tc_pass_kernel(TcPassArgs a, un
                             }
                         }
                     }
-                    tc::fence_before_sync();
-                    __syncthreads();
+                    // the next M-tile's operand build reads only its own groups' elements, and its
+                    // MMAs (which overwrite the accumulators read here) start after the barrier that
+                    // follows the build: only the last M-tile of a step, and the inverse step's
+                    // post-twiddle (other threads' outputs), need a barrier here
+                    if (SK == TC_IFFT || mt + 1 == FT_GROUPS / 128) {
+                        tc::fence_before_sync();
+                        __syncthreads();
+                    }
                     if (SK == TC_IFFT) {
                         // post-twiddle w^-br(q) of the inverse step
                         const u32 gi = 128 * mt + (threadIdx.x & 127), half = threadIdx.x >> 7;
