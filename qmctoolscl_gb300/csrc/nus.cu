@@ -73,12 +73,15 @@ __global__ void nus_keys_kernel(NusDims m, const u64 *__restrict__ xb, const u64
 // ---- 2-3. the radix sort and the bottom-up tree pass: nus_dev.cuh -------------------
 
 // ---- 4. the draws, one thread per generator --------------------------------------
-// One thread per generator.  L_v comes in 16 at a time (one 16-byte load per
-// group, rows start 16-byte aligned), three groups ahead of the draws.  A
-// group whose 16 draws are all 64-bit draws (33..63 bits) or all 32-bit
-// draws (1..32 bits), the usual case, runs unrolled without a branch per
-// draw; any other group (the first and last, repeated keys, mixed widths)
-// takes the general path.
+// One thread per generator, 32 generators (rows of the draw array) per warp.  L_v
+// comes in 16 at a time (one 16-byte load per group, rows start 16-byte aligned),
+// three groups ahead of the draws.  A group whose 16 draws are all 64-bit draws
+// (33..63 bits) or all 32-bit draws (1..32 bits), the usual case, runs unrolled
+// without a branch per draw, its draws kept in registers; the warp then writes
+// every such row's 128 bytes through shared memory, each 16-byte store
+// instruction covering four rows' whole lines (a thread storing its own row would
+// touch 32 lines per instruction).  Any other group (the first and last, repeated
+// keys, mixed widths) takes the general path and stores its draws one by one.
 
 // the top nb bits (33 <= nb <= 63) of a 64-bit output: a right shift by 64 - nb < 32
 __device__ __forceinline__ u64 top_bits64(u64 x, u32 nb)
@@ -106,57 +109,68 @@ constexpr int DRAW_AHEAD = 4;
 __global__ void __launch_bounds__(32) nus_draw_kernel(NusDims m, u64 *__restrict__ states,
                                                       const unsigned char *__restrict__ Lv, u64 *__restrict__ draw)
 {
-    const u32 g = blockIdx.x * blockDim.x + threadIdx.x;
-    if (g >= m.S) return;
-    u64 *st = states + (m.s0 + g) * 6;
-    Sfc64 r{st[0], st[1], st[2], st[3], st[5], (u32)(st[4] != 0)};
-    const u64 off = (u64)g * m.NP;
+    // a warp's 32 rows of one group, 128 bytes each plus 16 of padding (the rows' 16-byte
+    // chunks then fall in different banks)
+    __shared__ uint4 stage[32][9];
+    const u32 lane = threadIdx.x, g0 = blockIdx.x * 32, g = g0 + lane;
+    const bool active = g < m.S;  // lanes past the last generator stay for the warp's stores
+    u64 *st = states + (u64)(active ? m.s0 + g : 0) * 6;
+    Sfc64 r{0, 0, 0, 0, 0, 0};
+    if (active) r = Sfc64{st[0], st[1], st[2], st[3], st[5], (u32)(st[4] != 0)};
+    const u64 off = (u64)(active ? g : 0) * m.NP;
     const int T = (int)m.T;
     u64 *D = draw + off;
-    if (m.fresh) D[0] = r.bits((u32)T);
+    if (active && m.fresh) D[0] = r.bits((u32)T);
     const uint4 *L4 = reinterpret_cast<const uint4 *>(Lv + off);
     const u32 gend = (m.N + 15) >> 4;  // groups covering [0, N); NP keeps the last one in the row
     u32 gq = m.H0 >> 4;
     uint4 ring[DRAW_AHEAD];
 #pragma unroll
-    for (int k = 0; k < DRAW_AHEAD; k++) ring[k] = gq + k < gend ? L4[gq + k] : make_uint4(0, 0, 0, 0);
-    for (; gq < gend; gq++) {
+    for (int k = 0; k < DRAW_AHEAD; k++)
+        ring[k] = (active && gq + k < gend) ? L4[gq + k] : make_uint4(0, 0, 0, 0);
+    for (; gq < gend; gq++) {  // the same groups in every lane
         const uint4 cur = ring[0];
 #pragma unroll
         for (int k = 0; k < DRAW_AHEAD - 1; k++) ring[k] = ring[k + 1];
-        ring[DRAW_AHEAD - 1] = gq + DRAW_AHEAD < gend ? L4[gq + DRAW_AHEAD] : make_uint4(0, 0, 0, 0);
+        ring[DRAW_AHEAD - 1] = (active && gq + DRAW_AHEAD < gend) ? L4[gq + DRAW_AHEAD] : make_uint4(0, 0, 0, 0);
         const u32 w[4] = {cur.x, cur.y, cur.z, cur.w};
         const u32 v0 = gq << 4;
-        const bool inside = v0 >= m.H0 && v0 + 16 <= m.N;
+        const bool inside = active && v0 >= m.H0 && v0 + 16 <= m.N;
         const int lmax = (int)max_byte(cur), lmin = (int)min_byte(cur);
+        u64 y[16];
+        bool staged = false;
         if (inside && lmax <= T - 34) {  // 16 draws of T-1-L in [33, 63] bits
 #pragma unroll
-            for (int e = 0; e < 16; e++) D[v0 + e] = top_bits64(r.next64(), (u32)(T - 1) - byte_of(w, e));
+            for (int e = 0; e < 16; e++) y[e] = top_bits64(r.next64(), (u32)(T - 1) - byte_of(w, e));
+            staged = true;
         } else if (inside && lmin >= T - 33 && lmax <= T - 2) {  // 16 draws of 1..32 bits
-            const u32 sh0 = 32u - ((u32)(T - 1) - byte_of(w, 0));
-            int e0 = 0;
-            if (r.has) {  // the buffered half first, then pairs, the last output's high half kept
-                D[v0] = (u32)r.half >> sh0;
-                e0 = 1;
-            }
+            // a draw of nb bits is the top nb bits of a 32-bit half: numpy's buffered half first,
+            // then both halves of each output, low first; the last output's high half is kept
+#define NUS_SH(e) (32u - ((u32)(T - 1) - byte_of(w, (e))))
+            if (r.has) {
+                y[0] = (u32)r.half >> NUS_SH(0);
 #pragma unroll
-            for (int e = 0; e < 16; e += 2) {
-                if (e + e0 + 1 < 16) {
+                for (int e = 1; e < 15; e += 2) {
                     const u64 x = r.next64();
-                    D[v0 + e + e0] = (u32)x >> (32u - ((u32)(T - 1) - byte_of(w, e + e0)));
-                    D[v0 + e + e0 + 1] = (u32)(x >> 32) >> (32u - ((u32)(T - 1) - byte_of(w, e + e0 + 1)));
-                    r.half = x >> 32;
+                    y[e] = (u32)x >> NUS_SH(e);
+                    y[e + 1] = (u32)(x >> 32) >> NUS_SH(e + 1);
                 }
-            }
-            if (e0) {  // 15 draws after the buffered one: the last takes a low half
                 const u64 x = r.next64();
-                D[v0 + 15] = (u32)x >> (32u - ((u32)(T - 1) - byte_of(w, 15)));
+                y[15] = (u32)x >> NUS_SH(15);
                 r.half = x >> 32;
                 r.has = 1;
             } else {
-                r.has = 0;
+#pragma unroll
+                for (int e = 0; e < 16; e += 2) {
+                    const u64 x = r.next64();
+                    y[e] = (u32)x >> NUS_SH(e);
+                    y[e + 1] = (u32)(x >> 32) >> NUS_SH(e + 1);
+                    r.half = x >> 32;
+                }
             }
-        } else {
+#undef NUS_SH
+            staged = true;
+        } else if (active) {
 #pragma unroll 1
             for (int e = 0; e < 16; e++) {
                 const u32 v = v0 + e;
@@ -166,7 +180,27 @@ __global__ void __launch_bounds__(32) nus_draw_kernel(NusDims m, u64 *__restrict
                 }
             }
         }
+        if (staged) {
+#pragma unroll
+            for (int c = 0; c < 8; c++)
+                stage[lane][c] = make_uint4((u32)y[2 * c], (u32)(y[2 * c] >> 32), (u32)y[2 * c + 1],
+                                            (u32)(y[2 * c + 1] >> 32));
+        }
+        const u32 rows = __ballot_sync(0xFFFFFFFFu, staged);
+        __syncwarp();
+        if (rows) {
+            // store i: rows 4i .. 4i+3, eight lanes (16 bytes each) per row
+            const u32 c = lane & 7;
+#pragma unroll
+            for (int i = 0; i < 8; i++) {
+                const u32 R = 4 * i + (lane >> 3);
+                if ((rows >> R) & 1u)
+                    *reinterpret_cast<uint4 *>(draw + (u64)(g0 + R) * m.NP + v0 + 2 * c) = stage[R][c];
+            }
+        }
+        __syncwarp();
     }
+    if (!active) return;
     st[0] = r.a;
     st[1] = r.b;
     st[2] = r.c;
