@@ -408,10 +408,12 @@ int qmc_dnb2_nested_uniform_scramble(uint64_t r, uint64_t n, uint64_t d, uint64_
         u32 *vfree = nullptr;
         if (n > 0) {
             const dim3 tg((unsigned)((NT + NUS_WARPS - 1) / NUS_WARPS), m.S);
+            if (int rc2 = qmcgb::raise_smem_limit((const void *)nus_scatter_kernel, NUS_SCATTER_SMEM, "dnb2_nus sort"))
+                return rc2;
             auto pass = [&](const u64 *kin, const u32 *vin, u32 digit, u64 *kout, u32 *vout) {
                 nus_hist_kernel<<<tg, NUS_THREADS, 0, st>>>(m, kin, 8 * digit, w.cnt);
                 nus_scan_kernel<<<m.S, 1024, 0, st>>>(m, w.cnt);
-                nus_scatter_kernel<<<tg, NUS_THREADS, 0, st>>>(m, kin, vin, 8 * digit, w.cnt, kout, vout);
+                nus_scatter_kernel<<<tg, NUS_THREADS, NUS_SCATTER_SMEM, st>>>(m, kin, vin, 8 * digit, w.cnt, kout, vout);
                 return qmcgb::launch_status("dnb2_nus sort");
             };
             // the top digits only: enough for keys that differ in their

@@ -30,8 +30,11 @@ struct NusDims {
 // ---- stable LSD radix sort, 8 bits per pass -----------------------------------
 // Each warp owns a tile of WT consecutive entries of one generator.  Pass:
 // per-tile digit counts, a per-generator exclusive scan over (digit, tile),
-// then each warp scatters its tile in order (ranks among equal digits from
-// __match_any_sync), so equal digits keep their order.
+// then each warp sorts its tile by digit in shared memory (ranks among equal
+// digits from __match_any_sync, so equal digits keep their order) and writes
+// it out in that order: a digit's entries of one tile (about WT/256) land in
+// consecutive output slots, so a warp's store covers a few runs of
+// consecutive addresses instead of 32 scattered ones.
 
 __global__ void __launch_bounds__(NUS_THREADS) nus_hist_kernel(NusDims m, const u64 *__restrict__ key, u32 shift,
                                                                u32 *__restrict__ cnt)
@@ -83,16 +86,50 @@ __global__ void __launch_bounds__(1024) nus_scan_kernel(NusDims m, u32 *__restri
     }
 }
 
+// shared memory of the scatter: per warp the tile's output offsets and staging slots per digit
+// (2 x 256 words), then the tile's entries in digit order as indices into the tile (WT x 2 bytes)
+constexpr size_t NUS_SCATTER_WARP_BYTES = 2 * 256 * 4 + (size_t)WT * 2;
+constexpr size_t NUS_SCATTER_SMEM = NUS_WARPS * NUS_SCATTER_WARP_BYTES;
+
 __global__ void __launch_bounds__(NUS_THREADS) nus_scatter_kernel(NusDims m, const u64 *__restrict__ kin,
                                                                   const u32 *__restrict__ vin, u32 shift,
                                                                   const u32 *__restrict__ cnt, u64 *__restrict__ kout,
                                                                   u32 *__restrict__ vout)
 {
-    __shared__ u32 base[NUS_WARPS][256];
+    extern __shared__ __align__(16) unsigned char nus_sc_smem[];
     const u32 w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    unsigned char *ws = nus_sc_smem + w * NUS_SCATTER_WARP_BYTES;
+    u32 *delta = (u32 *)ws;            // [256] output slot of staged slot j of digit dg: delta[dg] + j
+    u32 *lpos = delta + 256;           // [256] the digit's next staging slot
+    unsigned short *sx = (unsigned short *)(lpos + 256);  // [WT] the tile's entries in digit order
     const u32 tile = blockIdx.x * NUS_WARPS + w, g = blockIdx.y;
     if (tile >= m.NT) return;  // whole warps leave; nothing below synchronises the block
-    for (u32 dg = lane; dg < 256; dg += 32) base[w][dg] = cnt[((u64)g * 256 + dg) * m.NT + tile];
+    // the tile's count of digit dg is the next (digit, tile) offset of the exclusive scan minus
+    // its own (the last of all ends at N); lane L takes digits 8L .. 8L+7
+    const u64 cb = (u64)g * 256 * m.NT;
+    u32 b0[8], c8[8], sum = 0;
+#pragma unroll
+    for (int k = 0; k < 8; k++) {
+        const u32 dg = lane * 8 + k;
+        const u64 idx = cb + (u64)dg * m.NT + tile;
+        b0[k] = cnt[idx];
+        const u32 b1 = (dg == 255 && tile == m.NT - 1) ? m.N : cnt[idx + 1];
+        c8[k] = b1 - b0[k];
+        sum += c8[k];
+    }
+    u32 incl = sum;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const u32 y = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+        if (lane >= (u32)o) incl += y;
+    }
+    u32 run = incl - sum;  // first staging slot of digit 8L
+#pragma unroll
+    for (int k = 0; k < 8; k++) {
+        lpos[lane * 8 + k] = run;
+        delta[lane * 8 + k] = b0[k] - run;  // mod 2^32: delta + j is the output slot
+        run += c8[k];
+    }
     __syncwarp();
     const u64 off = (u64)g * m.NP;
     const u32 beg = tile * WT, end = min(beg + WT, m.N);
@@ -100,18 +137,22 @@ __global__ void __launch_bounds__(NUS_THREADS) nus_scatter_kernel(NusDims m, con
         const u32 p = p0 + lane;
         const bool ok = p < end;
         const u64 k = ok ? kin[off + p] : 0;
-        const u32 v = ok ? (vin ? vin[off + p] : p) : 0;
         const u32 dg = ok ? ((u32)(k >> shift) & 255u) : 256u + lane;  // idle lanes match nobody
         const u32 peers = __match_any_sync(0xFFFFFFFFu, dg);
         const u32 rank = __popc(peers & ((1u << lane) - 1u));
-        const u32 pos = ok ? base[w][dg] + rank : 0;
+        const u32 slot = ok ? lpos[dg] + rank : 0;
         __syncwarp();
-        if (ok && rank == 0) base[w][dg] += __popc(peers);
+        if (ok && rank == 0) lpos[dg] += __popc(peers);
+        if (ok) sx[slot] = (unsigned short)(p - beg);
         __syncwarp();
-        if (ok) {
-            kout[off + pos] = k;
-            vout[off + pos] = v;
-        }
+    }
+    // the key and value again from the tile the warp has just read (still in L1)
+    for (u32 j = lane; j < end - beg; j += 32) {
+        const u32 p = beg + sx[j];
+        const u64 k = kin[off + p];
+        const u32 pos = delta[(u32)(k >> shift) & 255u] + j;
+        kout[off + pos] = k;
+        vout[off + pos] = vin ? vin[off + p] : p;
     }
 }
 
