@@ -52,37 +52,46 @@ __global__ void __launch_bounds__(NUS_THREADS) nus_hist_kernel(NusDims m, const 
     for (u32 dg = lane; dg < 256; dg += 32) cnt[((u64)g * 256 + dg) * m.NT + tile] = h[w][dg];
 }
 
+// Exclusive scan of one generator's 256 * NT counts per block: each warp takes a contiguous
+// segment, sums it (lanes on consecutive words), and after a scan of the 32 warp sums scans
+// its segment in rows of 32 consecutive words (five shuffles a row, the running total carried)
 __global__ void __launch_bounds__(1024) nus_scan_kernel(NusDims m, u32 *__restrict__ cnt)
 {
     __shared__ u32 wsum[32];
     const u64 total = 256ull * m.NT;
     u32 *c = cnt + (u64)blockIdx.x * total;
-    const u64 per = (total + 1023) / 1024;
-    const u64 beg = min((u64)threadIdx.x * per, total), end = min(beg + per, total);
-    u32 sum = 0;
-    for (u64 k = beg; k < end; k++) sum += c[k];
     const u32 lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    u32 incl = sum;
-    for (int o = 1; o < 32; o <<= 1) {
-        const u32 y = __shfl_up_sync(0xFFFFFFFFu, incl, o);
-        if (lane >= (u32)o) incl += y;
-    }
-    if (lane == 31) wsum[w] = incl;
+    const u64 per = ((total + 31) / 32 + 31) & ~31ull;  // a warp's segment, whole rows of 32
+    const u64 beg = min((u64)w * per, total), end = min(beg + per, total);
+    u32 sum = 0;
+    for (u64 k = beg + lane; k < end; k += 32) sum += c[k];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xFFFFFFFFu, sum, o);
+    if (lane == 0) wsum[w] = sum;
     __syncthreads();
     if (w == 0) {
-        u32 x = wsum[lane];
+        const u32 x0 = wsum[lane];
+        u32 x = x0;
+#pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
             const u32 y = __shfl_up_sync(0xFFFFFFFFu, x, o);
             if (lane >= (u32)o) x += y;
         }
-        wsum[lane] = x;
+        wsum[lane] = x - x0;  // exclusive: the counts before warp `lane`'s segment
     }
     __syncthreads();
-    u32 run = incl - sum + (w ? wsum[w - 1] : 0u);
-    for (u64 k = beg; k < end; k++) {
-        const u32 t = c[k];
-        c[k] = run;
-        run += t;
+    u32 run = wsum[w];
+    for (u64 r0 = beg; r0 < end; r0 += 32) {
+        const u64 k = r0 + lane;
+        const u32 t = k < end ? c[k] : 0u;
+        u32 incl = t;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const u32 y = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+            if (lane >= (u32)o) incl += y;
+        }
+        if (k < end) c[k] = run + incl - t;
+        run += __shfl_sync(0xFFFFFFFFu, incl, 31);
     }
 }
 
