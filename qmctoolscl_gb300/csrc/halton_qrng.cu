@@ -12,10 +12,14 @@
 // point with m digits.  Each CTA owns one dimension and computes, once, the
 // prefix P[m] after the steps k = 31 .. m (P[0] is the reference's point 0);
 // a point then needs only its own m steps, each the reference's rounded add
-// and divide -- in integer arithmetic (qrng_step.cuh), because on GB300 an
-// FP64 divide is a sequence of several operations on the narrow FP64 pipe.
-// The digits come from the top down by divisions by b^k (32-bit
-// multiply-high, exact).
+// and divide.  Three warps in four take them in integer arithmetic
+// (qrng_step.cuh), the fourth on the FP64 unit as the reference's own two
+// operations: on GB300 an FP64 divide is a sequence of several operations on a
+// narrow pipe, so neither kind of unit alone keeps up, and the two run side by
+// side (n = 2^20, d = 100: 2.82 ms with integer steps only, 2.51 ms with a
+// quarter of the warps on FP64; a third, a fifth, a sixth, or the FP64 warps
+// spread over the SM's sub-partitions, measured slower).  The digits come from
+// the top down by divisions by b^k (32-bit multiply-high, exact).
 #include "common.cuh"
 #include "qrng_step.cuh"
 
@@ -131,6 +135,7 @@ __global__ void __launch_bounds__(QRNG_THREADS, 8) halton_qrng_kernel(int n, int
     double *out = res + (u64)j * (u64)n;
     for (u64 q = (u64)blockIdx.x * QRNG_THREADS + threadIdx.x; q < (u64)n; q += (u64)gridDim.x * QRNG_THREADS) {
         const u32 t = (u32)(int)((long long)n0 + (long long)q);  // halton_qrng.c:110: tmp = i
+        const bool fp64 = ((q >> 5) & 3u) == 0;                   // the warp's steps on the FP64 unit
         int m = 0;  // base-b digit count of t (at most 32)
         while (m < 32 && pwv[m + 1] <= (u64)t && pwv[m + 1] < (1ull << 32)) m++;
         if (t) m++;
@@ -140,7 +145,7 @@ __global__ void __launch_bounds__(QRNG_THREADS, 8) halton_qrng_kernel(int n, int
             const u32 dig = top - fd_div(fb, top) * (u32)b;  // its lowest digit: digit k of t
             const u32 c = fd_mod(fb, f * dig + s[k]);       // halton_qrng.c:135
             u64 o;                                          // halton_qrng.c:135-136: v = RN(RN(v + c) / b)
-            if (!qstep::step(v, c, qd, o)) o = qrng_step_hw(v, c, bd);
+            if (fp64 || !qstep::step(v, c, qd, o)) o = qrng_step_hw(v, c, bd);
             v = o;
         }
         out[q] = __longlong_as_double((long long)v);
@@ -162,8 +167,14 @@ int qmc_halton_qrng(int n, int d, int n0, int generalized, double *res, const do
     QMC_REQUIRE(res && randu_d_32 && dvec, "halton_qrng: null array pointer");
     unsigned *err = qmcgb::device_error_ptr();
     QMC_REQUIRE(err, "device error word unavailable");
-    const unsigned gx = qmcgb::grid_for((u64)n, QRNG_THREADS,
-                                        (unsigned)(qmcgb::sm_count() * 8 / (d < 8 ? d : 8) + 1));
+    // about four waves of CTAs (eight per SM) over all dimensions, at least 64 per dimension:
+    // every CTA builds its dimension's tables first (a serial chain of FP64 divides), so
+    // fewer, longer CTAs cost less than one per few points (153 per dimension at d = 100
+    // measured 3 % slower than 64)
+    unsigned per_dim = (unsigned)(qmcgb::sm_count() * 8 * 4 / d);
+    if (per_dim < 64) per_dim = 64;
+    if (per_dim > (unsigned)qmcgb::sm_count() * 8) per_dim = (unsigned)qmcgb::sm_count() * 8;
+    const unsigned gx = qmcgb::grid_for((u64)n, QRNG_THREADS, per_dim);
     halton_qrng_kernel<<<dim3(gx, (unsigned)d, 1), QRNG_THREADS, 0, QMC_STREAM(s)>>>(n, n0, generalized, res,
                                                                                        randu_d_32, dvec, err);
     return qmcgb::launch_status("halton_qrng");
