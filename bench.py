@@ -1436,8 +1436,10 @@ def run_qrng(args):
             "config": {"workload": "halton_qrng, generalized, n=2^%d, d=100 (first 100 primes)" % (n.bit_length() - 1),
                        "n": n, "d": d, "l2": "%.0f MB output per step" % (8 * n * d / 1e6)},
             "roofline": dict(roofline(8.0 * n * d, ms), kernel="halton_qrng_kernel",
-                             note="bound by the FP64 unit: each digit step is the reference's rounded add and "
-                                  "divide (a divide is several FP64 operations), not by HBM"),
+                             note="bound by instruction issue on two units, not by HBM: each digit step is the "
+                                  "reference's rounded add and divide, a quarter of the warps on the FP64 pipe and "
+                                  "the rest in integer arithmetic (ncu: FP64 pipe 64 %, ALU 63 %, issue 76 %; "
+                                  "profiles/halton_qrng_kernel_n2p20_d100.md)"),
             "gpu_launches": args.steps,
             "cpu_baseline": {"value": ns / t_cpu, "unit": "points/s (d=100)", "cores": threads, "kind": "port",
                              "sample": "2^%d points of all 100 dimensions, one dimension per thread, by the oracle "
