@@ -84,6 +84,17 @@ __device__ __forceinline__ double to_f64(float v)
     return fpc::f32_to_f64_bits(__float_as_uint(v), o) ? __longlong_as_double((long long)o) : f32_to_f64_hw(v);
 }
 
+// The same conversions on the FP64 unit or in integer arithmetic (the same bits either way).  The
+// passes are bound by instruction issue and leave the FP64 pipe idle, so half the loads' and
+// stores' rounds (chosen the same in every lane of a warp) convert there: none 14.64 ms for the
+// 4096-vector bench, half 14.40, three quarters 14.43, all 14.56
+__device__ __forceinline__ float to_f32_on(u64 b, bool fp64_unit)
+{
+    return fp64_unit ? __double2float_rn(__longlong_as_double((long long)b)) : to_f32(b);
+}
+
+__device__ __forceinline__ double to_f64_on(float v, bool fp64_unit) { return fp64_unit ? (double)v : to_f64(v); }
+
 struct TcPassArgs {
     u64 total;       // nvec * n values
     u32 L;           // log2 n
@@ -374,11 +385,12 @@ __global__ void __launch_bounds__(FT_THREADS, 3) tc_pass_kernel(TcPassArgs a, un
             for (u32 i = 0; i < PAIRS; i++) {
                 const u32 e = 2 * (threadIdx.x + i * FT_THREADS);
                 if (e < Q * ct) {
-                    sr[slot(e)] = to_f32(br[i].x);
-                    sr[slot(e + 1)] = to_f32(br[i].y);
+                    const bool hw = (i & 1u) == 0;  // even rounds on the FP64 unit
+                    sr[slot(e)] = to_f32_on(br[i].x, hw);
+                    sr[slot(e + 1)] = to_f32_on(br[i].y, hw);
                     if (!REAL) {
-                        si[slot(e)] = to_f32(bi[i].x);
-                        si[slot(e + 1)] = to_f32(bi[i].y);
+                        si[slot(e)] = to_f32_on(bi[i].x, hw);
+                        si[slot(e + 1)] = to_f32_on(bi[i].y, hw);
                     }
                 }
             }
@@ -644,10 +656,13 @@ __global__ void __launch_bounds__(FT_THREADS, 3) tc_pass_kernel(TcPassArgs a, un
                 if (f < a.total)
                     *(float4 *)(a.xr + f) = make_float4(sr[slot(e)], si[slot(e)], sr[slot(e + 1)], si[slot(e + 1)]);
             } else if (f < a.total) {
-                *(double2 *)(a.xr + f) = make_double2(to_f64(sr[slot(e)] * a.scale), to_f64(sr[slot(e + 1)] * a.scale));
+                static_assert(2 * FT_THREADS == 512, "the store loop's round is e >> 9");
+                const bool hw = ((e >> 9) & 1u) == 0;  // the loop's round, the same in a warp: even ones on FP64
+                *(double2 *)(a.xr + f) =
+                    make_double2(to_f64_on(sr[slot(e)] * a.scale, hw), to_f64_on(sr[slot(e + 1)] * a.scale, hw));
                 if (!REAL)
                     *(double2 *)(a.xi + f) =
-                        make_double2(to_f64(si[slot(e)] * a.scale), to_f64(si[slot(e + 1)] * a.scale));
+                        make_double2(to_f64_on(si[slot(e)] * a.scale, hw), to_f64_on(si[slot(e + 1)] * a.scale, hw));
             }
         }
         __syncthreads();
