@@ -47,8 +47,8 @@ PROFILE_LOG2N = 16  # --small: the same kernel on 512 MiB of output, for ncu cap
 SEED = 2
 FALLBACK_HBM_GBS = 6800.0
 # DRAM bytes / algorithmic bytes of the two captured tensor-core FFT passes (n = 2^20, 24
-# vectors, 48 B per sample): (403.9 + 154.9 + 202.2 + 341.6) MB / 1208.0 MB
-TC_FFT_TRAFFIC_RATIO = 0.9127
+# vectors, 48 B per sample): (403.5 + 155.5 + 202.1 + 341.8) MB / 1208.0 MB
+TC_FFT_TRAFFIC_RATIO = 0.9131
 
 
 def workload_inputs(seed=SEED):
