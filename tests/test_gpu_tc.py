@@ -53,8 +53,11 @@ def _bitrev(m):
     return out
 
 
+# (11, 7, 143): 501 tiles of 4096 values, more than the grid's CTAs and the last one half full, so a
+# CTA prefetches a partial tile while it works on a full one
 @pytest.mark.parametrize("m,d1,d2", [(1, 1, 1), (4, 2, 3), (5, 1, 1), (8, 3, 5), (10, 2, 2), (11, 1, 3), (12, 2, 1),
-                                     (13, 1, 2), (16, 1, 1), (17, 2, 1), (20, 1, 1), (22, 1, 1), (24, 1, 1)])
+                                     (13, 1, 2), (16, 1, 1), (17, 2, 1), (20, 1, 1), (22, 1, 1), (24, 1, 1),
+                                     (11, 7, 143)])
 def test_tc_fft_and_inverse_against_numpy(m, d1, d2):
     from qmctoolscl_gb300 import tc_fft
     rng = np.random.Generator(np.random.SFC64(m))
@@ -97,7 +100,8 @@ def _ifft_bro_np(X, br):
 @pytest.mark.parametrize("m,d1,d2,per_element,divide", [(1, 1, 1, False, False), (5, 2, 1, False, False),
                                                         (10, 1, 3, True, False), (12, 2, 2, False, True),
                                                         (13, 1, 2, False, False), (16, 1, 1, True, True),
-                                                        (20, 1, 1, False, False), (22, 1, 1, False, True)])
+                                                        (20, 1, 1, False, False), (22, 1, 1, False, True),
+                                                        (11, 7, 143, False, False)])
 def test_tc_fft_mul_ifft_against_numpy(m, d1, d2, per_element, divide):
     """y <- IFFT(FFT(y) * lam) * s (or / lam) in one call against numpy: one, two and three
     passes, lam shared or per element, product and quotient."""
